@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Real-time factor of the per-gulp FRB search on GB300.
+
+Workload (the configuration the headline metric is quoted on): one beam of
+uint8 filterbank, 2048 channels over 375-468.75 MHz, tsamp 0.524288 ms,
+gulps of 65536 samples (34.36 s of sky) with max-delay overlap, DM 0-2000
+at smearing tolerance 1.25 (2501 trials), smoothing widths 1..256, 7 sigma.
+A step is one gulp through the whole path: flag + normalise + requantise,
+dedisperse, smooth + standardise, find peaks, rewind.  Synthetic seeded
+data (noise with bandpass slope, RFI channels, spikes, 8 dispersed bursts).
+
+value: beam-seconds searched per wall second with the gulp already in HBM
+(CUDA events on the search stream).  e2e: the same through the public C ABI
+(hella_process_gulp) from pinned host memory, H2D of the gulp and D2H of
+the candidates inside the timed region, with per-gulp p50/p99 latency.
+
+--impl reference: the reference path's CPU implementation (the oracle
+port; the reference itself has no CPU path and does not build here) on the
+host cores, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "casm-hella_gb300"))
+
+WORKLOAD = ("full single beam: 2048 ch 375-468.75 MHz, tsamp 0.524288 ms, gulp 65536, "
+            "DM 0-2000 tol 1.25, widths 1-256, 7 sigma")
+METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp latency"
+UNIT = "beam·s/s"
+
+
+def args_():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+# ------------------------------------------------------------- workload
+
+def workload(rank: int, ngulps: int = 3):
+    import synth
+
+    params, sky = synth.config_full(seed=2 + rank)
+    gulps = [sky.gulp(g, params["gulp"]) for g in range(ngulps)]
+    return params, sky, gulps
+
+
+def cpu_sample(params, gulp, dm_rows: int = 128):
+    """The oracle on one bounded sample of a gulp: the full flagger, then
+    dedispersion + smoothing + standardisation + peaks over `dm_rows` DM
+    trials of the middle of the list; the search part is scaled to all
+    trials.  Returns (seconds for a whole gulp, threads, description)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    f32 = lambda v: float(np.float32(v))
+    nch, G = params["nchan"], params["gulp"]
+    dms = oracle.dm_list(0.0, f32(params["dm_max"]), f32(params["ti_us"]), f32(params["dm_tol"]), nch,
+                         f32(params["plan_dt"]), f32(params["f0_mhz"]), f32(params["df_mhz"]))
+    delays = oracle.dm_delays(dms, oracle.delay_table(nch, f32(params["plan_dt"]), f32(params["f0_mhz"]),
+                                                      f32(params["df_mhz"])))
+    md = int(delays[-1, -1])
+    wmax = params["width_max"]
+    ntd = G + wmax
+    a = len(dms) // 2 - dm_rows // 2
+    t0 = time.perf_counter()
+    flagged, _, _ = oracle.flag_beam(gulp)
+    t1 = time.perf_counter()
+    reps = (md + ntd + G - 1) // G + 1
+    window = np.ascontiguousarray(np.concatenate([flagged] * reps)[: md + ntd])
+    t2 = time.perf_counter()
+    dd = oracle.dedisperse(window, delays[a:a + dm_rows], nout=ntd)
+    nbox, sm = 0, params["width_min"]
+    while sm < wmax:
+        nbox, sm = nbox + 1, sm * 2
+    boxes = np.zeros((nbox, dm_rows - 2, G), np.float32)
+    m, s = np.zeros(nbox, np.float32), np.zeros(nbox, np.float32)
+    L = oracle.lib()
+    L.ho_smooth_normalise(dd.ctypes.data, dm_rows, ntd, ntd, params["width_min"], wmax, 0, G, boxes.ctypes.data,
+                          m.ctypes.data, s.ctypes.data)
+    cands = np.zeros(10000, oracle.CAND_DTYPE)
+    L.ho_find_peaks(boxes.ctypes.data, nbox, dm_rows, G, params["snr"], 0, 10000, cands.ctypes.data, None)
+    t3 = time.perf_counter()
+    per_gulp = (t1 - t0) + (t3 - t2) * len(dms) / dm_rows
+    desc = (f"oracle port: flagger on a full {nch}x{G} gulp ({t1 - t0:.1f} s) + search over {dm_rows} of "
+            f"{len(dms)} DM trials ({t3 - t2:.1f} s), search scaled linearly to all trials")
+    return per_gulp, os.cpu_count(), desc
+
+
+# ---------------------------------------------------------------- main
+
+def main():
+    a = args_()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if a.impl == "gb300" else "gloo")
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+
+    torch.cuda.set_device(local)
+    import hella_gb300 as hg
+
+    hg.lib()
+    params, sky, gulps = workload(rank)
+    G, nch = params["gulp"], params["nchan"]
+    gulp_s = G * params["tsamp"]
+    s = hg.Search(hg.default_params(**params, device=local))
+    info = s.info
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    dev = [torch.from_numpy(g).cuda() for g in gulps]
+    host = [torch.from_numpy(g).pin_memory() for g in gulps]
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    dd_ms, sm_ms, fl_ms = [], [], []
+
+    def step(i, timed):
+        e = [ev() for _ in range(4)] if timed else None
+        s.clear_peaks()
+        s.load_gulp(dev[i % len(dev)].data_ptr(), on_device=True)
+        if timed:
+            e[0].record(stream)
+        s.fast_flagger()
+        if timed:
+            e[1].record(stream)
+        s.dedisperse(0)
+        if timed:
+            e[2].record(stream)
+        s.smooth(1)
+        if timed:
+            e[3].record(stream)
+        s.find_peaks(0)
+        s.rewind()
+        return e
+
+    # fill the ring, then warm up on searched gulps
+    gi = 0
+    for _ in range(info.min_gulp + a.warmup):
+        step(gi, False)
+        gi += 1
+    torch.cuda.synchronize()
+
+    # ---------------- device-resident timing
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = hg.kernel_launches()
+    t0, t1 = ev(), ev()
+    t0.record(stream)
+    marks = []
+    for _ in range(a.steps):
+        marks.append(step(gi, True))
+        gi += 1
+    t1.record(stream)
+    torch.cuda.synchronize()
+    launches = hg.kernel_launches() - l0
+    if dist:
+        dist.barrier()
+    ms = t0.elapsed_time(t1)
+    for e in marks:
+        fl_ms.append(e[0].elapsed_time(e[1]))
+        dd_ms.append(e[1].elapsed_time(e[2]))
+        sm_ms.append(e[2].elapsed_time(e[3]))
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / a.steps
+    value = world * a.steps * gulp_s / (ms / 1e3)
+
+    # ---------------- end to end through the C ABI from pinned host memory
+    lat = []
+    ncand = []
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    w0 = time.perf_counter()
+    for _ in range(a.steps):
+        q0 = time.perf_counter()
+        cands, searched = s.process_gulp(host[gi % len(host)].data_ptr(), on_device=False)
+        lat.append(time.perf_counter() - q0)
+        ncand.append(len(cands))
+        gi += 1
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - w0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * a.steps * gulp_s / e2e_s
+
+    # ---------------- rooflines
+    nact = nch
+    adds = float(info.ndms) * nact * info.ntime_dd
+    dd_t = float(np.mean(dd_ms)) / 1e3
+    peak_int = hg.int_add_peak(local)
+    achieved = adds / dd_t / 1e12
+    peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
+    roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
+            "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
+            "ms_per_launch": round(dd_t * 1e3, 3)}
+    hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") if (
+        ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
+    sm_t = float(np.mean(sm_ms)) / 1e3
+    plane = 4.0 * info.ndms * info.ntime_dd
+    boxes = 4.0 * info.nboxcar * (info.ndms - 2) * info.ntime_out
+    smooth_bytes = 3 * plane + boxes * 3 + 4.0 * (info.ndms - 2) * info.ntime_out * 2
+    fl_t = float(np.mean(fl_ms)) / 1e3
+    flag_bytes = 10.0 * nch * G
+    extra = {
+        "smooth": {"bound": "hbm", "achieved": round(smooth_bytes / sm_t / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                   "frac": round(smooth_bytes / sm_t / 1e9 / hbm, 4), "ms_per_launch": round(sm_t * 1e3, 3),
+                   "note": "FIR + per-width statistics; bytes = dd plane read x3 + planes write/read"},
+        "flagger": {"bound": "hbm", "achieved": round(flag_bytes / fl_t / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(flag_bytes / fl_t / 1e9 / hbm, 4), "ms_per_launch": round(fl_t * 1e3, 3),
+                    "note": "9 u8 passes + 1 u8 write per sample"},
+    }
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)",
+        "config": {"workload": WORKLOAD, "nchan": nch, "gulp": G, "tsamp": params["tsamp"],
+                   "ndms": info.ndms, "max_delay": info.max_delay, "ntime": info.ntime,
+                   "widths": info.nboxcar, "beams_per_gpu": 1, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2: 134 MB gulp, 1.1 GB ring, 0.66 GB plane, 5.9 GB smoothed planes"},
+        "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": G * nch,
+                "d2h_bytes_per_step": int(4 + 20 * np.mean(ncand)),
+                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "rooflines_other": extra,
+        "clocks": clk,
+        "candidates_per_gulp": float(np.mean(ncand)),
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        per, cores, desc = cpu_sample(params, gulps[0])
+        line["cpu_baseline"] = {"value": round(gulp_s / per, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": desc}
+    s.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(a, rank, world):
+    """The reference path's CPU implementation on the host cores."""
+    if rank != 0:
+        return
+    params, sky, gulps = workload(0, ngulps=1)
+    gulp_s = params["gulp"] * params["tsamp"]
+    for _ in range(a.warmup):
+        cpu_sample(params, gulps[0], dm_rows=32)
+    times, desc, cores = [], "", os.cpu_count()
+    for _ in range(a.steps):
+        per, cores, desc = cpu_sample(params, gulps[0])
+        times.append(per)
+    per = float(np.mean(times))
+    v = gulp_s / per
+    line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)",
+            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,354 @@
+// flagger.cu -- casm-hella's spectral RFI flagger and normaliser on GB300.
+//
+// Reference: src/hella/src/flagger.cu:345-411 (fast_flagger) with the
+// default configuration (no SCRUNCH lines): bandpass_flag (:216-242), then
+// apply_scrunch(8, 8, 100, flag=0, ts=1) (:385-401), then transpose_output
+// (transpose.cu:48-76).
+//
+// Design.  The reference materialises an fp16 copy of the gulp and rewrites
+// it ~14 times.  Here the fp16 plane is never stored: up to the time-series
+// correction every value depends only on its channel and its u8 input level,
+// so each stage publishes a 256-entry lookup table per channel and every
+// reduction pass re-reads the u8 gulp (1 byte per sample) and maps it
+// through the table.  The per-time division and the final normalisation are
+// applied on the fly.  Each reduction reproduces the reference's order:
+//   calc_bandpass_new  (flagger.cu:86-112)   32 lane partials in time order,
+//                                            warp shuffle tree, / width
+//   computeRowMeans    (normalization.cu:19-69) 256 strided partials, warp
+//   computeRowVariances(normalization.cu:72-122) trees, 8-warp sum, / width
+//   calculate_stddev host loops (normalization.cu:138-153) sequential over
+//                                            channels, done by one thread
+//   measure_ts         (timeseries.cu:19-36)  fp16 running sum over channels
+// so the output bytes equal the reference's on the same gulp.
+#include "hg_internal.h"
+#include "hella_search.h"
+
+namespace hg {
+namespace {
+
+constexpr int kCT = 32;  // channels per block (a warp spans channels)
+
+__device__ __forceinline__ __half hzero() { return __float2half_rn(0.f); }
+__device__ __forceinline__ __half hone() { return __float2half_rn(1.f); }
+
+// Value of u8 level v of (beam b, channel c) after flagger stage `stage`:
+//  1 bandpass_correct   divide_by_bp (flagger.cu:180-194)
+//  2 normalize_data     (x + half(-mean)) * half(1/std) (flagger.cu:198-214)
+//  3 spectral flag      1, or x + 1 (replace_data_and_add_bandpass :146-158)
+//  4 bandpass_correct   of the final scrunch
+__device__ __half chain_value(int stage, int v, const FlagState &st, int b,
+                              int c) {
+  const int bc = b * st.nchan + c;
+  __half x = __float2half_rn((float)v);
+  if (stage >= 1) {
+    float bp = st.bp1[bc];
+    x = bp > 0.f ? __hdiv(x, __float2half_rn(bp)) : hzero();
+  }
+  if (stage >= 2) x = __hmul(__hadd(x, st.hsc[b * 8 + 0]), st.hsc[b * 8 + 1]);
+  if (stage >= 3) x = st.flag2[bc] ? hone() : __hadd(x, hone());
+  if (stage >= 4) {
+    float bp = st.bp3[bc];
+    x = bp > 0.f ? __hdiv(x, __float2half_rn(bp)) : hzero();
+  }
+  return x;
+}
+
+__global__ void k_build_lut(FlagState st, int stage) {
+  const int c = blockIdx.x, b = blockIdx.y, v = threadIdx.x;
+  st.lut[((size_t)b * st.nchan + c) * 256 + v] = chain_value(stage, v, st, b, c);
+}
+
+// Stage a block's 32-channel slice of the table as lut_s[level][channel]:
+// lanes (consecutive channels) then hit at most two-way bank conflicts.
+__device__ __forceinline__ void load_lut_slice(__half (*lut_s)[kCT],
+                                               const __half *lut, int nchan,
+                                               int b, int c0) {
+  const __half *lb = lut + ((size_t)b * nchan + c0) * 256;
+  for (int i = threadIdx.x; i < kCT * 256; i += blockDim.x) {
+    int cc = i >> 8, v = i & 255;
+    lut_s[v][cc] = lb[(size_t)cc * 256 + v];
+  }
+}
+
+// calc_bandpass_new partials: lane l of channel c sums samples l, l+32, ...
+// (below 32*floor(w/32)) in time order.  Block = 32 channels x 8 lanes.
+__global__ void __launch_bounds__(256) k_lane_partials(const uint8_t *__restrict__ gulp,
+                                                       const __half *__restrict__ lut,
+                                                       float *__restrict__ part,
+                                                       int nchan, int w) {
+  __shared__ __half lut_s[256][kCT];
+  const int b = blockIdx.z, c0 = blockIdx.x * kCT;
+  load_lut_slice(lut_s, lut, nchan, b, c0);
+  __syncthreads();
+  const int cl = threadIdx.x & 31, l = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int c = c0 + cl;
+  const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)l * nchan + c;
+  const size_t step = (size_t)32 * nchan;
+  const int np = w / 32;
+  float s = 0.f;
+#pragma unroll 8
+  for (int i = 0; i < np; ++i) s = __fadd_rn(s, __half2float(lut_s[g[i * step]][cl]));
+  part[((size_t)b * nchan + c) * 32 + l] = s;
+}
+
+// Warp tree over the 32 lane partials, / w (flagger.cu:103-111).  One warp
+// per (beam, channel).  mode 0: bp1, 1: bp2 + spectral flag, 2: bp3.
+__global__ void k_lane_finish(FlagState st, int mode) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= st.nbeam * st.nchan) return;
+  float v = st.part[(size_t)gw * 32 + lane];
+  for (int off = 16; off > 0; off /= 2) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
+  if (lane == 0) {
+    float bp = __fdiv_rn(v, (float)st.gulp);
+    if (mode == 0) st.bp1[gw] = bp;
+    if (mode == 1) {
+      st.bp2[gw] = bp;
+      st.flag2[gw] = (bp < st.spec_min || bp > st.spec_max) ? 1 : 0;
+    }
+    if (mode == 2) st.bp3[gw] = bp;
+  }
+}
+
+// computeRowMeans / computeRowVariances partials: thread j of channel c sums
+// columns j, j+256, ... below nw = 256*floor(w/256).  TS: values divided by
+// half(ts[t]) (divide_by_ts, timeseries.cu:38-55).  VAR: (x - mean)^2 with
+// the fused multiply-add the reference's compiler emits.
+template <bool VAR, bool TS>
+__global__ void __launch_bounds__(256) k_row_partials(const uint8_t *__restrict__ gulp,
+                                                      FlagState st, int which) {
+  __shared__ __half lut_s[256][kCT];
+  const int b = blockIdx.z, c0 = blockIdx.x * kCT, nchan = st.nchan, w = st.gulp;
+  load_lut_slice(lut_s, st.lut, nchan, b, c0);
+  __syncthreads();
+  const int cl = threadIdx.x & 31, j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int c = c0 + cl;
+  const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)j * nchan + c;
+  const __half *hts = st.hts + (size_t)b * w + j;
+  const size_t step = (size_t)256 * nchan;
+  const int nk = w / 256;
+  const float mean = VAR ? st.scal[b * 8 + 2 * which] : 0.f;
+  float s = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < nk; ++k) {
+    __half hv = lut_s[g[k * step]][cl];
+    if (TS) hv = __hdiv(hv, hts[k * 256]);
+    float f = __half2float(hv);
+    if (VAR) {
+      float d = __fsub_rn(f, mean);
+      s = __fmaf_rn(d, d, s);
+    } else {
+      s = __fadd_rn(s, f);
+    }
+  }
+  st.part[((size_t)b * nchan + c) * 256 + j] = s;
+}
+
+// Thread 0 of the reference's 256-thread block: each warp's shuffle tree,
+// then warp totals 1..7 added in order, / nw.  One warp per channel.
+__global__ void k_row_finish(FlagState st) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= st.nbeam * st.nchan) return;
+  const float *p = st.part + (size_t)gw * 256;
+  float tot = 0.f;
+  for (int wi = 0; wi < 8; ++wi) {
+    float v = p[wi * 32 + lane];
+    for (int off = 16; off > 0; off /= 2) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
+    tot = wi == 0 ? v : __fadd_rn(tot, v);
+  }
+  if (lane == 0) st.rowval[gw] = __fdiv_rn(tot, (float)(256 * (st.gulp / 256)));
+}
+
+// calculate_stddev's host loops (normalization.cu:138-153): sequential sum
+// over channels, / nchan; the variance pass also forms the half-precision
+// normalisation constants of normalize_data (flagger.cu:205-206).
+template <bool VAR>
+__global__ void k_beam_sum(FlagState st, int which) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= st.nbeam) return;
+  const float *rv = st.rowval + (size_t)b * st.nchan;
+  float s = 0.f;
+  for (int c = 0; c < st.nchan; ++c) s = __fadd_rn(s, rv[c]);
+  s = __fdiv_rn(s, (float)st.nchan);
+  if (!VAR) {
+    st.scal[b * 8 + 2 * which] = s;
+  } else {
+    float sd = __fsqrt_rn(s);
+    float mean = st.scal[b * 8 + 2 * which];
+    st.scal[b * 8 + 2 * which + 1] = sd;
+    st.hsc[b * 8 + 2 * which] = __float2half_rn(-mean);
+    st.hsc[b * 8 + 2 * which + 1] = __float2half_rn(__fdiv_rn(1.f, sd));
+  }
+}
+
+// measure_ts: per sample, fp16 running sum over channels in channel order,
+// then ts = float(sum) / nchan.  Block = 128 consecutive samples; rows and
+// table slices are staged through shared memory 64 channels at a time.
+constexpr int kTsT = 128, kTsC = 64;
+__global__ void __launch_bounds__(kTsT) k_ts(const uint8_t *__restrict__ gulp,
+                                             FlagState st) {
+  __shared__ uint8_t rows_s[kTsT][kTsC + 4];
+  __shared__ __half lut_s[kTsC][256];
+  const int b = blockIdx.y, t0 = blockIdx.x * kTsT, nchan = st.nchan, w = st.gulp;
+  const int tid = threadIdx.x;
+  const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)t0 * nchan;
+  const __half *lb = st.lut + (size_t)b * nchan * 256;
+  __half s = hzero();
+  for (int c0 = 0; c0 < nchan; c0 += kTsC) {
+    const int nc = min(kTsC, nchan - c0);
+    __syncthreads();
+    for (int i = tid; i < kTsT * kTsC; i += kTsT) {
+      int r = i / kTsC, cc = i % kTsC;
+      if (cc < nc && t0 + r < w) rows_s[r][cc] = g[(size_t)r * nchan + c0 + cc];
+    }
+    for (int i = tid; i < kTsC * 256; i += kTsT) {
+      int cc = i >> 8, v = i & 255;
+      if (cc < nc) lut_s[cc][v] = lb[(size_t)(c0 + cc) * 256 + v];
+    }
+    __syncthreads();
+    if (t0 + tid < w)
+      for (int cc = 0; cc < nc; ++cc) s = __hadd(s, lut_s[cc][rows_s[tid][cc]]);
+  }
+  if (t0 + tid < w) {
+    float ts = __fdiv_rn(__half2float(s), (float)nchan);
+    st.ts[(size_t)b * w + t0 + tid] = ts;
+    st.hts[(size_t)b * w + t0 + tid] = __float2half_rn(ts);
+  }
+}
+
+// transpose_output (transpose.cu:321-331): u8 = trunc(clamp(255/14 (x+4))).
+__device__ __forceinline__ uint8_t requant(__half h) {
+  float v = __half2float(h);
+  const float scf = 255.f / 14.f;
+  v = __fmul_rn(scf, __fadd_rn(v, 4.f));
+  if (v < 0.f) v = 0.f;
+  if (v > 255.f) v = 255.f;
+  return (uint8_t)v;
+}
+
+// Final stage: divide_by_ts, normalize_data, requantise, and write the
+// channel-major ring (32 x 32 tiles transposed through shared memory).
+__global__ void k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
+                           uint8_t *__restrict__ plain, long R, long wpos) {
+  __shared__ uint8_t tile[32][33];
+  const int b = blockIdx.z, c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y, nchan = st.nchan, w = st.gulp;
+  const __half a2 = st.hsc[b * 8 + 2], m2 = st.hsc[b * 8 + 3];
+  const uint8_t *g = gulp + (size_t)b * w * nchan;
+  const __half *lb = st.lut + (size_t)b * nchan * 256;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int t = t0 + ty + j, c = c0 + tx;
+    const uint8_t x0 = g[(size_t)t * nchan + c];
+    __half x = __hdiv(lb[(size_t)c * 256 + x0], st.hts[(size_t)b * w + t]);
+    x = __hmul(__hadd(x, a2), m2);
+    tile[ty + j][tx] = requant(x);
+  }
+  __syncthreads();
+  uint8_t *pb = plain + (size_t)b * nchan * R;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int c = c0 + ty + j, t = t0 + tx;
+    long pos = wpos + t;
+    if (pos >= R) pos -= R;
+    pb[(size_t)c * R + pos] = tile[tx][ty + j];
+  }
+}
+
+}  // namespace
+
+cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
+                      long R, long wpos, cudaStream_t s) {
+  const dim3 lutg(st.nchan, st.nbeam);
+  const dim3 laneg(st.nchan / kCT, 32 / 8, st.nbeam);
+  const dim3 rowg(st.nchan / kCT, 256 / 8, st.nbeam);
+  const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
+  const int beam_blocks = (st.nbeam + 63) / 64;
+
+  // bandpass_flag: bandpass_correct (calc_bandpass_new, divide_by_bp)
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 0);
+  k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
+  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 0);
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 1);
+  // normalize_data: calculate_stddev (mean pass, variance pass)
+  k_row_partials<false, false><<<rowg, 256, 0, s>>>(gulp, st, 0);
+  k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+  k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 0);
+  k_row_partials<true, false><<<rowg, 256, 0, s>>>(gulp, st, 0);
+  k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+  k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 0);
+  // calc_bandpass_new of the normalised data -> spectral flag
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 2);
+  k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
+  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 1);
+  // apply_scrunch(8,8,100,flag=0,ts=1): bandpass_correct ...
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
+  k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
+  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 2);
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 4);
+  // ... ts_correct ...
+  k_ts<<<dim3((st.gulp + kTsT - 1) / kTsT, st.nbeam), kTsT, 0, s>>>(gulp, st);
+  // ... normalize_data
+  k_row_partials<false, true><<<rowg, 256, 0, s>>>(gulp, st, 1);
+  k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+  k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 1);
+  k_row_partials<true, true><<<rowg, 256, 0, s>>>(gulp, st, 1);
+  k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+  k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 1);
+  // transpose_output into the ring
+  k_flag_out<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(gulp, st, plain,
+                                                                                 R, wpos);
+  count_launches(24);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- self-check
+namespace {
+
+__global__ void k_fp16_selftest(unsigned long long *bad, unsigned int *first) {
+  const unsigned long long n = 31744ull * 31743ull;  // a in [0, 0x7c00), b in [1, 0x7c00)
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned short ab = (unsigned short)(i / 31743ull);
+    const unsigned short bb = (unsigned short)(i % 31743ull + 1);
+    const __half a = __ushort_as_half(ab), b = __ushort_as_half(bb);
+    const float fa = __half2float(a), fb = __half2float(b);
+    bool mismatch = __half_as_ushort(__hdiv(a, b)) != __half_as_ushort(__float2half_rn(__fdiv_rn(fa, fb)));
+    if ((i & 63) == 0) {
+      mismatch |= __half_as_ushort(__hadd(a, b)) != __half_as_ushort(__float2half_rn(__fadd_rn(fa, fb)));
+      mismatch |= __half_as_ushort(__hmul(a, b)) != __half_as_ushort(__float2half_rn(__fmul_rn(fa, fb)));
+    }
+    if (mismatch) {
+      atomicAdd(bad, 1ull);
+      atomicCAS(first, 0xffffffffu, ((unsigned int)ab << 16) | bb);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace hg
+
+extern "C" hella_status hella_fp16_selftest(int device, unsigned long long *mismatches,
+                                            uint32_t *first_bad) {
+  if (!mismatches || !first_bad) return HELLA_ERR_INVALID_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return HELLA_ERR_CUDA;
+  unsigned long long *d_bad = nullptr;
+  unsigned int *d_first = nullptr;
+  hella_status st = HELLA_OK;
+  if (cudaMalloc(&d_bad, 8) != cudaSuccess || cudaMalloc(&d_first, 4) != cudaSuccess) {
+    st = HELLA_ERR_ALLOC;
+  } else if (cudaMemset(d_bad, 0, 8) != cudaSuccess || cudaMemset(d_first, 0xff, 4) != cudaSuccess) {
+    st = HELLA_ERR_CUDA;
+  } else {
+    hg::k_fp16_selftest<<<152 * 8, 256>>>(d_bad, d_first);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(mismatches, d_bad, 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(first_bad, d_first, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = HELLA_ERR_CUDA;
+  }
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  cudaGetLastError();
+  return st;
+}

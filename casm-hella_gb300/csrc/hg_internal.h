@@ -1,0 +1,122 @@
+// hg_internal.h -- shared declarations of the GB300 search library.
+//
+// Layout of the per-beam state in HBM (all device arrays are beam-major):
+//   gulp     u8  [nbeam][gulp][nchan]       time-major input gulp
+//   plain    u8  [nbeam][nchan][R]          channel-major ring, R = NTIME
+//   packed   u32 [nbeam][nchan][R]          word q holds samples q, q+S,
+//                                           q+2S, q+3S (S = kPackS) of the
+//                                           ring, the dedispersion operand
+//   lut      f16 [nbeam][nchan][256]        flagger value of each u8 level
+//   dd       f32 [ndms][ntime_dd]           dedispersed sums of one beam
+//   boxes    f32 [nbox][ndms-2][ntime_out]  smoothed planes (pre-normalise)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace hg {
+
+// Kernels launched by this library (process-wide, for the benchmark).
+void count_launches(unsigned n);
+
+// Interleave stride of the packed ring: one 32-bit word carries the samples
+// q, q+S, q+2S, q+3S of a channel, so a warp reading 32 consecutive words
+// at any delay gets 4 x 32 consecutive output samples of one DM trial.
+constexpr int kPackS = 256;
+// Dedispersion block: kPackS threads, one per packed word position.
+constexpr int kDedispThreads = kPackS;
+
+// ------------------------------------------------------------- flagger
+struct FlagState {
+  int nbeam, nchan, gulp;
+  float spec_min, spec_max;
+  float *bp1, *bp2, *bp3;   // [nbeam][nchan]
+  float *part;              // [nbeam][nchan][256] reduction partials
+  float *rowval;            // [nbeam][nchan] per-channel row statistic
+  float *scal;              // [nbeam][8] mean1 std1 mean2 std2
+  __half *hsc;              // [nbeam][8] half(-mean1) half(1/std1) ...
+  __half *lut;              // [nbeam][nchan][256]
+  uint8_t *flag2;           // [nbeam][nchan] spectral flag decision
+  float *ts;                // [nbeam][gulp]
+  __half *hts;              // [nbeam][gulp]
+};
+
+// Runs the whole parity flagger for all beams of `gulp` (u8 [nbeam][gulp]
+// [nchan]) and writes the requantised output into the plain ring at ring
+// position `wpos` (mod R) of every beam.
+cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
+                      long R, long wpos, cudaStream_t s);
+
+// ---------------------------------------------------------- packing
+// Rebuild packed words at ring positions [q0, q0 + nq) (mod R) of every
+// beam from the plain ring.
+cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam,
+                      int nchan, long R, long q0, long nq, cudaStream_t s);
+// Time-major input [nsamps][in_stride] -> channel-major plain [nchan][R].
+cudaError_t transpose_tf(const uint8_t *in, size_t in_stride, int nsamps,
+                         int nchan, uint8_t *plain, long R, cudaStream_t s);
+
+// ------------------------------------------------------ dedispersion
+struct DedispArgs {
+  const uint32_t *packed;   // [nchan][R] packed words of one beam
+  long R;                   // ring length (words per channel row), % 4 == 0
+  long win0;                // ring position of window sample 0
+  const int *delays;        // [ndms][nchan] device delay table
+  int nchan;
+  const int *chans;         // active channel list (killmask applied)
+  int nact;
+  int dm_first, dm_count;   // trials computed; output row 0 = dm_first
+  int nout;                 // output samples per trial
+  float *out;               // [dm_count][out_stride]
+  long out_stride;
+  int dpt;                  // DM trials per block (a supported tile)
+  int max_spread;           // max over tiles of delay(c,d_last)-delay(c,d0)
+};
+cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s);
+// Host side: picks the largest DM tile whose staged rows fit in shared
+// memory for trials [dm_first, dm_first + dm_count) and returns it; *spread
+// receives that tile's largest delay(c,d_last) - delay(c,d0).
+int dedisp_pick_tile(const int *delays_host, int nchan, const int *chans_host,
+                     int nact, int dm_first, int dm_count, int *spread);
+
+// ------------------------------------------------------- smoothing
+struct SmoothArgs {
+  const float *dd;          // [ndms][dd_stride]
+  long dd_stride;
+  int ndms, ntime_dd, ntime_out;
+  int nbox, wmin, wmax, anchor;
+  const float *taps;        // middle-row taps of every width, padded
+  const int *tap_off;       // [nbox] offset into taps
+  const int *tap_n;         // [nbox] padded tap count (multiple of 8)
+  int max_taps;             // 2*sm_max + 1
+  float *boxes;             // [nbox][ndms-2][ntime_out]
+  float *rowmean;           // [nbox][ndms-2]
+  float *rowmax;            // [nbox][ndms-2]
+  float *rowvar;            // [nbox][ndms-2]
+  float *stats;             // [nbox][4] mean, std, -mean, 1/std
+  float *gate;              // [4]: mean0n, sigma0n, threshold, pass
+  float snr;
+};
+cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s);
+// scale = 1: per-width mean/std (normalisation); 0: planes left as they are.
+// Both then form the width-0 gate statistics.
+cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale);
+
+struct PeakArgs {
+  const SmoothArgs *sm;
+  int *counts;              // [nbox][ndms-2]
+  int *offsets;             // [nbox][ndms-2]
+  int *total;               // [1] candidates found (capped at cap)
+  int cap;
+  int beam;                 // reported beam index
+  int4 *cand_i;             // [cap] beam, dm_idx, width, samp
+  float *cand_v;            // [cap] normalised value
+};
+cudaError_t find_peaks(const PeakArgs &a, cudaStream_t s);
+// Normalised copy of the planes (inspection).
+cudaError_t normalise_copy(const SmoothArgs &a, float *dst, cudaStream_t s);
+
+}  // namespace hg

@@ -1,0 +1,389 @@
+// plan.cpp -- the hdd_ plan/execute API (include/hella_dedisp.h).
+//
+// Host side of dedispersion: DM list, delay table, killmask, and the
+// execute calls that casm-hella makes through dedisp
+// (src/apps/casm_hella_refactored.cu:205-210, src/hella/src/dedisperse.cpp:
+// 17-48).  The device work is in dedisp.cu.
+#include "hella_dedisp.h"
+#include "hg_internal.h"
+#include "hg_plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace hg {
+
+// DM trials from a smearing tolerance (Cordes & McLaughlin 2003; the rule
+// of brute-force dedispersion codes, Barsdell et al. 2012).  With ts the
+// sample time, ti the pulse width, a = 8.3 us |df| / f^3 the in-channel
+// smearing per unit DM at the band centre f (GHz) and b = a*nchan/4 the
+// band smearing per unit DM error, the next trial D' satisfies
+//   ts^2 + ti^2 + a^2 D'^2 + b^2 (D' - D)^2 = tol^2 (ts^2 + ti^2 + a^2 D^2),
+// whose larger root is taken.  Trials stop at the first one >= dm_end.
+std::vector<float> generate_dm_list(double dm_start, double dm_end, double ti_us,
+                                    double tol, int nchan, double dt_s, double f0,
+                                    double df) {
+  const double ts = dt_s * 1e6;
+  const double adf = std::fabs(df);
+  const double f = (f0 - (nchan * 0.5 - 0.5) * adf) * 1e-3;
+  const double tol2 = tol * tol;
+  const double a = 8.3 * adf / (f * f * f);
+  const double a2 = a * a;
+  const double b2 = a2 * (double)nchan * (double)nchan / 16.0;
+  const double c = (ts * ts + ti_us * ti_us) * (tol2 - 1.0);
+  std::vector<float> out;
+  double dm = dm_start;
+  out.push_back((float)dm);
+  while (dm < dm_end && out.size() < (1u << 22)) {
+    const double d2 = dm * dm;
+    const double k = c + tol2 * a2 * d2;
+    dm = (b2 * dm + std::sqrt(-a2 * b2 * d2 + (a2 + b2) * k)) / (a2 + b2);
+    out.push_back((float)dm);
+  }
+  return out;
+}
+
+// Samples of delay per unit DM, relative to channel 0 (frequency f0):
+// 4.148808e3 s MHz^2 (1/f_c^2 - 1/f0^2) / dt with f_c = f0 - c |df|.
+std::vector<float> delay_table(int nchan, double dt_s, double f0, double df) {
+  std::vector<float> t(nchan);
+  const double adf = std::fabs(df);
+  for (int c = 0; c < nchan; ++c) {
+    const double fc = f0 - c * adf;
+    t[c] = (float)(4.148808e3 / dt_s * (1.0 / (fc * fc) - 1.0 / (f0 * f0)));
+  }
+  return t;
+}
+
+// delay(c, d) = (int)(DM_d * table[c] + 0.5f), each operation in fp32.
+std::vector<int> dm_delays(const std::vector<float> &dms, const std::vector<float> &table) {
+  const size_t nchan = table.size();
+  std::vector<int> d(dms.size() * nchan);
+  for (size_t i = 0; i < dms.size(); ++i)
+    for (size_t c = 0; c < nchan; ++c) {
+      float p = dms[i] * table[c];
+      p = p + 0.5f;
+      d[i * nchan + c] = (int)p;
+    }
+  return d;
+}
+
+}  // namespace hg
+
+struct hdd_plan_struct {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nchans = 0;
+  float dt = 0, f0 = 0, df = 0;
+  std::vector<float> table, dms;
+  std::vector<int> delays, chans;
+  std::vector<hdd_bool> killmask;
+  int max_delay = 0;
+  int *d_delays = nullptr, *d_chans = nullptr;
+  bool dirty = true;
+  uint8_t *d_in = nullptr, *d_plain = nullptr, *d_out = nullptr;
+  uint32_t *d_packed = nullptr;
+  size_t in_cap = 0, plain_cap = 0, out_cap = 0, packed_cap = 0;
+  int spread_first = -1, spread_count = -1, spread = 0, dpt = 0;
+};
+
+namespace {
+
+thread_local int t_device = 0;
+
+void refresh_delays(hdd_plan p) {
+  p->delays = hg::dm_delays(p->dms, p->table);
+  p->max_delay = p->dms.empty() ? 0 : p->delays[(p->dms.size() - 1) * p->nchans + p->nchans - 1];
+  p->dirty = true;
+  p->spread_first = -1;
+}
+
+void rebuild_chans(hdd_plan p) {
+  p->chans.clear();
+  for (int c = 0; c < p->nchans; ++c)
+    if (p->killmask[c]) p->chans.push_back(c);
+  p->dirty = true;
+  p->spread_first = -1;
+}
+
+hdd_error grow(void **ptr, size_t *cap, size_t need) {
+  if (*cap >= need) return HDD_NO_ERROR;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  if (cudaMalloc(ptr, need) != cudaSuccess) {
+    cudaGetLastError();
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  *cap = need;
+  return HDD_NO_ERROR;
+}
+
+hdd_error sync_tables(hdd_plan p) {
+  if (!p->dirty) return HDD_NO_ERROR;
+  cudaFree(p->d_delays);
+  cudaFree(p->d_chans);
+  p->d_delays = nullptr;
+  p->d_chans = nullptr;
+  const size_t nd = p->delays.size() * sizeof(int);
+  const size_t nc = std::max<size_t>(1, p->chans.size()) * sizeof(int);
+  if (cudaMalloc(&p->d_delays, std::max<size_t>(nd, 4)) != cudaSuccess ||
+      cudaMalloc(&p->d_chans, nc) != cudaSuccess) {
+    cudaGetLastError();
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  if (nd && cudaMemcpy(p->d_delays, p->delays.data(), nd, cudaMemcpyHostToDevice) != cudaSuccess)
+    return HDD_MEM_COPY_FAILED;
+  if (!p->chans.empty() && cudaMemcpy(p->d_chans, p->chans.data(), p->chans.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice) != cudaSuccess)
+    return HDD_MEM_COPY_FAILED;
+  p->dirty = false;
+  return HDD_NO_ERROR;
+}
+
+}  // namespace
+
+namespace hg {
+
+hdd_error plan_device_tables(hdd_plan p, const int **d_delays, const int **d_chans, int *nact) {
+  hdd_error e = sync_tables(p);
+  if (e != HDD_NO_ERROR) return e;
+  *d_delays = p->d_delays;
+  *d_chans = p->d_chans;
+  *nact = (int)p->chans.size();
+  return HDD_NO_ERROR;
+}
+
+int plan_tile(hdd_plan p, int first, int count, int *spread) {
+  if (p->spread_first != first || p->spread_count != count) {
+    p->dpt = dedisp_pick_tile(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(),
+                              first, count, &p->spread);
+    p->spread_first = first;
+    p->spread_count = count;
+  }
+  *spread = p->spread;
+  return p->dpt;
+}
+
+}  // namespace hg
+
+extern "C" {
+
+hdd_error hdd_create_plan(hdd_plan *plan, hdd_size nchans, hdd_float dt, hdd_float f0,
+                          hdd_float df) {
+  if (!plan) return HDD_INVALID_POINTER;
+  *plan = nullptr;
+  if (nchans == 0 || nchans > HDD_MAX_NCHANS) return HDD_NCHANS_EXCEEDS_LIMIT;
+  if (!(dt > 0) || !(f0 > 0) || !(df != 0)) return HDD_UNKNOWN_ERROR;
+  hdd_plan p = new (std::nothrow) hdd_plan_struct;
+  if (!p) return HDD_MEM_ALLOC_FAILED;
+  p->device = t_device;
+  p->nchans = (int)nchans;
+  p->dt = dt;
+  p->f0 = f0;
+  p->df = df;
+  p->table = hg::delay_table(p->nchans, dt, f0, df);
+  p->killmask.assign(p->nchans, 1);
+  rebuild_chans(p);
+  *plan = p;
+  return HDD_NO_ERROR;
+}
+
+void hdd_destroy_plan(hdd_plan p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  cudaFree(p->d_delays);
+  cudaFree(p->d_chans);
+  cudaFree(p->d_in);
+  cudaFree(p->d_plain);
+  cudaFree(p->d_packed);
+  cudaFree(p->d_out);
+  delete p;
+}
+
+hdd_error hdd_set_device(int device_idx) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return HDD_INVALID_DEVICE_INDEX;
+  }
+  if (device_idx < 0 || device_idx >= n) return HDD_INVALID_DEVICE_INDEX;
+  if (cudaSetDevice(device_idx) != cudaSuccess) return HDD_INVALID_DEVICE_INDEX;
+  t_device = device_idx;
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_set_stream(hdd_plan p, void *stream) {
+  if (!p) return HDD_INVALID_PLAN;
+  p->stream = (cudaStream_t)stream;
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_set_dm_list(hdd_plan p, const hdd_float *dm_list, hdd_size count) {
+  if (!p) return HDD_INVALID_PLAN;
+  if (!dm_list) return HDD_INVALID_POINTER;
+  p->dms.assign(dm_list, dm_list + count);
+  refresh_delays(p);
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_generate_dm_list(hdd_plan p, hdd_float dm_start, hdd_float dm_end, hdd_float ti,
+                               hdd_float tol) {
+  if (!p) return HDD_INVALID_PLAN;
+  p->dms = hg::generate_dm_list(dm_start, dm_end, ti, tol, p->nchans, p->dt, p->f0, p->df);
+  refresh_delays(p);
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_set_killmask(hdd_plan p, const hdd_bool *killmask) {
+  if (!p) return HDD_INVALID_PLAN;
+  if (killmask)
+    p->killmask.assign(killmask, killmask + p->nchans);
+  else
+    p->killmask.assign(p->nchans, 1);
+  rebuild_chans(p);
+  return HDD_NO_ERROR;
+}
+
+hdd_size hdd_get_max_delay(const hdd_plan p) { return p ? (hdd_size)p->max_delay : 0; }
+hdd_size hdd_get_dm_delay(const hdd_plan p, int trial) {
+  if (!p || trial < 0 || trial >= (int)p->dms.size()) return 0;
+  return (hdd_size)p->delays[(size_t)trial * p->nchans + p->nchans - 1];
+}
+hdd_size hdd_get_channel_count(const hdd_plan p) { return p ? (hdd_size)p->nchans : 0; }
+hdd_size hdd_get_dm_count(const hdd_plan p) { return p ? (hdd_size)p->dms.size() : 0; }
+const hdd_float *hdd_get_dm_list(const hdd_plan p) {
+  return (p && !p->dms.empty()) ? p->dms.data() : nullptr;
+}
+const hdd_bool *hdd_get_killmask(const hdd_plan p) { return p ? p->killmask.data() : nullptr; }
+hdd_float hdd_get_dt(const hdd_plan p) { return p ? p->dt : 0.f; }
+hdd_float hdd_get_df(const hdd_plan p) { return p ? p->df : 0.f; }
+hdd_float hdd_get_f0(const hdd_plan p) { return p ? p->f0 : 0.f; }
+const int *hdd_get_delay_table(const hdd_plan p) {
+  return (p && !p->delays.empty()) ? p->delays.data() : nullptr;
+}
+
+hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_size in_nbits,
+                           hdd_size in_stride, hdd_byte *out, hdd_size out_nbits,
+                           hdd_size out_stride, hdd_size first_dm_idx, hdd_size dm_count,
+                           unsigned flags) {
+  if (!p) return HDD_INVALID_PLAN;
+  if (!in || !out) return HDD_INVALID_POINTER;
+  if (p->dms.empty()) return HDD_NO_DM_LIST_SET;
+  if ((flags & HDD_HOST_POINTERS) && (flags & HDD_DEVICE_POINTERS))
+    return HDD_INVALID_FLAG_COMBINATION;
+  if ((flags & HDD_WAIT) && (flags & HDD_ASYNC)) return HDD_INVALID_FLAG_COMBINATION;
+  if (in_nbits != 8) return HDD_UNSUPPORTED_IN_NBITS;
+  if (out_nbits != 32) return HDD_UNSUPPORTED_OUT_NBITS;
+  if (nsamps <= (hdd_size)p->max_delay) return HDD_TOO_FEW_NSAMPS;
+  if (nsamps > (hdd_size)(65535u * 32u)) return HDD_UNKNOWN_ERROR;  // transpose grid limit
+  const int nout = (int)(nsamps - p->max_delay);
+  if (in_stride < (hdd_size)p->nchans) return HDD_INVALID_STRIDE;
+  if (out_stride % 4 != 0 || out_stride < (hdd_size)nout * 4) return HDD_INVALID_STRIDE;
+  if (first_dm_idx + dm_count > p->dms.size() || dm_count == 0) return HDD_UNKNOWN_ERROR;
+  if (cudaSetDevice(p->device) != cudaSuccess) return HDD_INVALID_DEVICE_INDEX;
+  if (cudaPeekAtLastError() != cudaSuccess) return HDD_PRIOR_GPU_ERROR;
+  const bool device = (flags & HDD_DEVICE_POINTERS) != 0;
+
+  hdd_error e = sync_tables(p);
+  if (e != HDD_NO_ERROR) return e;
+  const uint8_t *din = in;
+  const size_t in_bytes = (size_t)(nsamps - 1) * in_stride + p->nchans;
+  if (!device) {
+    if ((e = grow((void **)&p->d_in, &p->in_cap, in_bytes)) != HDD_NO_ERROR) return e;
+    if (cudaMemcpyAsync(p->d_in, in, in_bytes, cudaMemcpyHostToDevice, p->stream) != cudaSuccess)
+      return HDD_MEM_COPY_FAILED;
+    din = p->d_in;
+  }
+  const long R = ((long)nsamps + 3) / 4 * 4;
+  if ((e = grow((void **)&p->d_plain, &p->plain_cap, (size_t)p->nchans * R)) != HDD_NO_ERROR)
+    return e;
+  if ((e = grow((void **)&p->d_packed, &p->packed_cap, (size_t)p->nchans * R * 4)) != HDD_NO_ERROR)
+    return e;
+  float *dout = reinterpret_cast<float *>(out);
+  if (!device) {
+    if ((e = grow((void **)&p->d_out, &p->out_cap, (size_t)dm_count * out_stride)) != HDD_NO_ERROR)
+      return e;
+    dout = reinterpret_cast<float *>(p->d_out);
+  }
+  if (hg::transpose_tf(din, in_stride, (int)nsamps, p->nchans, p->d_plain, R, p->stream) !=
+      cudaSuccess)
+    return HDD_INTERNAL_GPU_ERROR;
+  if (hg::pack_ring(p->d_plain, p->d_packed, 1, p->nchans, R, 0, R, p->stream) != cudaSuccess)
+    return HDD_INTERNAL_GPU_ERROR;
+  hg::DedispArgs a{};
+  a.packed = p->d_packed;
+  a.R = R;
+  a.win0 = 0;
+  a.delays = p->d_delays;
+  a.nchan = p->nchans;
+  a.chans = p->d_chans;
+  a.nact = (int)p->chans.size();
+  a.dm_first = (int)first_dm_idx;
+  a.dm_count = (int)dm_count;
+  a.nout = nout;
+  a.out = dout;
+  a.out_stride = (long)(out_stride / 4);
+  a.dpt = hg::plan_tile(p, a.dm_first, a.dm_count, &a.max_spread);
+  if (a.nact == 0) {
+    for (hdd_size d = 0; d < dm_count; ++d)
+      if (cudaMemsetAsync(reinterpret_cast<uint8_t *>(dout) + d * out_stride, 0, (size_t)nout * 4,
+                          p->stream) != cudaSuccess)
+        return HDD_INTERNAL_GPU_ERROR;
+  } else if (hg::dedisperse(a, p->stream) != cudaSuccess) {
+    return HDD_INTERNAL_GPU_ERROR;
+  }
+  if (!device) {
+    if (cudaMemcpy2DAsync(out, out_stride, dout, out_stride, (size_t)nout * 4, dm_count,
+                          cudaMemcpyDeviceToHost, p->stream) != cudaSuccess)
+      return HDD_MEM_COPY_FAILED;
+  }
+  if (!(flags & HDD_ASYNC) && cudaStreamSynchronize(p->stream) != cudaSuccess)
+    return HDD_INTERNAL_GPU_ERROR;
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_execute_adv(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_size in_nbits,
+                          hdd_size in_stride, hdd_byte *out, hdd_size out_nbits,
+                          hdd_size out_stride, unsigned flags) {
+  if (!p) return HDD_INVALID_PLAN;
+  return hdd_execute_guru(p, nsamps, in, in_nbits, in_stride, out, out_nbits, out_stride, 0,
+                          p->dms.size(), flags);
+}
+
+hdd_error hdd_execute(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_size in_nbits,
+                      hdd_byte *out, hdd_size out_nbits, unsigned flags) {
+  if (!p) return HDD_INVALID_PLAN;
+  if (nsamps <= (hdd_size)p->max_delay) return HDD_TOO_FEW_NSAMPS;
+  const hdd_size in_stride = (hdd_size)p->nchans * in_nbits / 8;
+  const hdd_size out_stride = (nsamps - p->max_delay) * out_nbits / 8;
+  return hdd_execute_adv(p, nsamps, in, in_nbits, in_stride, out, out_nbits, out_stride, flags);
+}
+
+const char *hdd_get_error_string(hdd_error e) {
+  switch (e) {
+    case HDD_NO_ERROR: return "no error";
+    case HDD_MEM_ALLOC_FAILED: return "mem alloc failed";
+    case HDD_MEM_COPY_FAILED: return "mem copy failed";
+    case HDD_NCHANS_EXCEEDS_LIMIT: return "nchans exceeds limit";
+    case HDD_INVALID_PLAN: return "invalid plan";
+    case HDD_INVALID_POINTER: return "invalid pointer";
+    case HDD_INVALID_STRIDE: return "invalid stride";
+    case HDD_NO_DM_LIST_SET: return "no dm list set";
+    case HDD_TOO_FEW_NSAMPS: return "too few nsamps";
+    case HDD_INVALID_FLAG_COMBINATION: return "invalid flag combination";
+    case HDD_UNSUPPORTED_IN_NBITS: return "unsupported in nbits";
+    case HDD_UNSUPPORTED_OUT_NBITS: return "unsupported out nbits";
+    case HDD_INVALID_DEVICE_INDEX: return "invalid device index";
+    case HDD_DEVICE_ALREADY_SET: return "device already set";
+    case HDD_PRIOR_GPU_ERROR: return "prior gpu error";
+    case HDD_INTERNAL_GPU_ERROR: return "internal gpu error";
+    case HDD_UNKNOWN_ERROR: return "unknown error";
+  }
+  return "unknown code";
+}
+
+}  // extern "C"

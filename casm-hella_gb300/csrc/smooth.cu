@@ -1,0 +1,362 @@
+// smooth.cu -- casm-hella's smoothing, per-width normalisation and peak
+// finding on GB300.
+//
+// Reference: src/hella/src/smooth.cpp:21-127 and src/hella/src/peaks.cu:
+// 31-117.  For every width sm = wmin*2^k < wmax the reference filters the
+// dedispersed plane with a 3 x (2sm+1) kernel (DM weights 0.3/1/0.3 times
+// time taps v(u)^2, normalised to sum 1), crops rows 1..ndms-2 and columns
+// wmax/2 .. wmax/2+gulp, and standardises each width with
+// calculate_stddev (normalization.cu:125-162).  find_peaks takes sigma of
+// the standardised width-0 plane, gates the beam on 0.1 < sigma < 5 and
+// emits every sample above snr*sigma in (width, DM row, time) order.
+//
+// Arithmetic (the oracle follows it operation for operation):
+//   y[x]   = fmaf(0.3f, dd[r][x] + dd[r+2][x], dd[r+1][x])  (exact sum)
+//   out[j] = fmaf chain over k = 0..2sm of tap[k] * y[clamp(x0 + k)]
+// i.e. the DM weights factored out of the 2-D kernel, whose middle row
+// supplies the time taps.  Borders replicate (NPP_BORDER_REPLICATE).
+//
+// Kernels.  k_fir: one block per output row; the row's y values for a
+// 2048-sample chunk are staged in shared memory in an 8-phase layout
+// (Y[x % 8][x / 8]) so that each thread keeps a sliding window of 8
+// outputs in registers and reads one conflict-free word per tap.  Every
+// width is produced from the same staged chunk; the row-mean partials of
+// the reference's order (thread j sums columns j, j+256, ...) are
+// accumulated as the chunk is written, so the plane is written once and
+// read once more for the variance.  Row maxima let the peak pass skip rows
+// that cannot hold a candidate.
+#include "hg_internal.h"
+
+namespace hg {
+namespace {
+
+constexpr int kR = 8;             // outputs per thread
+constexpr int kT = 256;           // threads per row block
+constexpr int kCH = kR * kT;      // outputs per chunk
+
+__device__ __forceinline__ float block256_tree(const float *p) {
+  // p: 256 partials in shared memory; returns thread 0's total
+  // (normalization.cu:41-68) in every thread of warp 0.
+  const int lane = threadIdx.x & 31;
+  float tot = 0.f;
+  for (int wi = 0; wi < 8; ++wi) {
+    float v = p[wi * 32 + lane];
+    for (int off = 16; off > 0; off /= 2) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
+    tot = wi == 0 ? v : __fadd_rn(tot, v);
+  }
+  return tot;
+}
+
+__device__ __forceinline__ float normv(float x, const float *st) {
+  // smooth.cpp:105-123: skipped when std <= 0; else AddC(-mean), MulC(1/std)
+  return st[1] > 0.f ? __fmul_rn(__fadd_rn(x, st[2]), st[3]) : x;
+}
+
+__global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  const int nbox = a.nbox, h = a.ndms - 2, tid = threadIdx.x;
+  const int span = 2 * (a.wmin << (nbox - 1));
+  const int ylen = kCH + span + 2 * kR;
+  const int M = (ylen + kR - 1) / kR;
+  int ntaps_total = 0;
+  for (int b = 0; b < nbox; ++b) ntaps_total += a.tap_n[b];
+  float *taps = sm;
+  float *Y = taps + ((ntaps_total + 3) / 4) * 4;
+  float *out_s = Y + kR * M;
+  float *part_s = out_s + kCH;
+  float *max_s = part_s + nbox * kT;
+  for (int i = tid; i < ntaps_total; i += kT) taps[i] = a.taps[i];
+  for (int b = 0; b < nbox; ++b) {
+    part_s[b * kT + tid] = 0.f;
+    max_s[b * kT + tid] = -INFINITY;
+  }
+  const int r = blockIdx.x;
+  const float *ra = a.dd + (size_t)r * a.dd_stride;
+  const float *rb = ra + a.dd_stride;
+  const float *rc = rb + a.dd_stride;
+  const int nw = 256 * (a.ntime_out / 256);
+  const int org = a.wmax / 2 - (a.anchor ? span : 0);
+
+  for (int cs = 0; cs < a.ntime_out; cs += kCH) {
+    __syncthreads();
+    for (int x = tid; x < kR * M; x += kT) {
+      int col = cs + org + x;
+      col = col < 0 ? 0 : (col >= a.ntime_dd ? a.ntime_dd - 1 : col);
+      Y[(x % kR) * M + x / kR] = __fmaf_rn(0.3f, __fadd_rn(ra[col], rc[col]), rb[col]);
+    }
+    __syncthreads();
+    for (int b = 0; b < nbox; ++b) {
+      const int smw = a.wmin << b;
+      const int off = a.anchor ? span - 2 * smw : 0;
+      const float *tp = taps + a.tap_off[b];
+      const int n = a.tap_n[b];
+      const int base = kR * tid + off;
+      float acc[kR], win[kR];
+#pragma unroll
+      for (int i = 0; i < kR; ++i) {
+        acc[i] = 0.f;
+        const int x = base + i;
+        win[i] = Y[(x % kR) * M + x / kR];
+      }
+      for (int kb = 0; kb < n; kb += kR) {
+#pragma unroll
+        for (int kk = 0; kk < kR; ++kk) {
+          const float cf = tp[kb + kk];
+#pragma unroll
+          for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cf, win[(i + kk) % kR], acc[i]);
+          const int x = base + kb + kk + kR;
+          win[kk] = Y[(x % kR) * M + x / kR];
+        }
+      }
+      float4 *o4 = reinterpret_cast<float4 *>(out_s + kR * tid);
+      o4[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      o4[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      __syncthreads();
+      float *dst = a.boxes + ((size_t)b * h + r) * a.ntime_out;
+      float ps = part_s[b * kT + tid], mx = max_s[b * kT + tid];
+#pragma unroll
+      for (int m = 0; m < kR; ++m) {
+        const int j = tid + kT * m, col = cs + j;
+        if (col < a.ntime_out) {
+          const float v = out_s[j];
+          dst[col] = v;
+          mx = fmaxf(mx, v);
+          if (col < nw) ps = __fadd_rn(ps, v);
+        }
+      }
+      part_s[b * kT + tid] = ps;
+      max_s[b * kT + tid] = mx;
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  for (int b = tid >> 5; b < nbox; b += kT / 32) {
+    const float tot = block256_tree(part_s + b * kT);
+    float mx = -INFINITY;
+    for (int i = threadIdx.x & 31; i < kT; i += 32) mx = fmaxf(mx, max_s[b * kT + i]);
+    for (int off = 16; off > 0; off /= 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if ((tid & 31) == 0) {
+      a.rowmean[(size_t)b * h + r] = __fdiv_rn(tot, (float)nw);
+      a.rowmax[(size_t)b * h + r] = mx;
+    }
+  }
+}
+
+// Host loop of calculate_stddev (normalization.cu:138-142): sequential over
+// rows, / height.  One thread per width.
+__global__ void k_mean_finish(SmoothArgs a) {
+  const int b = threadIdx.x;
+  if (b >= a.nbox) return;
+  const int h = a.ndms - 2;
+  float s = 0.f;
+  for (int r = 0; r < h; ++r) s = __fadd_rn(s, a.rowmean[(size_t)b * h + r]);
+  a.stats[b * 4 + 0] = __fdiv_rn(s, (float)h);
+}
+
+// computeRowVariances over one row of one width plane.  NORM0: the
+// normalised width-0 plane (find_peaks' sigma, peaks.cu:171-178).
+template <bool NORM0, bool VAR>
+__global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
+  __shared__ float p_s[kT];
+  const int r = blockIdx.x, b = NORM0 ? 0 : blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
+  const float *x = a.boxes + ((size_t)b * h + r) * a.ntime_out;
+  const int nw = 256 * (a.ntime_out / 256);
+  const float *st = a.stats + b * 4;
+  const float mean = NORM0 ? a.gate[0] : st[0];
+  float s = 0.f;
+  for (int col = tid; col < nw; col += kT) {
+    float v = NORM0 ? normv(x[col], st) : x[col];
+    if (VAR) {
+      const float d = __fsub_rn(v, mean);
+      s = __fmaf_rn(d, d, s);
+    } else {
+      s = __fadd_rn(s, v);
+    }
+  }
+  p_s[tid] = s;
+  __syncthreads();
+  if (tid < 32) {
+    const float tot = block256_tree(p_s);
+    if (tid == 0) a.rowvar[(size_t)b * h + r] = __fdiv_rn(tot, (float)nw);
+  }
+}
+
+// Per width: variance -> std and the normalisation constants.  NORM0: the
+// gate statistics of the normalised width-0 plane.
+template <bool NORM0, bool VAR>
+__global__ void k_stat_finish(SmoothArgs a) {
+  const int b = threadIdx.x;
+  if (b >= (NORM0 ? 1 : a.nbox)) return;
+  const int h = a.ndms - 2;
+  float s = 0.f;
+  for (int r = 0; r < h; ++r) s = __fadd_rn(s, a.rowvar[(size_t)b * h + r]);
+  s = __fdiv_rn(s, (float)h);
+  if (NORM0) {
+    if (!VAR) {
+      a.gate[0] = s;
+    } else {
+      const float sig = __fsqrt_rn(s);
+      a.gate[1] = sig;
+      a.gate[2] = __fmul_rn(a.snr, sig);
+      a.gate[3] = (sig < 5 && (double)sig > 0.1) ? 1.f : 0.f;  // definitions.h:71-72
+    }
+  } else {
+    const float sd = __fsqrt_rn(s), mean = a.stats[b * 4 + 0];
+    a.stats[b * 4 + 1] = sd;
+    a.stats[b * 4 + 2] = -1.0f * mean;
+    a.stats[b * 4 + 3] = __fdiv_rn(1.0f, sd);
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_count(PeakArgs p, SmoothArgs a) {
+  __shared__ int c_s[kT / 32];
+  const int r = blockIdx.x, b = blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
+  const size_t row = (size_t)b * h + r;
+  const float *st = a.stats + b * 4;
+  const float thr = a.gate[2];
+  // normalisation is monotonic, so the row maximum decides the whole row
+  if (a.gate[3] == 0.f || !(normv(a.rowmax[row], st) > thr)) {
+    if (tid == 0) p.counts[row] = 0;
+    return;
+  }
+  const float *x = a.boxes + row * a.ntime_out;
+  int n = 0;
+  for (int col = tid; col < a.ntime_out; col += kT) n += normv(x[col], st) > thr;
+  for (int off = 16; off > 0; off /= 2) n += __shfl_xor_sync(0xffffffffu, n, off);
+  if ((tid & 31) == 0) c_s[tid >> 5] = n;
+  __syncthreads();
+  if (tid == 0) {
+    int t = 0;
+    for (int i = 0; i < kT / 32; ++i) t += c_s[i];
+    p.counts[row] = t;
+  }
+}
+
+// Exclusive scan of the row counts in (width, row) order; total capped.
+__global__ void __launch_bounds__(1024) k_scan(PeakArgs p, int nrows) {
+  __shared__ int s_s[1024];
+  const int tid = threadIdx.x;
+  const int per = (nrows + 1023) / 1024;
+  const int lo = min(nrows, tid * per), hi = min(nrows, lo + per);
+  int sum = 0;
+  for (int i = lo; i < hi; ++i) sum += p.counts[i];
+  s_s[tid] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off *= 2) {
+    int v = tid >= off ? s_s[tid - off] : 0;
+    __syncthreads();
+    s_s[tid] += v;
+    __syncthreads();
+  }
+  int run = s_s[tid] - sum;
+  for (int i = lo; i < hi; ++i) {
+    p.offsets[i] = run;
+    run += p.counts[i];
+  }
+  if (tid == 1023) p.total[0] = min(s_s[1023], p.cap);
+}
+
+// Ordered compaction of one row's candidates.
+__global__ void __launch_bounds__(kT) k_write(PeakArgs p, SmoothArgs a) {
+  __shared__ int w_s[kT / 32];
+  __shared__ int base_s;
+  const int r = blockIdx.x, b = blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const size_t row = (size_t)b * h + r;
+  if (p.counts[row] == 0 || p.offsets[row] >= p.cap) return;
+  const float *st = a.stats + b * 4;
+  const float thr = a.gate[2];
+  const float *x = a.boxes + row * a.ntime_out;
+  if (tid == 0) base_s = p.offsets[row];
+  for (int cs = 0; cs < a.ntime_out; cs += kT) {
+    const int col = cs + tid;
+    float v = 0.f;
+    bool hit = false;
+    if (col < a.ntime_out) {
+      v = normv(x[col], st);
+      hit = v > thr;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    __syncthreads();
+    if (lane == 0) w_s[warp] = __popc(bal);
+    __syncthreads();
+    int before = base_s;
+    for (int i = 0; i < warp; ++i) before += w_s[i];
+    before += __popc(bal & ((1u << lane) - 1u));
+    if (hit && before < p.cap) {
+      p.cand_i[before] = make_int4(p.beam, r + 1, b, col);
+      p.cand_v[before] = v;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int t = 0;
+      for (int i = 0; i < kT / 32; ++i) t += w_s[i];
+      base_s += t;
+    }
+  }
+}
+
+__global__ void k_normalise_copy(SmoothArgs a, float *dst) {
+  const size_t plane = (size_t)(a.ndms - 2) * a.ntime_out;
+  const size_t n = plane * a.nbox;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = normv(a.boxes[i], a.stats + (i / plane) * 4);
+}
+
+}  // namespace
+
+size_t fir_smem_bytes(const SmoothArgs &a, int ntaps_total) {
+  const int span = 2 * (a.wmin << (a.nbox - 1));
+  const int ylen = kCH + span + 2 * kR;
+  const int M = (ylen + kR - 1) / kR;
+  return sizeof(float) * ((size_t)(ntaps_total + 3) / 4 * 4 + (size_t)kR * M + kCH +
+                          (size_t)2 * a.nbox * kT);
+}
+
+cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s) {
+  int ntot = 0;  // the kernel re-derives this total from tap_n
+  for (int b = 0; b < a.nbox; ++b) ntot += ((2 * (a.wmin << b) + 1 + kR - 1) / kR) * kR;
+  const size_t smem = fir_smem_bytes(a, ntot);
+  cudaError_t e = cudaFuncSetAttribute(k_fir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_fir<<<a.ndms - 2, kT, smem, s>>>(a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale) {
+  const int h = a.ndms - 2;
+  if (scale) {
+    k_mean_finish<<<1, 32, 0, s>>>(a);
+    k_row_stat<false, true><<<dim3(h, a.nbox), kT, 0, s>>>(a);
+    k_stat_finish<false, true><<<1, 32, 0, s>>>(a);
+  } else {
+    cudaError_t e = cudaMemsetAsync(a.stats, 0, sizeof(float) * 4 * a.nbox, s);
+    if (e != cudaSuccess) return e;
+  }
+  k_row_stat<true, false><<<dim3(h, 1), kT, 0, s>>>(a);
+  k_stat_finish<true, false><<<1, 32, 0, s>>>(a);
+  k_row_stat<true, true><<<dim3(h, 1), kT, 0, s>>>(a);
+  k_stat_finish<true, true><<<1, 32, 0, s>>>(a);
+  count_launches(scale ? 7 : 4);
+  return cudaGetLastError();
+}
+
+cudaError_t find_peaks(const PeakArgs &p, cudaStream_t s) {
+  const SmoothArgs &a = *p.sm;
+  const int h = a.ndms - 2;
+  k_count<<<dim3(h, a.nbox), kT, 0, s>>>(p, a);
+  k_scan<<<1, 1024, 0, s>>>(p, h * a.nbox);
+  k_write<<<dim3(h, a.nbox), kT, 0, s>>>(p, a);
+  count_launches(3);
+  return cudaGetLastError();
+}
+
+cudaError_t normalise_copy(const SmoothArgs &a, float *dst, cudaStream_t s) {
+  k_normalise_copy<<<1024, 256, 0, s>>>(a, dst);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,375 @@
+"""ctypes binding of libhella_gb300.so (include/hella_dedisp.h, hella_search.h).
+
+A thin mirror of the C ABI for the Python test harness and the benchmark.
+Loading fails loudly when the library has not been built: there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libhella_gb300.so"
+
+_lib = None
+
+# --------------------------------------------------------------- structures
+
+HELLA_MAX_SCRUNCH = 16
+HELLA_MAX_GIANTS = 10000
+
+HDD_HOST_POINTERS = 1 << 1
+HDD_DEVICE_POINTERS = 1 << 2
+HDD_WAIT = 1 << 3
+HDD_ASYNC = 1 << 4
+
+HDD_ERRORS = [
+    "HDD_NO_ERROR", "HDD_MEM_ALLOC_FAILED", "HDD_MEM_COPY_FAILED", "HDD_NCHANS_EXCEEDS_LIMIT",
+    "HDD_INVALID_PLAN", "HDD_INVALID_POINTER", "HDD_INVALID_STRIDE", "HDD_NO_DM_LIST_SET",
+    "HDD_TOO_FEW_NSAMPS", "HDD_INVALID_FLAG_COMBINATION", "HDD_UNSUPPORTED_IN_NBITS",
+    "HDD_UNSUPPORTED_OUT_NBITS", "HDD_INVALID_DEVICE_INDEX", "HDD_DEVICE_ALREADY_SET",
+    "HDD_PRIOR_GPU_ERROR", "HDD_INTERNAL_GPU_ERROR", "HDD_UNKNOWN_ERROR",
+]
+
+
+class HellaScrunch(C.Structure):
+    _fields_ = [("tscrunch", C.c_int), ("fscrunch", C.c_int), ("nits", C.c_int), ("thresh", C.c_float)]
+
+
+class HellaParams(C.Structure):
+    _fields_ = [
+        ("nchan", C.c_int), ("nbeam", C.c_int), ("gulp", C.c_int),
+        ("tsamp", C.c_double), ("plan_dt", C.c_double), ("f0_mhz", C.c_double), ("df_mhz", C.c_double),
+        ("dm_min", C.c_float), ("dm_max", C.c_float), ("dm_tol", C.c_float), ("ti_us", C.c_float),
+        ("width_min", C.c_int), ("width_max", C.c_int), ("snr", C.c_float),
+        ("spec_min", C.c_float), ("spec_max", C.c_float), ("flag1", C.c_int), ("flag2", C.c_int),
+        ("nscrunch", C.c_int), ("scrunch", HellaScrunch * HELLA_MAX_SCRUNCH),
+        ("max_giants", C.c_int), ("beam0", C.c_int), ("smooth_anchor", C.c_int), ("device", C.c_int),
+        ("hbm_budget", C.c_size_t),
+    ]
+
+
+class HellaInfo(C.Structure):
+    _fields_ = [
+        ("ntime", C.c_int), ("ndms", C.c_int), ("max_delay", C.c_int), ("ntime_dd", C.c_int),
+        ("ntime_out", C.c_int), ("nboxcar", C.c_int), ("min_gulp", C.c_int), ("gulp_index", C.c_int),
+        ("device_bytes", C.c_size_t),
+    ]
+
+
+class HellaCand(C.Structure):
+    _fields_ = [("beam", C.c_int32), ("dm_idx", C.c_int32), ("width", C.c_int32),
+                ("samp", C.c_int32), ("snr", C.c_float)]
+
+
+CAND_DTYPE = np.dtype([("beam", "<i4"), ("dm_idx", "<i4"), ("width", "<i4"), ("samp", "<i4"),
+                       ("snr", "<f4")])
+
+# ------------------------------------------------------------------ loading
+
+_VP = C.c_void_p
+_SZ = C.c_ulong
+
+
+def _sig(lib, name, res, args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = args
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with casm-hella_gb300/build.py")
+    L = C.CDLL(str(LIB_PATH))
+    # hdd_ plan API
+    _sig(L, "hdd_create_plan", C.c_int, [C.POINTER(_VP), _SZ, C.c_float, C.c_float, C.c_float])
+    _sig(L, "hdd_destroy_plan", None, [_VP])
+    _sig(L, "hdd_set_device", C.c_int, [C.c_int])
+    _sig(L, "hdd_set_stream", C.c_int, [_VP, _VP])
+    _sig(L, "hdd_set_dm_list", C.c_int, [_VP, _VP, _SZ])
+    _sig(L, "hdd_generate_dm_list", C.c_int, [_VP, C.c_float, C.c_float, C.c_float, C.c_float])
+    _sig(L, "hdd_set_killmask", C.c_int, [_VP, _VP])
+    for n in ("hdd_get_max_delay", "hdd_get_channel_count", "hdd_get_dm_count"):
+        _sig(L, n, _SZ, [_VP])
+    _sig(L, "hdd_get_dm_delay", _SZ, [_VP, C.c_int])
+    _sig(L, "hdd_get_dm_list", C.POINTER(C.c_float), [_VP])
+    _sig(L, "hdd_get_killmask", C.POINTER(C.c_int), [_VP])
+    _sig(L, "hdd_get_delay_table", C.POINTER(C.c_int), [_VP])
+    for n in ("hdd_get_dt", "hdd_get_df", "hdd_get_f0"):
+        _sig(L, n, C.c_float, [_VP])
+    _sig(L, "hdd_execute", C.c_int, [_VP, _SZ, _VP, _SZ, _VP, _SZ, C.c_uint])
+    _sig(L, "hdd_execute_adv", C.c_int, [_VP, _SZ, _VP, _SZ, _SZ, _VP, _SZ, _SZ, C.c_uint])
+    _sig(L, "hdd_execute_guru", C.c_int, [_VP, _SZ, _VP, _SZ, _SZ, _VP, _SZ, _SZ, _SZ, _SZ, C.c_uint])
+    _sig(L, "hdd_get_error_string", C.c_char_p, [C.c_int])
+    # hella_ stage API
+    _sig(L, "hella_params_default", None, [C.POINTER(HellaParams)])
+    _sig(L, "hella_create", C.c_int, [C.POINTER(_VP), C.POINTER(HellaParams)])
+    _sig(L, "hella_destroy", None, [_VP])
+    _sig(L, "hella_set_stream", C.c_int, [_VP, _VP])
+    _sig(L, "hella_get_info", C.c_int, [_VP, C.POINTER(HellaInfo)])
+    _sig(L, "hella_get_dm_list", C.POINTER(C.c_float), [_VP])
+    _sig(L, "hella_set_killmask", C.c_int, [_VP, _VP])
+    _sig(L, "hella_load_gulp", C.c_int, [_VP, _VP, C.c_int])
+    for n in ("hella_fast_flagger", "hella_clear_peaks", "hella_rewind"):
+        _sig(L, n, C.c_int, [_VP])
+    for n in ("hella_dedisperse", "hella_smooth", "hella_find_peaks"):
+        _sig(L, n, C.c_int, [_VP, C.c_int])
+    _sig(L, "hella_get_peaks", C.c_int, [_VP, _VP, C.c_int, C.POINTER(C.c_int)])
+    _sig(L, "hella_process_gulp", C.c_int,
+         [_VP, _VP, C.c_int, _VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)])
+    _sig(L, "hella_copy_window", C.c_int, [_VP, C.c_int, _VP])
+    _sig(L, "hella_copy_dedisp", C.c_int, [_VP, _VP])
+    _sig(L, "hella_copy_boxes", C.c_int, [_VP, _VP])
+    _sig(L, "hella_get_smooth_stats", C.c_int, [_VP, _VP, _VP, _VP])
+    _sig(L, "hella_get_flag_stats", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP])
+    _sig(L, "hella_get_flag_spec", C.c_int, [_VP, _VP])
+    _sig(L, "hella_status_string", C.c_char_p, [C.c_int])
+    _sig(L, "hella_fp16_selftest", C.c_int, [C.c_int, C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint32)])
+    _sig(L, "hella_int_add_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)])
+    _sig(L, "hella_kernel_launches", C.c_ulonglong, [])
+    _lib = L
+    return L
+
+
+class HellaError(RuntimeError):
+    pass
+
+
+def _ptr(a) -> int:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _chk_hdd(rc: int) -> None:
+    if rc != 0:
+        raise HellaError(f"{HDD_ERRORS[rc] if rc < len(HDD_ERRORS) else rc}: "
+                         f"{lib().hdd_get_error_string(rc).decode()}")
+
+
+def _chk(rc: int) -> None:
+    if rc != 0:
+        raise HellaError(f"hella status {rc}: {lib().hella_status_string(rc).decode()}")
+
+
+def fp16_selftest(device: int = 0):
+    """(mismatches, first bad pair) of the device fp16 self-check."""
+    n, first = C.c_ulonglong(), C.c_uint32()
+    _chk(lib().hella_fp16_selftest(device, C.byref(n), C.byref(first)))
+    return n.value, first.value
+
+
+def int_add_peak(device: int = 0) -> float:
+    """Measured 32-bit integer adds per second (register-only chains)."""
+    v = C.c_double()
+    _chk(lib().hella_int_add_peak(device, C.byref(v)))
+    return v.value
+
+
+def kernel_launches() -> int:
+    return int(lib().hella_kernel_launches())
+
+
+# --------------------------------------------------------------- hdd plan
+
+class Plan:
+    """The dedisp-shaped plan (hdd_create_plan ... hdd_destroy_plan)."""
+
+    def __init__(self, nchans: int, dt: float, f0: float, df: float):
+        self.L = lib()
+        h = _VP()
+        _chk_hdd(self.L.hdd_create_plan(C.byref(h), nchans, dt, f0, df))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.hdd_destroy_plan(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def generate_dm_list(self, dm_start, dm_end, ti_us, tol):
+        _chk_hdd(self.L.hdd_generate_dm_list(self.h, dm_start, dm_end, ti_us, tol))
+
+    def set_dm_list(self, dms):
+        a = np.ascontiguousarray(dms, dtype=np.float32)
+        _chk_hdd(self.L.hdd_set_dm_list(self.h, a.ctypes.data, a.size))
+
+    def set_killmask(self, mask):
+        a = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        _chk_hdd(self.L.hdd_set_killmask(self.h, None if a is None else a.ctypes.data))
+
+    def set_stream(self, stream: int):
+        _chk_hdd(self.L.hdd_set_stream(self.h, stream))
+
+    @property
+    def dm_count(self) -> int:
+        return int(self.L.hdd_get_dm_count(self.h))
+
+    @property
+    def max_delay(self) -> int:
+        return int(self.L.hdd_get_max_delay(self.h))
+
+    @property
+    def nchans(self) -> int:
+        return int(self.L.hdd_get_channel_count(self.h))
+
+    def dm_list(self) -> np.ndarray:
+        n = self.dm_count
+        p = self.L.hdd_get_dm_list(self.h)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.float32)
+
+    def delay_table(self) -> np.ndarray:
+        p = self.L.hdd_get_delay_table(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.dm_count, self.nchans)).copy()
+
+    def execute_adv(self, nsamps, inp, in_stride, out, out_stride, flags=HDD_HOST_POINTERS, in_nbits=8,
+                    out_nbits=32):
+        _chk_hdd(self.L.hdd_execute_adv(self.h, nsamps, _ptr(inp), in_nbits, in_stride, _ptr(out), out_nbits,
+                                        out_stride, flags))
+
+    def execute_guru(self, nsamps, inp, in_stride, out, out_stride, first, count, flags=HDD_HOST_POINTERS):
+        _chk_hdd(self.L.hdd_execute_guru(self.h, nsamps, _ptr(inp), 8, in_stride, _ptr(out), 32, out_stride,
+                                         first, count, flags))
+
+    def dedisperse(self, data: np.ndarray) -> np.ndarray:
+        """Host convenience: u8 [nsamps][nchans] -> f32 [ndms][nsamps - max_delay]."""
+        data = np.ascontiguousarray(data, dtype=np.uint8)
+        nout = data.shape[0] - self.max_delay
+        out = np.empty((self.dm_count, nout), np.float32)
+        self.execute_adv(data.shape[0], data, data.shape[1], out, nout * 4)
+        return out
+
+
+# ------------------------------------------------------------ hella search
+
+def default_params(**kw) -> HellaParams:
+    p = HellaParams()
+    lib().hella_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "scrunches":
+            p.nscrunch = len(v)
+            for i, (t, f, th, n) in enumerate(v):
+                p.scrunch[i] = HellaScrunch(t, f, n, th)
+            continue
+        setattr(p, k, v)
+    return p
+
+
+class Search:
+    """One search pipeline (hella_create ... hella_destroy)."""
+
+    def __init__(self, params: HellaParams):
+        self.L = lib()
+        h = _VP()
+        _chk(self.L.hella_create(C.byref(h), C.byref(params)))
+        self.h = h
+        self.params = params
+        self.info = self.get_info()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def get_info(self) -> HellaInfo:
+        i = HellaInfo()
+        _chk(self.L.hella_get_info(self.h, C.byref(i)))
+        return i
+
+    def dm_list(self) -> np.ndarray:
+        p = self.L.hella_get_dm_list(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.info.ndms,)).copy()
+
+    def set_stream(self, stream: int):
+        _chk(self.L.hella_set_stream(self.h, stream))
+
+    def set_killmask(self, mask):
+        a = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        _chk(self.L.hella_set_killmask(self.h, None if a is None else a.ctypes.data))
+
+    def load_gulp(self, gulp, on_device=False):
+        _chk(self.L.hella_load_gulp(self.h, _ptr(gulp), int(on_device)))
+
+    def fast_flagger(self):
+        _chk(self.L.hella_fast_flagger(self.h))
+
+    def dedisperse(self, beam: int):
+        _chk(self.L.hella_dedisperse(self.h, beam))
+
+    def smooth(self, scale: int = 1):
+        _chk(self.L.hella_smooth(self.h, scale))
+
+    def find_peaks(self, beam: int):
+        _chk(self.L.hella_find_peaks(self.h, beam))
+
+    def clear_peaks(self):
+        _chk(self.L.hella_clear_peaks(self.h))
+
+    def rewind(self):
+        _chk(self.L.hella_rewind(self.h))
+
+    def get_peaks(self, max_n: int | None = None) -> np.ndarray:
+        max_n = self.params.max_giants if max_n is None else max_n
+        out = np.zeros(max_n, CAND_DTYPE)
+        n = C.c_int()
+        _chk(self.L.hella_get_peaks(self.h, out.ctypes.data, max_n, C.byref(n)))
+        return out[: n.value]
+
+    def process_gulp(self, gulp, on_device=False):
+        """Returns (candidates, searched)."""
+        out = np.zeros(self.params.max_giants, CAND_DTYPE)
+        n, s = C.c_int(), C.c_int()
+        _chk(self.L.hella_process_gulp(self.h, _ptr(gulp), int(on_device), out.ctypes.data,
+                                       self.params.max_giants, C.byref(n), C.byref(s)))
+        self.info = self.get_info()
+        return out[: n.value], bool(s.value)
+
+    def copy_window(self, beam: int) -> np.ndarray:
+        out = np.empty((self.info.ntime, self.params.nchan), np.uint8)
+        _chk(self.L.hella_copy_window(self.h, beam, out.ctypes.data))
+        return out
+
+    def copy_dedisp(self) -> np.ndarray:
+        out = np.empty((self.info.ndms, self.info.ntime_dd), np.float32)
+        _chk(self.L.hella_copy_dedisp(self.h, out.ctypes.data))
+        return out
+
+    def copy_boxes(self) -> np.ndarray:
+        i = self.info
+        out = np.empty((i.nboxcar, i.ndms - 2, i.ntime_out), np.float32)
+        _chk(self.L.hella_copy_boxes(self.h, out.ctypes.data))
+        return out
+
+    def smooth_stats(self):
+        n = self.info.nboxcar
+        mean, std, s0 = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(1, np.float32)
+        _chk(self.L.hella_get_smooth_stats(self.h, mean.ctypes.data, std.ctypes.data, s0.ctypes.data))
+        return mean, std, float(s0[0])
+
+    def flag_stats(self, beam: int):
+        nch = self.params.nchan
+        bp1, bp2, bp3 = (np.zeros(nch, np.float32) for _ in range(3))
+        sc = np.zeros(4, np.float32)
+        ts = np.zeros(self.params.gulp, np.float32)
+        _chk(self.L.hella_get_flag_stats(self.h, beam, bp1.ctypes.data, bp2.ctypes.data, bp3.ctypes.data,
+                                         sc.ctypes.data, ts.ctypes.data))
+        return dict(bp1=bp1, bp2=bp2, bp3=bp3, mean1=sc[0], std1=sc[1], mean2=sc[2], std2=sc[3], ts=ts)
+
+    def flag_spec(self) -> np.ndarray:
+        out = np.zeros(self.params.nchan, np.float32)
+        _chk(self.L.hella_get_flag_spec(self.h, out.ctypes.data))
+        return out

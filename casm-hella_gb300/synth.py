@@ -1,0 +1,177 @@
+"""Seeded synthetic filterbank gulps for the search's parity tests and bench.
+
+No public dataset is named for this path; these generators stand in for it
+with the shapes and value distributions of the search configurations:
+u8 samples ~ round(N(mean, sd)) clipped to 0..255, narrowband RFI channels
+with a larger sd, broadband impulses, and dispersed Gaussian bursts.  The
+dispersion follows the reference's injection script
+(scripts/make_noise_fil_with_frb.py:123-173): per-channel delay
+4.148808 ms DM (f_GHz^-2 - f0_GHz^-2) rounded to whole samples, a Gaussian
+pulse painted within +-4 sigma of each channel's arrival.  Every gulp is a
+pure function of (seed, gulp index), so a stream can be regenerated
+anywhere, and bursts that straddle gulps are painted consistently.
+"""
+from __future__ import annotations
+
+import dataclasses as dc
+import math
+
+import numpy as np
+
+K_MS = 4.148808  # ms GHz^2 / (pc cm^-3)
+
+
+@dc.dataclass
+class Burst:
+    t0: int            # absolute arrival sample at channel 0 (f0)
+    dm: float
+    fwhm_ms: float
+    amp: float         # counts per channel at f0 (before the spectral index)
+    index: float = 0.0
+
+
+@dc.dataclass
+class Spike:
+    t0: int            # absolute first sample
+    width: int         # samples
+    amp: float         # counts, all channels
+
+
+@dc.dataclass
+class Sky:
+    nchan: int
+    tsamp: float       # s
+    f0: float          # MHz, channel 0
+    df: float          # MHz per channel (negative: descending)
+    seed: int
+    mean: float = 128.0
+    sd: float = 20.0
+    rfi_chans: tuple = ()
+    rfi_sd: float = 80.0
+    slope: float = 0.0              # bandpass gain 1 + slope*(c/(nchan-1) - 0.5)
+    bursts: list = dc.field(default_factory=list)
+    spikes: list = dc.field(default_factory=list)
+
+    def freqs(self) -> np.ndarray:
+        return self.f0 + np.arange(self.nchan) * self.df
+
+    def delays(self, dm: float) -> np.ndarray:
+        f = self.freqs() / 1000.0
+        ms = K_MS * dm * (1.0 / f**2 - 1.0 / (self.f0 / 1000.0) ** 2)
+        return np.round(ms / (self.tsamp * 1000.0)).astype(np.int64)
+
+    def gulp(self, g: int, n: int) -> np.ndarray:
+        """Samples [g*n, (g+1)*n) as u8 [n][nchan]."""
+        rng = np.random.Generator(np.random.PCG64([self.seed, g]))
+        x = rng.standard_normal((n, self.nchan), dtype=np.float32)
+        sd = np.full(self.nchan, self.sd, np.float32)
+        if len(self.rfi_chans):
+            sd[list(self.rfi_chans)] = self.rfi_sd
+        gain = 1.0 + self.slope * (np.arange(self.nchan, dtype=np.float32) / max(1, self.nchan - 1) - 0.5)
+        x *= sd
+        x += (self.mean * gain).astype(np.float32)
+        a0 = g * n
+        for s in self.spikes:
+            lo, hi = max(s.t0, a0), min(s.t0 + s.width, a0 + n)
+            if lo < hi:
+                x[lo - a0:hi - a0] += s.amp
+        f = self.freqs()
+        for b in self.bursts:
+            dl = self.delays(b.dm)
+            sig = max(1.0, b.fwhm_ms / 2.3548 / (self.tsamp * 1000.0))
+            hw = int(math.ceil(4.0 * sig))
+            centers = b.t0 + dl
+            sel = np.nonzero((centers + hw >= a0) & (centers - hw < a0 + n))[0]
+            if sel.size == 0:
+                continue
+            spec = b.amp * (f[sel] / self.f0) ** b.index
+            offs = np.arange(-hw, hw + 1)
+            prof = np.exp(-0.5 * (offs / sig) ** 2)
+            tt = centers[sel][:, None] + offs[None, :] - a0
+            ok = (tt >= 0) & (tt < n)
+            cc = np.broadcast_to(sel[:, None], tt.shape)
+            np.add.at(x, (tt[ok], cc[ok]), (spec[:, None] * prof[None, :])[ok].astype(np.float32))
+        np.rint(x, out=x)
+        np.clip(x, 0, 255, out=x)
+        return x.astype(np.uint8)
+
+
+def snr_amp(snr: float, sd: float, nchan: int, fwhm_ms: float, tsamp: float) -> float:
+    """Per-channel amplitude of a flat-spectrum Gaussian with band-integrated
+    matched-filter S/N `snr` in noise of `sd` counts."""
+    sig = max(1.0, fwhm_ms / 2.3548 / (tsamp * 1000.0))
+    return snr * sd / math.sqrt(nchan * sig * math.sqrt(math.pi))
+
+
+# ------------------------------------------------------------ configurations
+F0, FLO = 468.75, 375.0
+
+
+def first_window(sky: Sky, gulp: int, dm_max: float, wmax: int):
+    """(gulp index, first absolute sample, NTIME) of the first searched
+    window, from the search geometry (casm_hella_refactored.cu:217-224,632):
+    NTIME = 32*((gulp + max_delay + wmax)//32 + 1), searched from gulp
+    NTIME//gulp on, window = the last NTIME samples of that gulp."""
+    md = int(sky.delays(dm_max).max())
+    ntime = 32 * ((gulp + md + wmax) // 32 + 1)
+    g = ntime // gulp
+    return g, (g + 1) * gulp - ntime, ntime
+
+
+def place(rng, sky: Sky, gulp: int, dm_max: float, wmax: int, dm: float, fwhm_ms: float) -> int:
+    """A channel-0 arrival sample inside the first searched window's output
+    span whose whole dispersed sweep has arrived by the end of that gulp."""
+    g, ws, _ = first_window(sky, gulp, dm_max, wmax)
+    pad = wmax + int(4 * fwhm_ms / (sky.tsamp * 1000.0)) + 8
+    lo = ws + pad
+    hi = min(ws + gulp - pad, (g + 1) * gulp - int(sky.delays(dm).max()) - pad)
+    return int(rng.integers(lo, max(lo + 1, hi)))
+
+
+def config_plain(seed: int = 1, nchan: int = 512, gulp: int = 16384, dm_max: float = 500.0):
+    """Plain single-beam search: 512 ch over 375-468.75 MHz, tsamp
+    1.048576 ms, gulp 16384; noise N(128, 20), 4 RFI channels (sd 80), three
+    +60 broadband impulses of 5 samples, one flat-spectrum burst at DM 300,
+    FWHM 2 ms, band-integrated S/N 20; DM 0-500 at tolerance 1.25 for a
+    0.5 ms pulse; widths 1..32; 7 sigma."""
+    rng = np.random.default_rng(seed)
+    tsamp = 1.048576e-3
+    df = -(F0 - FLO) / nchan
+    rfi = tuple(int(c) for c in rng.choice(nchan, 4, replace=False))
+    sky = Sky(nchan, tsamp, F0, df, seed, 128.0, 20.0, rfi, 80.0, 0.0, [], [])
+    g, ws, _ = first_window(sky, gulp, dm_max, 64)
+    sky.spikes = [Spike(int(ws + rng.integers(0, gulp)), 5, 60.0) for _ in range(3)]
+    amp = snr_amp(20.0, 20.0, nchan, 2.0, tsamp)
+    sky.bursts = [Burst(place(rng, sky, gulp, dm_max, 64, 300.0, 2.0), 300.0, 2.0, amp, 0.0)]
+    params = dict(nchan=nchan, nbeam=1, gulp=gulp, tsamp=tsamp, plan_dt=tsamp, f0_mhz=F0, df_mhz=df,
+                  dm_min=0.0, dm_max=dm_max, dm_tol=1.25, ti_us=500.0, width_min=1, width_max=64, snr=7.0)
+    return params, sky
+
+
+def config_full(seed: int = 2, nchan: int = 2048, gulp: int = 65536, dm_max: float = 2000.0):
+    """Full single beam: 2048 ch over 375-468.75 MHz, tsamp 0.524288 ms,
+    gulp 65536; N(128, 16) with a +-30% bandpass slope, 2% RFI channels
+    (sd x4), 10 broadband spikes, 8 bursts with DM U[100,1800], FWHM
+    logU[0.5,10] ms, S/N 8-50, spectral index -2..2; DM 0-2000 at tolerance
+    1.25; widths 1..256."""
+    rng = np.random.default_rng(seed)
+    tsamp = 0.524288e-3
+    df = -(F0 - FLO) / nchan
+    rfi = tuple(int(c) for c in rng.choice(nchan, max(1, nchan // 50), replace=False))
+    sky = Sky(nchan, tsamp, F0, df, seed, 128.0, 16.0, rfi, 64.0, float(rng.choice([-0.6, 0.6])), [], [])
+    g, ws, _ = first_window(sky, gulp, dm_max, 512)
+    sky.spikes = [Spike(int(ws + rng.integers(0, gulp)), int(rng.integers(1, 6)), 40.0) for _ in range(10)]
+    for _ in range(8):
+        dm = float(rng.uniform(100, min(1800.0, dm_max)))
+        fwhm = float(np.exp(rng.uniform(np.log(0.5), np.log(10.0))))
+        snr = float(rng.uniform(8, 50))
+        sky.bursts.append(Burst(place(rng, sky, gulp, dm_max, 512, dm, fwhm), dm, fwhm,
+                                snr_amp(snr, 16.0, nchan, fwhm, tsamp), float(rng.uniform(-2, 2))))
+    params = dict(nchan=nchan, nbeam=1, gulp=gulp, tsamp=tsamp, plan_dt=tsamp, f0_mhz=F0, df_mhz=df,
+                  dm_min=0.0, dm_max=dm_max, dm_tol=1.25, ti_us=40.0, width_min=1, width_max=512, snr=7.0)
+    return params, sky
+
+
+def multibeam_gulp(skies, g: int, n: int) -> np.ndarray:
+    """u8 [nbeam][n][nchan] for gulp g of every beam's sky."""
+    return np.stack([s.gulp(g, n) for s in skies])

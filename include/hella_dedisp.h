@@ -1,0 +1,130 @@
+/*
+ * hella_dedisp.h -- brute-force direct dedispersion on GB300 (sm_103a),
+ * with the plan/execute interface casm-hella drives through the dedisp
+ * library.  The function set mirrors that interface one for one under the
+ * `hdd_` prefix, so a caller swaps `dedisp_` for `hdd_` and links
+ * libhella_gb300.so.  Reference call sites replaced (Coherent-All-Sky-
+ * Monitor/casm-hella):
+ *   src/apps/casm_hella_refactored.cu:205   dedisp_create_plan
+ *   src/apps/casm_hella_refactored.cu:207   dedisp_generate_dm_list
+ *   src/apps/casm_hella_refactored.cu:208   dedisp_get_dm_list
+ *   src/apps/casm_hella_refactored.cu:209   dedisp_get_dm_count
+ *   src/apps/casm_hella_refactored.cu:210   dedisp_get_max_delay
+ *   src/hella/src/dedisperse.cpp:32-38       dedisp_execute_adv
+ *   src/hella/src/dedisperse.cpp:50-91       error names (dedisp_error)
+ *
+ * Conventions (the dedisp library is not part of the reference; these are
+ * this library's definitions, restated from the published method):
+ *   - channel 0 is the highest frequency f0; channel c is f0 - c*|df| (MHz);
+ *   - delay(c, DM) = (int)(DM * tab[c] + 0.5f) in fp32, with
+ *     tab[c] = 4.148808e3 (1/f_c^2 - 1/f0^2) / dt samples per unit DM;
+ *   - the DM list follows the Cordes & McLaughlin smearing tolerance;
+ *   - out_nbits = 32 writes each sum as the exact integer in fp32;
+ *   - in_nbits = 8: unsigned bytes, time-major, in_stride bytes per sample.
+ * Every call returns a status; nothing exits or throws.  One plan per
+ * thread; all device work is issued on the plan's stream.
+ */
+#ifndef HELLA_DEDISP_H
+#define HELLA_DEDISP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hdd_plan_struct *hdd_plan;
+typedef unsigned long hdd_size;
+typedef float hdd_float;
+typedef unsigned char hdd_byte;
+typedef int hdd_bool;
+
+/* Same order and meaning as the names at dedisperse.cpp:54-88. */
+typedef enum {
+  HDD_NO_ERROR = 0,
+  HDD_MEM_ALLOC_FAILED,
+  HDD_MEM_COPY_FAILED,
+  HDD_NCHANS_EXCEEDS_LIMIT,
+  HDD_INVALID_PLAN,
+  HDD_INVALID_POINTER,
+  HDD_INVALID_STRIDE,
+  HDD_NO_DM_LIST_SET,
+  HDD_TOO_FEW_NSAMPS,
+  HDD_INVALID_FLAG_COMBINATION,
+  HDD_UNSUPPORTED_IN_NBITS,
+  HDD_UNSUPPORTED_OUT_NBITS,
+  HDD_INVALID_DEVICE_INDEX,
+  HDD_DEVICE_ALREADY_SET,
+  HDD_PRIOR_GPU_ERROR,
+  HDD_INTERNAL_GPU_ERROR,
+  HDD_UNKNOWN_ERROR
+} hdd_error;
+
+/* Execute flags; the reference passes 1<<2 (device pointers,
+ * dedisperse.cpp:417). */
+#define HDD_USE_DEFAULT 0
+#define HDD_HOST_POINTERS (1 << 1)
+#define HDD_DEVICE_POINTERS (1 << 2)
+#define HDD_WAIT (1 << 3)
+#define HDD_ASYNC (1 << 4)
+
+#define HDD_MAX_NCHANS 16384
+
+/* dedisp_create_plan (casm_hella_refactored.cu:205): nchans channels of
+ * width df (MHz, sign ignored) below f0 (MHz), samples of dt seconds. */
+hdd_error hdd_create_plan(hdd_plan *plan, hdd_size nchans, hdd_float dt,
+                          hdd_float f0, hdd_float df);
+void hdd_destroy_plan(hdd_plan plan);
+
+/* Selects the CUDA device for plans created afterwards on this thread. */
+hdd_error hdd_set_device(int device_idx);
+/* Stream (a cudaStream_t passed as void*) for the plan's device work;
+ * NULL selects the legacy default stream. */
+hdd_error hdd_set_stream(hdd_plan plan, void *stream);
+
+hdd_error hdd_set_dm_list(hdd_plan plan, const hdd_float *dm_list,
+                          hdd_size count);
+/* dedisp_generate_dm_list (casm_hella_refactored.cu:207): trials from
+ * dm_start until >= dm_end for a pulse of width ti (microseconds) and
+ * smearing tolerance tol. */
+hdd_error hdd_generate_dm_list(hdd_plan plan, hdd_float dm_start,
+                               hdd_float dm_end, hdd_float ti, hdd_float tol);
+/* killmask[c] == 0 drops channel c from every sum. */
+hdd_error hdd_set_killmask(hdd_plan plan, const hdd_bool *killmask);
+
+hdd_size hdd_get_max_delay(const hdd_plan plan);
+hdd_size hdd_get_dm_delay(const hdd_plan plan, int dm_trial);
+hdd_size hdd_get_channel_count(const hdd_plan plan);
+hdd_size hdd_get_dm_count(const hdd_plan plan);
+const hdd_float *hdd_get_dm_list(const hdd_plan plan);
+const hdd_bool *hdd_get_killmask(const hdd_plan plan);
+hdd_float hdd_get_dt(const hdd_plan plan);
+hdd_float hdd_get_df(const hdd_plan plan);
+hdd_float hdd_get_f0(const hdd_plan plan);
+/* Host copy of the integer delay table, [dm_count][nchans]. */
+const int *hdd_get_delay_table(const hdd_plan plan);
+
+/* out[d][t] for t < nsamps - max_delay (dedisp_execute). */
+hdd_error hdd_execute(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
+                      hdd_size in_nbits, hdd_byte *out, hdd_size out_nbits,
+                      unsigned flags);
+/* dedisp_execute_adv (dedisperse.cpp:418): strides in bytes. */
+hdd_error hdd_execute_adv(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
+                          hdd_size in_nbits, hdd_size in_stride,
+                          hdd_byte *out, hdd_size out_nbits,
+                          hdd_size out_stride, unsigned flags);
+/* Subset of DM trials [first_dm_idx, first_dm_idx + dm_count); output row
+ * 0 is trial first_dm_idx. */
+hdd_error hdd_execute_guru(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
+                           hdd_size in_nbits, hdd_size in_stride,
+                           hdd_byte *out, hdd_size out_nbits,
+                           hdd_size out_stride, hdd_size first_dm_idx,
+                           hdd_size dm_count, unsigned flags);
+
+/* Text for a status, as get_dedisp_error (dedisperse.cpp:50-91). */
+const char *hdd_get_error_string(hdd_error error);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,175 @@
+/*
+ * hella_search.h -- casm-hella's per-gulp FRB search stages on GB300.
+ *
+ * Replaces the stage functions of Coherent-All-Sky-Monitor/casm-hella that
+ * the gulp loop (src/apps/casm_hella_refactored.cu:659-835) calls, over an
+ * opaque context instead of the monolithic pinfo_t (src/hella/
+ * definitions.h:84-173):
+ *
+ *   hella_create / hella_destroy   initialize (casm_hella_refactored.cu:54-309)
+ *                                  / deallocator (:312-335)
+ *   hella_load_gulp                H2D copy of a gulp (:688-695)
+ *   hella_fast_flagger             fast_flagger   src/hella/flagger.h:75
+ *   hella_dedisperse               dedisperse     src/hella/dedisperse.h:17
+ *   hella_smooth                   smooth         src/hella/smooth.h:16
+ *   hella_find_peaks               find_peaks     src/hella/peaks.h:17
+ *   hella_clear_peaks              clear_peaks    src/hella/peaks.h:20
+ *   hella_rewind                   ring rewind    (:775-797)
+ *   hella_process_gulp             one pass of the loop body (:659-835)
+ *
+ * Every call returns a hella_status; CUDA and argument errors come back as
+ * codes instead of exit() (macros.h:14-28).  All device work runs on the
+ * context's stream.  A context is not thread-safe.
+ */
+#ifndef HELLA_SEARCH_H
+#define HELLA_SEARCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hella_ctx hella_ctx;
+
+typedef enum {
+  HELLA_OK = 0,
+  HELLA_ERR_INVALID_ARG = 1,  /* a parameter is out of range */
+  HELLA_ERR_ALLOC = 2,        /* device or pinned host allocation failed */
+  HELLA_ERR_CUDA = 3,         /* a CUDA call failed (context left usable) */
+  HELLA_ERR_STATE = 4,        /* stage called out of order */
+  HELLA_ERR_DEDISP = 5,       /* the dedispersion plan rejected the call */
+  HELLA_ERR_BUDGET = 6,       /* HBM budget would be exceeded */
+  HELLA_ERR_TIMEOUT = 7       /* a bounded device wait expired */
+} hella_status;
+
+#define HELLA_MAX_SCRUNCH 16
+#define HELLA_MAX_GIANTS 10000 /* definitions.h:49 */
+
+/* One SCRUNCH line "t f thresh nits" (definitions.h:76-81). */
+typedef struct {
+  int tscrunch, fscrunch, nits;
+  float thresh;
+} hella_scrunch;
+
+/* Search configuration: the config keys of casm_hella_refactored.cu:72-169,
+ * with the band (nchan, tsamp, f0, df) made runtime. */
+typedef struct {
+  int nchan;        /* NCHAN (definitions.h:44 fixes 3072) */
+  int nbeam;        /* NBEAM */
+  int gulp;         /* GULP, samples; a multiple of 32 */
+  double tsamp;     /* data sample time, s */
+  double plan_dt;   /* dt of the dedispersion plan (reference: 1e-3) */
+  double f0_mhz;    /* frequency of channel 0 (CHAN0_FREQ) */
+  double df_mhz;    /* channel width (FREQ_CHANNEL_WIDTH) */
+  float dm_min, dm_max, dm_tol; /* DM_MIN, DM_MAX, DM_TOL (default 1.3) */
+  float ti_us;      /* pulse width for the DM list (reference: 40) */
+  int width_min, width_max;     /* WIDTH_MIN, WIDTH_MAX */
+  float snr;        /* SNR */
+  float spec_min, spec_max;     /* SPEC_MIN / SPEC_MAX (-0.05 / 0.15) */
+  int flag1, flag2;             /* FLAG1 / FLAG2 (-1 / -1) */
+  int nscrunch;                 /* SCRUNCH n */
+  hella_scrunch scrunch[HELLA_MAX_SCRUNCH];
+  int max_giants;   /* candidate cap per gulp (MAX_GIANTS) */
+  int beam0;        /* BEAM0, added to reported beam indices */
+  int smooth_anchor;/* 0: smoothing kernel anchored at its first tap (the
+                       reference's oAnchor {0,1}); 1: at its last tap */
+  int device;       /* GPU */
+  size_t hbm_budget;/* 0 = unlimited; otherwise creation fails with
+                       HELLA_ERR_BUDGET if the context would need more */
+} hella_params;
+
+/* Derived sizes (casm_hella_refactored.cu:184-224). */
+typedef struct {
+  int ntime;        /* NTIME: gulp + max_delay + width_max rounded up */
+  int ndms;         /* DM trials */
+  int max_delay;    /* samples */
+  int ntime_dd;     /* gulp + width_max: dedispersed samples kept */
+  int ntime_out;    /* gulp */
+  int nboxcar;      /* smoothing widths width_min*2^k < width_max */
+  int min_gulp;     /* first gulp index that is searched */
+  int gulp_index;   /* gulps processed so far */
+  size_t device_bytes; /* device memory held by the context */
+} hella_info;
+
+/* One candidate: a sample above SNR x sigma (peaks.cu:232-242). */
+typedef struct {
+  int32_t beam;     /* beam index + beam0 */
+  int32_t dm_idx;   /* DM trial (row + 1 of the smoothed plane) */
+  int32_t width;    /* smoothing width index */
+  int32_t samp;     /* sample within the gulp's output window */
+  float snr;        /* normalised smoothed value */
+} hella_cand;
+
+void hella_params_default(hella_params *p);
+hella_status hella_create(hella_ctx **ctx, const hella_params *p);
+void hella_destroy(hella_ctx *ctx);
+hella_status hella_set_stream(hella_ctx *ctx, void *stream);
+hella_status hella_get_info(const hella_ctx *ctx, hella_info *info);
+/* DM of each trial (host memory owned by the context). */
+const float *hella_get_dm_list(const hella_ctx *ctx);
+/* Killmask shared by all beams (0 = channel dropped from dedispersion). */
+hella_status hella_set_killmask(hella_ctx *ctx, const int *killmask);
+
+/* Gulp input: u8 [nbeam][gulp][nchan] (time-major, as a SIGPROC gulp);
+ * on_device != 0 means `gulp` is a device pointer. */
+hella_status hella_load_gulp(hella_ctx *ctx, const uint8_t *gulp,
+                             int on_device);
+hella_status hella_fast_flagger(hella_ctx *ctx);
+hella_status hella_dedisperse(hella_ctx *ctx, int beam);
+hella_status hella_smooth(hella_ctx *ctx, int scale);
+hella_status hella_find_peaks(hella_ctx *ctx, int beam);
+hella_status hella_clear_peaks(hella_ctx *ctx);
+hella_status hella_rewind(hella_ctx *ctx);
+/* Candidates gathered since the last clear (host copy). */
+hella_status hella_get_peaks(hella_ctx *ctx, hella_cand *out, int max,
+                             int *n);
+/* Load + flag + (search every beam while under max_giants, once the ring
+ * is full) + rewind.  *searched is set to 1 when the search ran. */
+hella_status hella_process_gulp(hella_ctx *ctx, const uint8_t *gulp,
+                                int on_device, hella_cand *out, int max,
+                                int *n, int *searched);
+
+/* Inspection (host copies, synchronous). */
+/* The beam's search window, u8 [ntime][nchan] time-major, oldest first. */
+hella_status hella_copy_window(hella_ctx *ctx, int beam, uint8_t *out);
+/* Last dedispersed plane, fp32 [ndms][ntime_dd]. */
+hella_status hella_copy_dedisp(hella_ctx *ctx, float *out);
+/* Last normalised smoothed planes, fp32 [nboxcar][ndms-2][ntime_out]. */
+hella_status hella_copy_boxes(hella_ctx *ctx, float *out);
+/* Per-width mean/std before normalisation and the peak gate sigma. */
+hella_status hella_get_smooth_stats(hella_ctx *ctx, float *mean,
+                                    float *std, float *sigma0);
+/* Flagger statistics of a beam's last gulp: bp1/bp2/bp3 [nchan] and
+ * scalars[4] = {mean1, std1, mean2, std2}; any pointer may be NULL. */
+hella_status hella_get_flag_stats(hella_ctx *ctx, int beam, float *bp1,
+                                  float *bp2, float *bp3, float *scalars,
+                                  float *ts);
+/* Accumulated per-channel flag fractions (d_flagSpec, flagger.cu:334). */
+hella_status hella_get_flag_spec(hella_ctx *ctx, float *out);
+
+const char *hella_status_string(hella_status s);
+
+/* Device self-check of the fp16 arithmetic the flagger relies on (no
+ * counterpart in the reference, whose kernels simply call these
+ * intrinsics): over every pair of positive finite binary16 values, counts
+ * the cases where __hdiv differs from the correctly rounded quotient
+ * (fp32 IEEE division rounded once to fp16), and likewise __hadd/__hmul on
+ * a strided subset.  first_bad receives (a << 16 | b) of the first
+ * mismatch.  Synchronous. */
+hella_status hella_fp16_selftest(int device, unsigned long long *mismatches,
+                                 uint32_t *first_bad);
+
+/* Measurement helpers (no counterpart in the reference).
+ * hella_int_add_peak: 32-bit integer adds per second the device sustains
+ * from registers (independent add chains on every SM, timed with CUDA
+ * events); the dedispersion roofline's denominator.  Synchronous.
+ * hella_kernel_launches: kernels this library has launched in this process. */
+hella_status hella_int_add_peak(int device, double *adds_per_s);
+unsigned long long hella_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,32 @@
+"""Shared helpers for the tests: parameter plumbing between the product's
+C-ABI parameters and the oracle pipeline."""
+import numpy as np
+
+
+def oracle_pipeline(oracle, params: dict, **over):
+    p = dict(params)
+    p.update(over)
+    return oracle.Pipeline(
+        nchan=p["nchan"], nbeam=p.get("nbeam", 1), gulp=p["gulp"], tsamp=p["tsamp"], plan_dt=p["plan_dt"],
+        f0=p["f0_mhz"], df=p["df_mhz"], dm_min=p["dm_min"], dm_max=p["dm_max"], dm_tol=p["dm_tol"],
+        ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
+        max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 0),
+        spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15))
+
+
+def small_params(**over):
+    """A small search that the oracle finishes in well under a second."""
+    p = dict(nchan=128, nbeam=1, gulp=2048, tsamp=1.048576e-3, plan_dt=1.048576e-3, f0_mhz=468.75,
+             df_mhz=-(468.75 - 375.0) / 128, dm_min=0.0, dm_max=120.0, dm_tol=1.25, ti_us=500.0,
+             width_min=1, width_max=16, snr=6.0)
+    p.update(over)
+    return p
+
+
+def cands_equal(a: np.ndarray, b: np.ndarray) -> bool:
+    if len(a) != len(b):
+        return False
+    for k in ("beam", "dm_idx", "width", "samp"):
+        if not np.array_equal(a[k], b[k]):
+            return False
+    return np.array_equal(a["snr"].view(np.uint32), b["snr"].view(np.uint32))

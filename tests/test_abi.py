@@ -1,0 +1,77 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every
+function include/*.h declares, its host-side plan math equals the oracle's
+bit for bit, and argument errors come back as status codes."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b((?:hdd|hella)_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(hella):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(hella.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    assert len(declared_functions()) > 40
+
+
+def test_plan_math_matches_oracle(hella, oracle):
+    """hdd_create_plan + hdd_generate_dm_list (host only) against the oracle."""
+    for nchan, dt, dm_max, ti, tol in [(512, 1.048576e-3, 500.0, 500.0, 1.25), (2048, 0.524288e-3, 2000.0, 40.0, 1.25),
+                                       (3072, 1e-3, 1000.0, 40.0, 1.3)]:
+        f0 = 468.75
+        df = -(f0 - 375.0) / nchan if nchan != 3072 else -0.03075
+        plan = hella.Plan(nchan, dt, f0, df)
+        plan.generate_dm_list(0.0, dm_max, ti, tol)
+        f32 = lambda v: float(np.float32(v))
+        dms = oracle.dm_list(0.0, f32(dm_max), f32(ti), f32(tol), nchan, f32(dt), f32(f0), f32(df))
+        assert np.array_equal(plan.dm_list().view(np.uint32), dms.view(np.uint32))
+        delays = oracle.dm_delays(dms, oracle.delay_table(nchan, f32(dt), f32(f0), f32(df)))
+        assert np.array_equal(plan.delay_table(), delays)
+        assert plan.max_delay == delays[-1, -1]
+        plan.close()
+
+
+def test_plan_error_codes(hella):
+    L = hella.lib()
+    h = C.c_void_p()
+    assert L.hdd_create_plan(C.byref(h), 0, 1e-3, 468.75, -0.1) == 3  # nchans exceeds limit
+    assert L.hdd_create_plan(C.byref(h), 64, 1e-3, 468.75, -0.5) == 0
+    buf = np.zeros(16, np.uint8)
+    # no DM list yet
+    assert L.hdd_execute(h, 10, buf.ctypes.data, 8, buf.ctypes.data, 32, 0) in (7, 8)
+    L.hdd_generate_dm_list(h, 0.0, 50.0, 40.0, 1.3)
+    md = L.hdd_get_max_delay(h)
+    assert L.hdd_execute_adv(h, md, buf.ctypes.data, 8, 64, buf.ctypes.data, 32, 4, 0) == 8  # too few nsamps
+    assert L.hdd_execute_adv(h, md + 10, buf.ctypes.data, 4, 64, buf.ctypes.data, 32, 40, 0) == 10
+    assert L.hdd_execute_adv(h, md + 10, buf.ctypes.data, 8, 64, buf.ctypes.data, 16, 40, 0) == 11
+    assert L.hdd_execute_adv(h, md + 10, buf.ctypes.data, 8, 32, buf.ctypes.data, 32, 40, 0) == 6
+    assert L.hdd_execute_adv(h, md + 10, buf.ctypes.data, 8, 64, buf.ctypes.data, 32, 39, 0) == 6
+    assert L.hdd_execute_adv(h, md + 10, buf.ctypes.data, 8, 64, buf.ctypes.data, 32, 40,
+                             hella.HDD_HOST_POINTERS | hella.HDD_DEVICE_POINTERS) == 9
+    assert L.hdd_get_error_string(6) == b"invalid stride"
+    L.hdd_destroy_plan(h)
+
+
+def test_search_rejects_bad_params(hella):
+    L = hella.lib()
+    h = C.c_void_p()
+    for bad in (dict(nchan=100), dict(gulp=100), dict(width_max=1), dict(dm_tol=1.0), dict(smooth_anchor=3)):
+        p = hella.default_params(**bad)
+        assert L.hella_create(C.byref(h), C.byref(p)) == 1
+    assert L.hella_status_string(6) == b"hbm budget exceeded"

@@ -43,7 +43,7 @@ UNIT = "beam·s/s"
 def args_():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -85,7 +85,7 @@ class Clocks:
         sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(sm)}
 
@@ -131,7 +131,7 @@ def cpu_sample(params, gulp, dm_rows: int = 128):
     boxes = np.zeros((nbox, dm_rows - 2, G), np.float32)
     m, s = np.zeros(nbox, np.float32), np.zeros(nbox, np.float32)
     L = oracle.lib()
-    L.ho_smooth_normalise(dd.ctypes.data, dm_rows, ntd, ntd, params["width_min"], wmax, 0, G, boxes.ctypes.data,
+    L.ho_smooth_normalise(dd.ctypes.data, dm_rows, ntd, ntd, params["width_min"], wmax, 1, G, boxes.ctypes.data,
                           m.ctypes.data, s.ctypes.data)
     cands = np.zeros(10000, oracle.CAND_DTYPE)
     L.ho_find_peaks(boxes.ctypes.data, nbox, dm_rows, G, params["snr"], 0, 10000, cands.ctypes.data, None)
@@ -225,7 +225,6 @@ def main():
         fl_ms.append(e[0].elapsed_time(e[1]))
         dd_ms.append(e[1].elapsed_time(e[2]))
         sm_ms.append(e[2].elapsed_time(e[3]))
-    clk = clocks.stop()
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -253,6 +252,8 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * a.steps * gulp_s / e2e_s
+
+    clk = clocks.stop()
 
     # ---------------- rooflines
     nact = nch

@@ -165,7 +165,7 @@ void hella_params_default(hella_params *p) {
   p->flag1 = -1;
   p->flag2 = -1;
   p->max_giants = HELLA_MAX_GIANTS;
-  p->smooth_anchor = 0;
+  p->smooth_anchor = 1;
 }
 
 void hella_destroy(hella_ctx *c) {

@@ -73,8 +73,10 @@ typedef struct {
   hella_scrunch scrunch[HELLA_MAX_SCRUNCH];
   int max_giants;   /* candidate cap per gulp (MAX_GIANTS) */
   int beam0;        /* BEAM0, added to reported beam indices */
-  int smooth_anchor;/* 0: smoothing kernel anchored at its first tap (the
-                       reference's oAnchor {0,1}); 1: at its last tap */
+  int smooth_anchor;/* where the 2sm+1 smoothing taps sit relative to output
+                       sample x: 1 (default) inputs x-2sm..x, which is where
+                       nppiFilterBorder_32f_C1R places the reference's
+                       oAnchor {0,1} (smooth.cpp:54); 0: inputs x..x+2sm */
   int device;       /* GPU */
   size_t hbm_budget;/* 0 = unlimited; otherwise creation fails with
                        HELLA_ERR_BUDGET if the context would need more */

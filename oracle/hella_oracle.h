@@ -135,9 +135,10 @@ void ho_smooth_plane(const float *dd, int ndms, int ntime_dd, size_t dd_stride,
 
 /* smooth(p, scale=1): every width sm = wmin*2^k < wmax, then per-width
  * (x + (-mean)) * (1/std) unless std <= 0.  boxes: [nbox][ndms-2][ntime_out]
- * packed.  mean/std: [nbox] (pre-normalisation statistics).  anchor 0: the
- * kernel's first tap sits on the output sample (the reference's oAnchor
- * {0,1}); 1: its last tap.  Returns nbox. */
+ * packed.  mean/std: [nbox] (pre-normalisation statistics).  anchor 1: the
+ * kernel's last tap sits on the output sample, which is where
+ * nppiFilterBorder_32f_C1R places the reference's oAnchor {0,1} (an impulse
+ * response measured on a GB300); 0: its first tap.  Returns nbox. */
 int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
                         size_t dd_stride, int wmin, int wmax, int anchor,
                         int ntime_out, float *boxes, float *mean, float *std);

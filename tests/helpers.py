@@ -10,7 +10,7 @@ def oracle_pipeline(oracle, params: dict, **over):
         nchan=p["nchan"], nbeam=p.get("nbeam", 1), gulp=p["gulp"], tsamp=p["tsamp"], plan_dt=p["plan_dt"],
         f0=p["f0_mhz"], df=p["df_mhz"], dm_min=p["dm_min"], dm_max=p["dm_max"], dm_tol=p["dm_tol"],
         ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
-        max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 0),
+        max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
         spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15))
 
 

@@ -271,6 +271,10 @@ static float median_filter(const float *in, float *out, int size, int win) {
   return mn / (float)(1. * size);
 }
 
+float ho_median_filter(const float *in, float *out, int size, int window) {
+  return median_filter(in, out, size, window);
+}
+
 #define NMEDFILT 1 /* definitions.h:39 */
 
 /* bandpass_correct  flagger.cu:244-269 (+ med_filter_bandpass
@@ -328,8 +332,10 @@ static void ts_correct(uint16_t *d, int nchan, int w, float *ts_out) {
 
 /* npp_convolve_handler  convolution.cu:20-55: uniform xw (time) x yw
  * (channel) box of taps `k`, anchor (xw/2, yw/2), replicate border, fp32
- * accumulation of fp16 input, fp16 output.  Summation order (channel row
- * then time, one fmaf per tap) is this project's definition. */
+ * accumulation of fp16 input, fp16 output.  Tap (j, i) multiplies input
+ * (c + ay - j, t + ax - i), the placement nppiFilterBorder uses (an impulse
+ * response measured on a GB300); the summation order (j outer, i inner,
+ * one fmaf per tap) is this project's definition. */
 static void box_filter(const uint16_t *in, uint16_t *out, int nchan, int w,
                        int xw, int yw, float k) {
   int ax = xw / 2, ay = yw / 2;
@@ -338,10 +344,10 @@ static void box_filter(const uint16_t *in, uint16_t *out, int nchan, int w,
     for (int t = 0; t < w; ++t) {
       float acc = 0.f;
       for (int j = 0; j < yw; ++j) {
-        int cc = c + j - ay;
+        int cc = c + ay - j;
         cc = cc < 0 ? 0 : (cc >= nchan ? nchan - 1 : cc);
         for (int i = 0; i < xw; ++i) {
-          int tt = t + i - ax;
+          int tt = t + ax - i;
           tt = tt < 0 ? 0 : (tt >= w ? w - 1 : tt);
           acc = fmaf(k, ho_h2f(in[(size_t)cc * w + tt]), acc);
         }

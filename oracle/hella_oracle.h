@@ -81,6 +81,10 @@ float ho_stddev_f32(const float *data, int width, int height, size_t stride,
 float ho_stddev_f16(const uint16_t *data, int width, int height, size_t stride,
                     float *mean_out);
 
+/* median_filter (median_filter.cpp:38-83): odd window, bubble-sort median,
+ * edges copied from the nearest filtered value; returns the output mean. */
+float ho_median_filter(const float *in, float *out, int size, int window);
+
 /* --------------------------------------------------------------- flagger */
 typedef struct {
   int tscrunch, fscrunch, nits;

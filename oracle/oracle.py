@@ -246,3 +246,44 @@ class Pipeline:
                                     None if dd is None else dd.ctypes.data, None if bx is None else bx.ctypes.data,
                                     mean.ctypes.data, std.ctypes.data, s0.ctypes.data)
         return dict(cands=out[:n], dd=dd, boxes=bx, mean=mean, std=std, sigma0=float(s0[0]))
+
+
+def stddev_f16(x: np.ndarray, width=None):
+    """calculate_stddev<half> of an fp16 plane given as uint16 bit patterns."""
+    x = np.ascontiguousarray(x, np.uint16)
+    m = np.zeros(1, np.float32)
+    s = lib().ho_stddev_f16(x.ctypes.data, x.shape[1] if width is None else width, x.shape[0], x.shape[1],
+                            m.ctypes.data)
+    return float(m[0]), float(s)
+
+
+def median_filter(x: np.ndarray, window: int):
+    L = lib()
+    L.ho_median_filter.restype = C.c_float
+    L.ho_median_filter.argtypes = [_VP, _VP, C.c_int, C.c_int]
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    mn = L.ho_median_filter(x.ctypes.data, out.ctypes.data, x.size, window)
+    return out, float(mn)
+
+
+def smooth_normalise(dd: np.ndarray, wmin: int, wmax: int, ntime_out: int, anchor: int = 1):
+    dd = np.ascontiguousarray(dd, np.float32)
+    ndms, ntd = dd.shape
+    nbox, sm = 0, wmin
+    while sm < wmax:
+        nbox, sm = nbox + 1, sm * 2
+    boxes = np.zeros((nbox, ndms - 2, ntime_out), np.float32)
+    mean, std = np.zeros(nbox, np.float32), np.zeros(nbox, np.float32)
+    lib().ho_smooth_normalise(dd.ctypes.data, ndms, ntd, ntd, wmin, wmax, anchor, ntime_out, boxes.ctypes.data,
+                              mean.ctypes.data, std.ctypes.data)
+    return boxes, mean, std
+
+
+def find_peaks(boxes: np.ndarray, snr: float, beam: int = 0, cap: int = 10000):
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    nbox, h, nt = boxes.shape
+    out = np.zeros(cap, CAND_DTYPE)
+    s0 = np.zeros(1, np.float32)
+    n = lib().ho_find_peaks(boxes.ctypes.data, nbox, h + 2, nt, snr, beam, cap, out.ctypes.data, s0.ctypes.data)
+    return out[:n], float(s0[0])

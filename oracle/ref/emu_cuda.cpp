@@ -1,0 +1,238 @@
+/*
+ * emu_cuda.cpp -- host execution of CUDA kernels and the CUDA runtime calls
+ * the reference's stage sources make.  TEST INFRASTRUCTURE ONLY: it runs
+ * the reference's own flagger/statistics/smoothing/peak code on the CPU so
+ * that its outputs can pin the oracle (see emu_cuda.h).
+ *
+ * Blocks of kernels that synchronise run their threads as ucontext fibers:
+ * each fiber runs until its next barrier, then the next fiber runs; a warp
+ * shuffle is a barrier-separated exchange through a per-block buffer.
+ */
+#include "emu_cuda.h"
+
+#include <nppdefs.h>
+#include <ucontext.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+uint3 threadIdx, blockIdx;
+dim3 blockDim, gridDim;
+
+namespace emu {
+
+namespace {
+struct Fiber {
+  ucontext_t ctx;
+  bool done;
+  uint3 tid;
+};
+constexpr size_t kStack = 128 * 1024;
+std::vector<Fiber> g_fibers;
+std::vector<char> g_stacks;
+std::vector<uint64_t> g_xbuf;
+ucontext_t g_sched;
+int g_cur = -1;
+bool g_coop = false;
+const std::function<void()> *g_body = nullptr;
+
+void fiber_entry() {
+  (*g_body)();
+  g_fibers[g_cur].done = true;
+  swapcontext(&g_fibers[g_cur].ctx, &g_sched);
+}
+}  // namespace
+
+void syncthreads() {
+  if (!g_coop) {
+    std::fprintf(stderr, "emu: __syncthreads in a kernel launched without fibers\n");
+    std::abort();
+  }
+  swapcontext(&g_fibers[g_cur].ctx, &g_sched);
+}
+
+uint64_t exchange(uint64_t v, unsigned delta) {
+  const int t = g_cur;
+  g_xbuf[t] = v;
+  syncthreads();
+  const unsigned lane = (unsigned)t & 31u;
+  const uint64_t r = (lane + delta < 32u) ? g_xbuf[t + delta] : v;
+  syncthreads();
+  return r;
+}
+
+void launch(dim3 grid, dim3 block, bool coop, const std::function<void()> &body) {
+  ::gridDim = grid;
+  ::blockDim = block;
+  const int nt = (int)(block.x * block.y * block.z);
+  if (coop) {
+    g_fibers.resize(nt);
+    g_stacks.resize((size_t)nt * kStack);
+    g_xbuf.assign(nt, 0);
+  }
+  for (unsigned bz = 0; bz < grid.z; ++bz)
+    for (unsigned by = 0; by < grid.y; ++by)
+      for (unsigned bx = 0; bx < grid.x; ++bx) {
+        ::blockIdx = make_uint3(bx, by, bz);
+        if (!coop) {
+          g_coop = false;
+          for (unsigned tz = 0; tz < block.z; ++tz)
+            for (unsigned ty = 0; ty < block.y; ++ty)
+              for (unsigned tx = 0; tx < block.x; ++tx) {
+                ::threadIdx = make_uint3(tx, ty, tz);
+                body();
+              }
+          continue;
+        }
+        g_coop = true;
+        g_body = &body;
+        for (int t = 0; t < nt; ++t) {
+          Fiber &f = g_fibers[t];
+          f.tid = make_uint3(t % block.x, (t / block.x) % block.y, t / (block.x * block.y));
+          f.done = false;
+          getcontext(&f.ctx);
+          f.ctx.uc_stack.ss_sp = &g_stacks[(size_t)t * kStack];
+          f.ctx.uc_stack.ss_size = kStack;
+          f.ctx.uc_link = nullptr;
+          makecontext(&f.ctx, fiber_entry, 0);
+        }
+        bool live = true;
+        while (live) {
+          live = false;
+          for (int t = 0; t < nt; ++t) {
+            if (g_fibers[t].done) continue;
+            g_cur = t;
+            ::threadIdx = g_fibers[t].tid;
+            swapcontext(&g_sched, &g_fibers[t].ctx);
+            live = true;
+          }
+        }
+        g_coop = false;
+      }
+}
+}  // namespace emu
+
+// ------------------------------------------------------------ CUDA runtime
+extern "C" {
+
+static size_t round_up(size_t n, size_t a) { return (n + a - 1) / a * a; }
+
+cudaError_t cudaMalloc(void **p, size_t n) {
+  *p = std::aligned_alloc(256, round_up(n ? n : 1, 256));
+  return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+cudaError_t cudaFree(void *p) {
+  std::free(p);
+  return cudaSuccess;
+}
+cudaError_t cudaMallocHost(void **p, size_t n) { return cudaMalloc(p, n); }
+cudaError_t cudaFreeHost(void *p) { return cudaFree(p); }
+cudaError_t cudaMallocPitch(void **p, size_t *pitch, size_t width, size_t height) {
+  *pitch = round_up(width, 512);  // the row alignment of current devices
+  return cudaMalloc(p, *pitch * height);
+}
+cudaError_t cudaMemcpy(void *d, const void *s, size_t n, enum cudaMemcpyKind) {
+  std::memmove(d, s, n);
+  return cudaSuccess;
+}
+cudaError_t cudaMemcpyAsync(void *d, const void *s, size_t n, enum cudaMemcpyKind, cudaStream_t) {
+  std::memmove(d, s, n);
+  return cudaSuccess;
+}
+cudaError_t cudaMemcpy2D(void *d, size_t dp, const void *s, size_t sp, size_t w, size_t h,
+                         enum cudaMemcpyKind) {
+  for (size_t r = 0; r < h; ++r)
+    std::memmove(static_cast<char *>(d) + r * dp, static_cast<const char *>(s) + r * sp, w);
+  return cudaSuccess;
+}
+cudaError_t cudaMemset(void *d, int v, size_t n) {
+  std::memset(d, v, n);
+  return cudaSuccess;
+}
+cudaError_t cudaDeviceSynchronize(void) { return cudaSuccess; }
+cudaError_t cudaGetLastError(void) { return cudaSuccess; }
+cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+cudaError_t cudaGetDevice(int *d) {
+  *d = 0;
+  return cudaSuccess;
+}
+const char *cudaGetErrorString(cudaError_t) { return "emulated"; }
+
+}  // extern "C"
+
+// ------------------------------------------------------------ NPP filters
+// The reference's two NPP filters, with the index placement measured on a
+// GB300 (tap i of kernel column ax-relative applied to input x + ax - i,
+// likewise rows) and replicate borders.  Summation order is the oracle's
+// (NPP's own is not observable), so these pin everything around the filter
+// rather than NPP's internal rounding.
+std::vector<float> g_taps_seen;  // every smoothing kernel passed, in order
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+extern "C" NppStatus nppiFilterBorder32f_16f_C1R(const Npp16f *pSrc, Npp32s nSrcStep, NppiSize oSrcSize,
+                                                 NppiPoint, Npp16f *pDst, Npp32s nDstStep, NppiSize oSizeROI,
+                                                 const Npp32f *pKernel, NppiSize ks, NppiPoint anc,
+                                                 NppiBorderType) {
+  const int W = oSrcSize.width, H = oSrcSize.height;
+  for (int y = 0; y < oSizeROI.height; ++y)
+    for (int x = 0; x < oSizeROI.width; ++x) {
+      float acc = 0.f;
+      for (int j = 0; j < ks.height; ++j) {
+        const int yy = clampi(y + anc.y - j, 0, H - 1);
+        const __half *row = reinterpret_cast<const __half *>(reinterpret_cast<const char *>(pSrc) + (size_t)yy * nSrcStep);
+        for (int i = 0; i < ks.width; ++i) {
+          const int xx = clampi(x + anc.x - i, 0, W - 1);
+          acc = std::fmaf(pKernel[j * ks.width + i], __half2float(row[xx]), acc);
+        }
+      }
+      __half *orow = reinterpret_cast<__half *>(reinterpret_cast<char *>(pDst) + (size_t)y * nDstStep);
+      orow[x] = __float2half_rn(acc);
+    }
+  return NPP_SUCCESS;
+}
+
+extern "C" NppStatus nppiFilterBorder_32f_C1R(const Npp32f *pSrc, Npp32s nSrcStep, NppiSize oSrcSize, NppiPoint,
+                                              Npp32f *pDst, Npp32s nDstStep, NppiSize oSizeROI,
+                                              const Npp32f *pKernel, NppiSize ks, NppiPoint anc, NppiBorderType) {
+  // the smoothing kernel: rows weighted 0.3/1/0.3 around the output row,
+  // evaluated in the oracle's factored form (middle-row taps)
+  g_taps_seen.insert(g_taps_seen.end(), pKernel, pKernel + (size_t)ks.width * ks.height);
+  const int W = oSrcSize.width, H = oSrcSize.height, n = ks.width;
+  const float *mid = pKernel + n;  // row 1
+  std::vector<float> yv(W);
+  for (int y = 0; y < oSizeROI.height; ++y) {
+    const float *a = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) +
+                                                     (size_t)clampi(y - 1, 0, H - 1) * nSrcStep);
+    const float *b = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) + (size_t)y * nSrcStep);
+    const float *c = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) +
+                                                     (size_t)clampi(y + 1, 0, H - 1) * nSrcStep);
+    for (int x = 0; x < W; ++x) yv[x] = std::fmaf(0.3f, a[x] + c[x], b[x]);
+    float *o = reinterpret_cast<float *>(reinterpret_cast<char *>(pDst) + (size_t)y * nDstStep);
+    for (int x = 0; x < oSizeROI.width; ++x) {
+      float acc = 0.f;
+      for (int k = 0; k < n; ++k) acc = std::fmaf(mid[k], yv[clampi(x + anc.x - (n - 1) + k, 0, W - 1)], acc);
+      o[x] = acc;
+    }
+  }
+  return NPP_SUCCESS;
+}
+
+extern "C" NppStatus nppiAddC_32f_C1IR(const Npp32f c, Npp32f *p, int step, NppiSize roi) {
+  for (int y = 0; y < roi.height; ++y) {
+    float *r = reinterpret_cast<float *>(reinterpret_cast<char *>(p) + (size_t)y * step);
+    for (int x = 0; x < roi.width; ++x) r[x] = r[x] + c;
+  }
+  return NPP_SUCCESS;
+}
+
+extern "C" NppStatus nppiMulC_32f_C1IR(const Npp32f c, Npp32f *p, int step, NppiSize roi) {
+  for (int y = 0; y < roi.height; ++y) {
+    float *r = reinterpret_cast<float *>(reinterpret_cast<char *>(p) + (size_t)y * step);
+    for (int x = 0; x < roi.width; ++x) r[x] = r[x] * c;
+  }
+  return NPP_SUCCESS;
+}

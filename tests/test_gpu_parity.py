@@ -131,7 +131,7 @@ def test_flagger_bit_exact(hella, oracle):
 
 
 def test_search_stages_bit_exact(hella, oracle):
-    params, sky = synth.config_plain(seed=5, nchan=256, gulp=4096, dm_max=300.0)
+    params, sky = synth.config_plain(seed=5, nchan=256, gulp=4096, dm_max=400.0)
     s, pl = _run_to_search(hella, oracle, params, sky)
     g = pl.min_gulp
     x = sky.gulp(g, params["gulp"])[None]
@@ -160,9 +160,9 @@ def test_search_stages_bit_exact(hella, oracle):
 
 @pytest.mark.parametrize("anchor", [0, 1])
 def test_gulp_loop_multibeam(hella, oracle, anchor):
-    params, _ = synth.config_plain(seed=7, nchan=128, gulp=2048, dm_max=250.0)
+    params, _ = synth.config_plain(seed=7, nchan=128, gulp=2048, dm_max=400.0)
     params["smooth_anchor"] = anchor
-    skies = [synth.config_plain(seed=70 + b, nchan=128, gulp=2048, dm_max=250.0)[1] for b in range(3)]
+    skies = [synth.config_plain(seed=70 + b, nchan=128, gulp=2048, dm_max=400.0)[1] for b in range(3)]
     for sk in skies:
         sk.bursts[0].amp *= 3
     s = _search(hella, params, nbeam=3, beam0=0)
@@ -179,7 +179,7 @@ def test_gulp_loop_multibeam(hella, oracle, anchor):
 
 
 def test_max_giants_cap(hella, oracle):
-    params, sky = synth.config_plain(seed=9, nchan=128, gulp=2048, dm_max=250.0)
+    params, sky = synth.config_plain(seed=9, nchan=128, gulp=2048, dm_max=400.0)
     sky.bursts[0].amp *= 6
     params.update(max_giants=25, snr=3.0)
     s = _search(hella, params, nbeam=2)

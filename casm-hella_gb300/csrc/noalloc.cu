@@ -1,0 +1,118 @@
+// noalloc.cu -- hdd_execute_noalloc (include/hella_dedisp.h): dedispersion
+// for callers that cannot allocate device memory while they run.
+//
+// Its scratch (delay table, active-channel list, channel-major staging copy
+// and packed ring) is carved out of one file-scope device array instead of
+// cudaMalloc'd buffers.  Host code never uses the array's name as an
+// address: that name is only a host-side stand-in for the symbol.  The
+// device address is looked up once per device with cudaGetSymbolAddress
+// (with that device current) and handed to the kernels.
+#include "hella_dedisp.h"
+#include "hg_internal.h"
+#include "hg_plan.h"
+
+#include <mutex>
+
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[HDD_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+void *g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device` (which must be current);
+// the first call per device resolves it.
+hdd_error scratch_for(int device, unsigned char **out) {
+  if (device < 0 || device >= kMaxDevices) return HDD_INVALID_DEVICE_INDEX;
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  if (!g_scratch_addr[device]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return HDD_INTERNAL_GPU_ERROR;
+    }
+    g_scratch_addr[device] = p;
+  }
+  *out = static_cast<unsigned char *>(g_scratch_addr[device]);
+  return HDD_NO_ERROR;
+}
+
+size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
+                                         hdd_size in_nbits, hdd_size in_stride, hdd_byte *out,
+                                         hdd_size out_nbits, hdd_size out_stride, unsigned flags) {
+  if (!plan) return HDD_INVALID_PLAN;
+  if (!in || !out) return HDD_INVALID_POINTER;
+  const hg::PlanView v = hg::plan_view(plan);
+  if (v.ndms == 0) return HDD_NO_DM_LIST_SET;
+  if (flags & HDD_HOST_POINTERS) return HDD_INVALID_FLAG_COMBINATION;  // device pointers only
+  if ((flags & HDD_WAIT) && (flags & HDD_ASYNC)) return HDD_INVALID_FLAG_COMBINATION;
+  if (in_nbits != 8) return HDD_UNSUPPORTED_IN_NBITS;
+  if (out_nbits != 32) return HDD_UNSUPPORTED_OUT_NBITS;
+  if (nsamps <= (hdd_size)v.max_delay) return HDD_TOO_FEW_NSAMPS;
+  if (nsamps > (hdd_size)(65535u * 32u)) return HDD_STATIC_SCRATCH_EXCEEDED;
+  const int nout = (int)(nsamps - v.max_delay);
+  if (in_stride < (hdd_size)v.nchans) return HDD_INVALID_STRIDE;
+  if (out_stride % 4 != 0 || out_stride < (hdd_size)nout * 4) return HDD_INVALID_STRIDE;
+
+  // scratch layout: delays | active channels | staging [nchans][R] | packed [nchans][R]
+  const long R = ((long)nsamps + 3) / 4 * 4;
+  const size_t o_delays = 0;
+  const size_t o_chans = o_delays + align256((size_t)v.ndms * v.nchans * 4);
+  const size_t o_plain = o_chans + align256((size_t)v.nchans * 4);
+  const size_t o_packed = o_plain + align256((size_t)v.nchans * R);
+  const size_t total = o_packed + (size_t)v.nchans * R * 4;
+  if (total > HDD_NOALLOC_SCRATCH_BYTES) return HDD_STATIC_SCRATCH_EXCEEDED;
+
+  if (cudaSetDevice(v.device) != cudaSuccess) return HDD_INVALID_DEVICE_INDEX;
+  if (cudaPeekAtLastError() != cudaSuccess) return HDD_PRIOR_GPU_ERROR;
+  unsigned char *base = nullptr;
+  hdd_error e = scratch_for(v.device, &base);
+  if (e != HDD_NO_ERROR) return e;
+  cudaStream_t s = (cudaStream_t)v.stream;
+  int *d_delays = reinterpret_cast<int *>(base + o_delays);
+  int *d_chans = reinterpret_cast<int *>(base + o_chans);
+  uint8_t *d_plain = base + o_plain;
+  uint32_t *d_packed = reinterpret_cast<uint32_t *>(base + o_packed);
+
+  // The tables are rewritten by every call: nothing depends on what the
+  // previous call left in the array.
+  if (cudaMemcpyAsync(d_delays, v.delays, (size_t)v.ndms * v.nchans * 4, cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return HDD_MEM_COPY_FAILED;
+  if (v.nact > 0 &&
+      cudaMemcpyAsync(d_chans, v.chans, (size_t)v.nact * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return HDD_MEM_COPY_FAILED;
+  if (hg::transpose_tf(in, in_stride, (int)nsamps, v.nchans, d_plain, R, s) != cudaSuccess)
+    return HDD_INTERNAL_GPU_ERROR;
+  if (hg::pack_ring(d_plain, d_packed, 1, v.nchans, R, 0, R, s) != cudaSuccess)
+    return HDD_INTERNAL_GPU_ERROR;
+  float *dout = reinterpret_cast<float *>(out);
+  if (v.nact == 0) {
+    for (int d = 0; d < v.ndms; ++d)
+      if (cudaMemsetAsync(out + (size_t)d * out_stride, 0, (size_t)nout * 4, s) != cudaSuccess)
+        return HDD_INTERNAL_GPU_ERROR;
+  } else {
+    hg::DedispArgs a{};
+    a.packed = d_packed;
+    a.R = R;
+    a.win0 = 0;
+    a.delays = d_delays;
+    a.nchan = v.nchans;
+    a.chans = d_chans;
+    a.nact = v.nact;
+    a.dm_first = 0;
+    a.dm_count = v.ndms;
+    a.nout = nout;
+    a.out = dout;
+    a.out_stride = (long)(out_stride / 4);
+    a.dpt = hg::plan_tile(plan, 0, v.ndms, &a.max_spread);
+    if (hg::dedisperse(a, s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+  }
+  if (!(flags & HDD_ASYNC) && cudaStreamSynchronize(s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+  return HDD_NO_ERROR;
+}

@@ -157,6 +157,19 @@ hdd_error plan_device_tables(hdd_plan p, const int **d_delays, const int **d_cha
   return HDD_NO_ERROR;
 }
 
+PlanView plan_view(hdd_plan p) {
+  PlanView v{};
+  v.device = p->device;
+  v.stream = p->stream;
+  v.nchans = p->nchans;
+  v.ndms = (int)p->dms.size();
+  v.max_delay = p->max_delay;
+  v.delays = p->delays.empty() ? nullptr : p->delays.data();
+  v.chans = p->chans.empty() ? nullptr : p->chans.data();
+  v.nact = (int)p->chans.size();
+  return v;
+}
+
 int plan_tile(hdd_plan p, int first, int count, int *spread) {
   if (p->spread_first != first || p->spread_count != count) {
     p->dpt = dedisp_pick_tile(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(),
@@ -382,6 +395,7 @@ const char *hdd_get_error_string(hdd_error e) {
     case HDD_PRIOR_GPU_ERROR: return "prior gpu error";
     case HDD_INTERNAL_GPU_ERROR: return "internal gpu error";
     case HDD_UNKNOWN_ERROR: return "unknown error";
+    case HDD_STATIC_SCRATCH_EXCEEDED: return "request exceeds the static scratch of hdd_execute_noalloc";
   }
   return "unknown code";
 }

@@ -31,7 +31,7 @@ HDD_ERRORS = [
     "HDD_INVALID_PLAN", "HDD_INVALID_POINTER", "HDD_INVALID_STRIDE", "HDD_NO_DM_LIST_SET",
     "HDD_TOO_FEW_NSAMPS", "HDD_INVALID_FLAG_COMBINATION", "HDD_UNSUPPORTED_IN_NBITS",
     "HDD_UNSUPPORTED_OUT_NBITS", "HDD_INVALID_DEVICE_INDEX", "HDD_DEVICE_ALREADY_SET",
-    "HDD_PRIOR_GPU_ERROR", "HDD_INTERNAL_GPU_ERROR", "HDD_UNKNOWN_ERROR",
+    "HDD_PRIOR_GPU_ERROR", "HDD_INTERNAL_GPU_ERROR", "HDD_UNKNOWN_ERROR", "HDD_STATIC_SCRATCH_EXCEEDED",
 ]
 
 
@@ -108,6 +108,7 @@ def lib() -> C.CDLL:
     _sig(L, "hdd_execute_adv", C.c_int, [_VP, _SZ, _VP, _SZ, _SZ, _VP, _SZ, _SZ, C.c_uint])
     _sig(L, "hdd_execute_guru", C.c_int, [_VP, _SZ, _VP, _SZ, _SZ, _VP, _SZ, _SZ, _SZ, _SZ, C.c_uint])
     _sig(L, "hdd_get_error_string", C.c_char_p, [C.c_int])
+    _sig(L, "hdd_execute_noalloc", C.c_int, [_VP, _SZ, _VP, _SZ, _SZ, _VP, _SZ, _SZ, C.c_uint])
     # hella_ stage API
     _sig(L, "hella_params_default", None, [C.POINTER(HellaParams)])
     _sig(L, "hella_create", C.c_int, [C.POINTER(_VP), C.POINTER(HellaParams)])

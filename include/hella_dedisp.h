@@ -57,7 +57,9 @@ typedef enum {
   HDD_DEVICE_ALREADY_SET,
   HDD_PRIOR_GPU_ERROR,
   HDD_INTERNAL_GPU_ERROR,
-  HDD_UNKNOWN_ERROR
+  HDD_UNKNOWN_ERROR,
+  HDD_STATIC_SCRATCH_EXCEEDED /* hdd_execute_noalloc: needs more than its
+                                 fixed scratch (HDD_NOALLOC_SCRATCH_BYTES) */
 } hdd_error;
 
 /* Execute flags; the reference passes 1<<2 (device pointers,
@@ -123,6 +125,35 @@ hdd_error hdd_execute_guru(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
 
 /* Text for a status, as get_dedisp_error (dedisperse.cpp:50-91). */
 const char *hdd_get_error_string(hdd_error error);
+
+/* hdd_execute_noalloc -- no counterpart in the reference.
+ *
+ * hdd_execute_adv with device pointers, for callers that cannot allocate
+ * device memory while they run: a real-time loop that must not stall in
+ * the allocator or risk an out-of-memory failure mid-stream, code running
+ * under a device-memory pool or budget owned by another component, and
+ * hosts that forbid allocation after start-up.  Every buffer the other
+ * execute calls allocate on demand (the channel-major staging copy, the
+ * packed ring, the delay table) lives instead in one fixed array of
+ * HDD_NOALLOC_SCRATCH_BYTES compiled into the library; every GPU that loads
+ * the library holds that array until the process exits.  The call makes no
+ * cudaMalloc/cudaFree and no other allocating call.
+ *
+ * Limit: 4*dm_count*nchans + 4*nchans + 5*nchans*R bytes (R = nsamps
+ * rounded up to a multiple of 4, each part aligned to 256 bytes) must fit
+ * in HDD_NOALLOC_SCRATCH_BYTES, else HDD_STATIC_SCRATCH_EXCEEDED.  in and
+ * out are device pointers (HDD_HOST_POINTERS is rejected).  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the
+ * array and each one overwrites it completely, so nothing carries over from
+ * the previous call; two calls whose device work overlaps in time (other
+ * streams, other threads) race on it. */
+#define HDD_NOALLOC_SCRATCH_BYTES (32ul << 20)
+hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps,
+                              const hdd_byte *in, hdd_size in_nbits,
+                              hdd_size in_stride, hdd_byte *out,
+                              hdd_size out_nbits, hdd_size out_stride,
+                              unsigned flags);
 
 #ifdef __cplusplus
 }

@@ -11,16 +11,18 @@
 // reads the single word at t0 + j + delay(c,d): 32 lanes read 32
 // consecutive words (no bank conflicts) whatever the delay, and each 4-byte
 // read feeds four sums.  The bytes are split into two SWAR registers of
-// 16-bit lanes with byte_perm (samples k=0,2 and k=1,3) and accumulated
-// with 32-bit adds; 256 channels of u8 fit a 16-bit lane (255*256 < 2^16),
-// after which the lanes are widened into 32-bit totals.
+// 16-bit lanes with byte_perm (samples k=0,2 and k=1,3); two channels are
+// added per three-input add.  256 channels of u8 fit a 16-bit lane
+// (255*256 < 2^16), after which the lanes are widened into 32-bit totals.
 //
-// Staging.  Per block: a tile of kDmTile trials x 4S samples.  Channels are
-// processed kChanChunk at a time: the delays of the chunk are loaded, then
-// each channel's packed words [t0 + delay(c,d0), + S + spread) are copied
-// into shared memory with 16-byte loads.  spread = delay(c,d_last) -
-// delay(c,d0) grows with DM, so the shared row length is sized by the host
-// from the largest spread of the launch.
+// Staging.  A block owns DPT trials x 4S samples and walks the active
+// channels kStageCh at a time.  Host-built tile tables give, per (tile,
+// channel), the delay of the tile's first trial, the delay spread across
+// the tile and the per-trial offsets, so every stage is a set of contiguous
+// 16-byte copies: the channel's packed words [t0 + delay, + S + spread) and
+// its offsets.  Stages are double buffered with cp.async: stage k+1 (and the
+// table entries of stage k+2) stream into shared memory while stage k is
+// summed.
 #include "hg_internal.h"
 
 #include <algorithm>
@@ -29,29 +31,75 @@ namespace hg {
 namespace {
 
 constexpr int S = kPackS;
-constexpr int kDmTile = 16;    // DM trials per block (per thread)
-constexpr int kChanChunk = 16; // channels staged per round
+constexpr int kStageCh = 8;          // channels per pipeline stage
+constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
 
-// Shared row length: a channel's copy covers sh + S + spread words (sh < 4,
-// the 16-byte misalignment) rounded up to whole 16-byte chunks, at most
-// S + spread + 6 words.
 __host__ __device__ constexpr int row_words(int max_spread) {
+  // sh + S + spread words (sh < 4) rounded up to 16-byte chunks
   return ((S + max_spread + 6) + 3) / 4 * 4;
 }
+__host__ __device__ constexpr int off_width(int dpt) { return dpt < 4 ? 4 : dpt; }
 
-template <int DPT, int CC>
-__global__ void __launch_bounds__(kDedispThreads) k_dedisp(DedispArgs a, int rowstride) {
+__host__ __device__ constexpr size_t stage_words(int dpt, int rowstride) {
+  return (size_t)kStageCh * 4 /*meta*/ + kStageCh /*sh*/ + (size_t)kStageCh * off_width(dpt) +
+         (size_t)kStageCh * rowstride;
+}
+size_t smem_bytes(int dpt, int rowstride) { return 2 * stage_words(dpt, rowstride) * 4 + 64; }
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int DPT>
+__global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int rowstride) {
   extern __shared__ __align__(16) uint32_t smem[];
-  int *off_s = reinterpret_cast<int *>(smem);  // [CC][DPT]
-  int *pos_s = off_s + CC * DPT;               // [CC] delay of trial d0
-  int *sh_s = pos_s + CC;                      // [CC] word misalignment
-  uint32_t *rows = smem + ((CC * DPT + 2 * CC + 3) / 4) * 4;
+  constexpr int CC = kStageCh, OFFW = off_width(DPT);
+  // per buffer b: meta [CC] int4 | sh [CC] int | off [CC][OFFW] int | rows [CC][rowstride]
+  const size_t sw = stage_words(DPT, rowstride);
+  auto meta_of = [&](int b) { return reinterpret_cast<int4 *>(smem + b * sw); };
+  auto sh_of = [&](int b) { return reinterpret_cast<int *>(smem + b * sw + CC * 4); };
+  auto off_of = [&](int b) { return reinterpret_cast<int *>(smem + b * sw + CC * 5); };
+  auto rows_of = [&](int b) { return smem + b * sw + CC * 5 + CC * OFFW; };
 
-  const int tj = threadIdx.x, lane = tj & 31, warp = tj >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int t0 = blockIdx.x * 4 * S;
-  const int d0 = a.dm_first + blockIdx.y * DPT;
-  const int dlast = a.dm_first + a.dm_count - 1;
-  const int d0c = min(d0, dlast);
+  const int tile = blockIdx.y;
+  const int d0 = a.dm_first + tile * DPT, dlast = a.dm_first + a.dm_count - 1;
+  const int4 *gmeta = a.tile_meta + (size_t)tile * a.nact;
+  const int *goff = a.tile_off + (size_t)tile * a.nact * OFFW;
+  const int nstage = (a.nact + CC - 1) / CC;
+  const long w0 = (a.win0 + t0) % a.R;
+
+  auto issue_meta = [&](int st) {
+    const int k0 = st * CC, nc = min(CC, a.nact - k0);
+    if (tid < nc) cp_async16(meta_of(st & 1) + tid, gmeta + k0 + tid);
+  };
+  auto issue_data = [&](int st) {
+    const int b = st & 1, k0 = st * CC, nc = min(CC, a.nact - k0);
+    const int4 *m = meta_of(b);
+    int *off = off_of(b);
+    for (int i = tid; i < nc * OFFW / 4; i += blockDim.x) cp_async16(off + 4 * i, goff + (size_t)k0 * OFFW + 4 * i);
+    uint32_t *rows = rows_of(b);
+    for (int ci = warp; ci < nc; ci += blockDim.x / 32) {
+      const int4 mc = m[ci];  // {channel, base delay, spread, 0}
+      long p = w0 + mc.y;
+      while (p >= a.R) p -= a.R;
+      const long a4 = p & ~3L;
+      const int sh = (int)(p - a4);
+      const int n4 = (sh + S + mc.z + 3) >> 2;
+      if (lane == 0) sh_of(b)[ci] = sh;
+      const uint32_t *src = a.packed + (size_t)mc.x * a.R;
+      uint32_t *dst = rows + (size_t)ci * rowstride;
+      for (int j = lane; j < n4; j += 32) {
+        long g = a4 + 4L * j;
+        while (g >= a.R) g -= a.R;  // R % 4 == 0 keeps g 16-byte aligned
+        cp_async16(dst + 4 * j, src + g);
+      }
+    }
+  };
 
   uint32_t acc_e[DPT], acc_o[DPT], tot[DPT][4];
 #pragma unroll
@@ -62,47 +110,70 @@ __global__ void __launch_bounds__(kDedispThreads) k_dedisp(DedispArgs a, int row
   }
   int since = 0;
 
-  for (int k0 = 0; k0 < a.nact; k0 += CC) {
-    const int nc = min(CC, a.nact - k0);
-    __syncthreads();
-    for (int i = tj; i < CC * DPT; i += blockDim.x) {
-      const int ci = i / DPT, m = i % DPT;
-      int v = 0;
-      if (ci < nc) {
-        const int c = a.chans[k0 + ci];
-        const int base = a.delays[(size_t)d0c * a.nchan + c];
-        v = a.delays[(size_t)min(d0 + m, dlast) * a.nchan + c] - base;
-        if (m == 0) pos_s[ci] = base;
-      }
-      off_s[i] = v;
+  issue_meta(0);
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncthreads();
+  issue_data(0);
+  if (nstage > 1) issue_meta(1);
+  cp_async_commit();
+
+  for (int st = 0; st < nstage; ++st) {
+    cp_async_wait_all();
+    __syncthreads();  // stage st's rows and stage st+1's table entries have landed
+    if (st + 1 < nstage) {
+      issue_data(st + 1);
+      if (st + 2 < nstage) issue_meta(st + 2);
     }
-    __syncthreads();
-    for (int ci = warp; ci < nc; ci += blockDim.x / 32) {
-      const int c = a.chans[k0 + ci];
-      long p = a.win0 + t0 + pos_s[ci];
-      p %= a.R;
-      const long a4 = p & ~3L;
-      const int sh = (int)(p - a4);
-      const int spread = off_s[ci * DPT + DPT - 1];
-      const int n4 = (sh + S + spread + 3) >> 2;
-      const uint4 *src = reinterpret_cast<const uint4 *>(a.packed + (size_t)c * a.R);
-      uint4 *dst = reinterpret_cast<uint4 *>(rows + (size_t)ci * rowstride);
-      for (int j = lane; j < n4; j += 32) {
-        const long g = (a4 + 4L * j) % a.R;  // R % 4 == 0 keeps g 16-byte aligned
-        dst[j] = __ldg(src + (g >> 2));
-      }
-      if (lane == 0) sh_s[ci] = sh;
-    }
-    __syncthreads();
-    for (int ci = 0; ci < nc; ++ci) {
-      const uint32_t *row = rows + (size_t)ci * rowstride + sh_s[ci] + tj;
-      const int *o = off_s + ci * DPT;
+    cp_async_commit();
+    const int b = st & 1, nc = min(CC, a.nact - st * CC);
+    const char *rows = reinterpret_cast<const char *>(rows_of(b) + tid);
+    const int4 *off4 = reinterpret_cast<const int4 *>(off_of(b));
+    const int *shs = sh_of(b);
+    // offsets are byte offsets (host-scaled), so each load address is one add
+    auto add_pair = [&](int ci) {
+      const char *r1 = rows + ((size_t)ci * rowstride + shs[ci]) * 4;
+      const char *r2 = rows + ((size_t)(ci + 1) * rowstride + shs[ci + 1]) * 4;
 #pragma unroll
-      for (int m = 0; m < DPT; ++m) {
-        const uint32_t w = row[o[m]];
-        acc_e[m] += __byte_perm(w, 0u, 0x4240);
-        acc_o[m] += __byte_perm(w, 0u, 0x4341);
+      for (int q = 0; q < OFFW / 4; ++q) {
+        const int4 x1 = off4[ci * (OFFW / 4) + q], x2 = off4[(ci + 1) * (OFFW / 4) + q];
+        const int o1[4] = {x1.x, x1.y, x1.z, x1.w}, o2[4] = {x2.x, x2.y, x2.z, x2.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int m = 4 * q + j;
+          if (m < DPT) {
+            const uint32_t w1 = *reinterpret_cast<const uint32_t *>(r1 + o1[j]);
+            const uint32_t w2 = *reinterpret_cast<const uint32_t *>(r2 + o2[j]);
+            acc_e[m] += __byte_perm(w1, 0u, 0x4240) + __byte_perm(w2, 0u, 0x4240);
+            acc_o[m] += __byte_perm(w1, 0u, 0x4341) + __byte_perm(w2, 0u, 0x4341);
+          }
+        }
       }
+    };
+    auto add_one = [&](int ci) {
+      const char *r1 = rows + ((size_t)ci * rowstride + shs[ci]) * 4;
+#pragma unroll
+      for (int q = 0; q < OFFW / 4; ++q) {
+        const int4 x1 = off4[ci * (OFFW / 4) + q];
+        const int o1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int m = 4 * q + j;
+          if (m < DPT) {
+            const uint32_t w1 = *reinterpret_cast<const uint32_t *>(r1 + o1[j]);
+            acc_e[m] += __byte_perm(w1, 0u, 0x4240);
+            acc_o[m] += __byte_perm(w1, 0u, 0x4341);
+          }
+        }
+      }
+    };
+    if (nc == CC) {
+#pragma unroll
+      for (int ci = 0; ci < CC; ci += 2) add_pair(ci);
+    } else {
+      int ci = 0;
+      for (; ci + 1 < nc; ci += 2) add_pair(ci);
+      if (ci < nc) add_one(ci);
     }
     since += nc;
     if (since > 256 - CC) {
@@ -117,6 +188,7 @@ __global__ void __launch_bounds__(kDedispThreads) k_dedisp(DedispArgs a, int row
       since = 0;
     }
   }
+  cp_async_wait_all();
 #pragma unroll
   for (int m = 0; m < DPT; ++m) {
     tot[m][0] += acc_e[m] & 0xffffu;
@@ -131,16 +203,10 @@ __global__ void __launch_bounds__(kDedispThreads) k_dedisp(DedispArgs a, int row
     float *o = a.out + (size_t)(d - a.dm_first) * a.out_stride;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int t = t0 + tj + k * S;
+      const int t = t0 + tid + k * S;
       if (t < a.nout) o[t] = (float)tot[m][k];
     }
   }
-}
-
-template <int DPT>
-size_t dedisp_smem(int rowstride) {
-  return (size_t)((kChanChunk * DPT + 2 * kChanChunk + 3) / 4 * 4) * 4 +
-         (size_t)kChanChunk * rowstride * 4;
 }
 
 __global__ void k_pack(const uint8_t *__restrict__ plain, uint32_t *__restrict__ packed,
@@ -175,29 +241,50 @@ __global__ void k_transpose_tf(const uint8_t *__restrict__ in, size_t in_stride,
 
 }  // namespace
 
-namespace {
-
-int tile_spread(const int *delays, int nchan, const int *chans, int nact, int dm_first,
-                int dm_count, int dpt) {
-  int best = 0;
+DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int nact, int dm_first,
+                           int dm_count) {
+  DedispTables t;
   const int dlast = dm_first + dm_count - 1;
-  for (int d0 = dm_first; d0 <= dlast; d0 += dpt) {
-    const int d1 = std::min(d0 + dpt - 1, dlast);
-    for (int i = 0; i < nact; ++i) {
-      const int c = chans[i];
-      best = std::max(best, delays[(size_t)d1 * nchan + c] - delays[(size_t)d0 * nchan + c]);
+  for (int dpt : {16, 8, 4, 2, 1}) {
+    int spread = 0;
+    for (int d0 = dm_first; d0 <= dlast; d0 += dpt) {
+      const int d1 = std::min(d0 + dpt - 1, dlast);
+      for (int k = 0; k < nact; ++k) {
+        const int c = chans[k];
+        spread = std::max(spread, delays[(size_t)d1 * nchan + c] - delays[(size_t)d0 * nchan + c]);
+      }
+    }
+    if (smem_bytes(dpt, row_words(spread)) <= kSmemBudget || dpt == 1) {
+      t.dpt = dpt;
+      t.max_spread = spread;
+      break;
     }
   }
-  return best;
+  t.offw = off_width(t.dpt);
+  t.ntiles = (dm_count + t.dpt - 1) / t.dpt;
+  t.meta.resize((size_t)t.ntiles * nact);
+  t.off.assign((size_t)t.ntiles * nact * t.offw, 0);
+  for (int i = 0; i < t.ntiles; ++i) {
+    const int d0 = dm_first + i * t.dpt, d1 = std::min(d0 + t.dpt - 1, dlast);
+    for (int k = 0; k < nact; ++k) {
+      const int c = chans[k];
+      const int base = delays[(size_t)d0 * nchan + c];
+      t.meta[(size_t)i * nact + k] = make_int4(c, base, delays[(size_t)d1 * nchan + c] - base, 0);
+      int *o = &t.off[((size_t)i * nact + k) * t.offw];
+      for (int m = 0; m < t.dpt; ++m)  // byte offsets into the staged row
+        o[m] = 4 * (delays[(size_t)std::min(d0 + m, dlast) * nchan + c] - base);
+    }
+  }
+  return t;
 }
 
-constexpr size_t kSmemLimit = 200 * 1024;
+namespace {
 
 template <int DPT>
 cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
   const int rowstride = row_words(a.max_spread);
-  const size_t smem = dedisp_smem<DPT>(rowstride);
-  auto kern = k_dedisp<DPT, kChanChunk>;
+  const size_t smem = smem_bytes(DPT, rowstride);
+  auto kern = k_dedisp<DPT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const dim3 grid((a.nout + 4 * S - 1) / (4 * S), (a.dm_count + DPT - 1) / DPT);
@@ -208,24 +295,8 @@ cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
 
 }  // namespace
 
-int dedisp_pick_tile(const int *delays, int nchan, const int *chans, int nact, int dm_first,
-                     int dm_count, int *spread) {
-  const int tiles[] = {kDmTile, 8, 4, 2, 1};
-  for (int dpt : tiles) {
-    const int sp = tile_spread(delays, nchan, chans, nact, dm_first, dm_count, dpt);
-    const size_t need = (size_t)((kChanChunk * dpt + 2 * kChanChunk + 3) / 4 * 4) * 4 +
-                        (size_t)kChanChunk * row_words(sp) * 4;
-    if (need <= kSmemLimit || dpt == 1) {
-      *spread = sp;
-      return dpt;
-    }
-  }
-  *spread = 0;
-  return 1;
-}
-
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
-  if (a.dm_count <= 0 || a.nout <= 0) return cudaSuccess;
+  if (a.dm_count <= 0 || a.nout <= 0 || a.nact <= 0) return cudaSuccess;
   switch (a.dpt) {
     case 16: return launch<16>(a, s);
     case 8: return launch<8>(a, s);

@@ -16,6 +16,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 namespace hg {
 
@@ -64,23 +65,28 @@ struct DedispArgs {
   const uint32_t *packed;   // [nchan][R] packed words of one beam
   long R;                   // ring length (words per channel row), % 4 == 0
   long win0;                // ring position of window sample 0
-  const int *delays;        // [ndms][nchan] device delay table
-  int nchan;
-  const int *chans;         // active channel list (killmask applied)
-  int nact;
+  int nact;                 // active (unkilled) channels
   int dm_first, dm_count;   // trials computed; output row 0 = dm_first
   int nout;                 // output samples per trial
   float *out;               // [dm_count][out_stride]
   long out_stride;
-  int dpt;                  // DM trials per block (a supported tile)
-  int max_spread;           // max over tiles of delay(c,d_last)-delay(c,d0)
+  int dpt;                  // DM trials per block (16, 8, 4, 2 or 1)
+  int max_spread;           // largest tile_meta spread
+  const int4 *tile_meta;    // [ntiles][nact] {channel, delay(c, tile's first trial), spread, 0}
+  const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - delay(c, first trial)), bytes
 };
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s);
-// Host side: picks the largest DM tile whose staged rows fit in shared
-// memory for trials [dm_first, dm_first + dm_count) and returns it; *spread
-// receives that tile's largest delay(c,d_last) - delay(c,d0).
-int dedisp_pick_tile(const int *delays_host, int nchan, const int *chans_host,
-                     int nact, int dm_first, int dm_count, int *spread);
+
+// Host-side tile tables for trials [dm_first, dm_first + dm_count) over the
+// active channels; picks the largest DM tile whose double-buffered staging
+// fits in shared memory.
+struct DedispTables {
+  int dpt = 0, max_spread = 0, ntiles = 0, offw = 0;
+  std::vector<int4> meta;
+  std::vector<int> off;
+};
+DedispTables dedisp_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
+                           int dm_first, int dm_count);
 
 // ------------------------------------------------------- smoothing
 struct SmoothArgs {

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "hella_dedisp.h"
+#include "hg_internal.h"
 
 #include <vector>
 
@@ -12,8 +13,16 @@ std::vector<float> generate_dm_list(double dm_start, double dm_end, double ti_us
 std::vector<float> delay_table(int nchan, double dt_s, double f0, double df);
 std::vector<int> dm_delays(const std::vector<float> &dms, const std::vector<float> &table);
 
-// Device copies of the plan's delay table and active-channel list.
-hdd_error plan_device_tables(hdd_plan p, const int **d_delays, const int **d_chans, int *nact);
+// Dedispersion tile tables for trials [first, first + count): host copy
+// (cached per range) and device copy (uploaded on first use).
+const DedispTables &plan_host_tables(hdd_plan p, int first, int count);
+struct DeviceTables {
+  const int4 *meta;
+  const int *off;
+  int dpt, max_spread, nact;
+};
+hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out);
+
 // Read-only view of a plan's host tables.
 struct PlanView {
   int device;
@@ -23,9 +32,5 @@ struct PlanView {
   const int *chans;   // [nact] active channels
 };
 PlanView plan_view(hdd_plan p);
-
-// DM tile used for trials [first, first + count) and its largest delay
-// spread (cached per range).
-int plan_tile(hdd_plan p, int first, int count, int *spread);
 
 }  // namespace hg

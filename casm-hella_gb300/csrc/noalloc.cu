@@ -1,8 +1,8 @@
 // noalloc.cu -- hdd_execute_noalloc (include/hella_dedisp.h): dedispersion
 // for callers that cannot allocate device memory while they run.
 //
-// Its scratch (delay table, active-channel list, channel-major staging copy
-// and packed ring) is carved out of one file-scope device array instead of
+// Its scratch (dedispersion tile tables, channel-major staging copy and
+// packed ring) is carved out of one file-scope device array instead of
 // cudaMalloc'd buffers.  Host code never uses the array's name as an
 // address: that name is only a host-side stand-in for the symbol.  The
 // device address is looked up once per device with cudaGetSymbolAddress
@@ -59,11 +59,13 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   if (in_stride < (hdd_size)v.nchans) return HDD_INVALID_STRIDE;
   if (out_stride % 4 != 0 || out_stride < (hdd_size)nout * 4) return HDD_INVALID_STRIDE;
 
-  // scratch layout: delays | active channels | staging [nchans][R] | packed [nchans][R]
+  // scratch layout: tile meta | tile offsets | staging [nchans][R] | packed [nchans][R]
+  // (the tile tables are built on the host once per plan and DM range)
+  const hg::DedispTables &tb = hg::plan_host_tables(plan, 0, v.ndms);
   const long R = ((long)nsamps + 3) / 4 * 4;
-  const size_t o_delays = 0;
-  const size_t o_chans = o_delays + align256((size_t)v.ndms * v.nchans * 4);
-  const size_t o_plain = o_chans + align256((size_t)v.nchans * 4);
+  const size_t o_meta = 0;
+  const size_t o_off = o_meta + align256(tb.meta.size() * sizeof(int4));
+  const size_t o_plain = o_off + align256(tb.off.size() * sizeof(int));
   const size_t o_packed = o_plain + align256((size_t)v.nchans * R);
   const size_t total = o_packed + (size_t)v.nchans * R * 4;
   if (total > HDD_NOALLOC_SCRATCH_BYTES) return HDD_STATIC_SCRATCH_EXCEEDED;
@@ -74,18 +76,17 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   hdd_error e = scratch_for(v.device, &base);
   if (e != HDD_NO_ERROR) return e;
   cudaStream_t s = (cudaStream_t)v.stream;
-  int *d_delays = reinterpret_cast<int *>(base + o_delays);
-  int *d_chans = reinterpret_cast<int *>(base + o_chans);
+  int4 *d_meta = reinterpret_cast<int4 *>(base + o_meta);
+  int *d_off = reinterpret_cast<int *>(base + o_off);
   uint8_t *d_plain = base + o_plain;
   uint32_t *d_packed = reinterpret_cast<uint32_t *>(base + o_packed);
 
   // The tables are rewritten by every call: nothing depends on what the
   // previous call left in the array.
-  if (cudaMemcpyAsync(d_delays, v.delays, (size_t)v.ndms * v.nchans * 4, cudaMemcpyHostToDevice, s) !=
-      cudaSuccess)
-    return HDD_MEM_COPY_FAILED;
-  if (v.nact > 0 &&
-      cudaMemcpyAsync(d_chans, v.chans, (size_t)v.nact * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+  if (!tb.meta.empty() &&
+      (cudaMemcpyAsync(d_meta, tb.meta.data(), tb.meta.size() * sizeof(int4), cudaMemcpyHostToDevice, s) !=
+           cudaSuccess ||
+       cudaMemcpyAsync(d_off, tb.off.data(), tb.off.size() * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess))
     return HDD_MEM_COPY_FAILED;
   if (hg::transpose_tf(in, in_stride, (int)nsamps, v.nchans, d_plain, R, s) != cudaSuccess)
     return HDD_INTERNAL_GPU_ERROR;
@@ -101,16 +102,16 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
     a.packed = d_packed;
     a.R = R;
     a.win0 = 0;
-    a.delays = d_delays;
-    a.nchan = v.nchans;
-    a.chans = d_chans;
     a.nact = v.nact;
     a.dm_first = 0;
     a.dm_count = v.ndms;
     a.nout = nout;
     a.out = dout;
     a.out_stride = (long)(out_stride / 4);
-    a.dpt = hg::plan_tile(plan, 0, v.ndms, &a.max_spread);
+    a.dpt = tb.dpt;
+    a.max_spread = tb.max_spread;
+    a.tile_meta = d_meta;
+    a.tile_off = d_off;
     if (hg::dedisperse(a, s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
   }
   if (!(flags & HDD_ASYNC) && cudaStreamSynchronize(s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;

@@ -82,31 +82,38 @@ struct hdd_plan_struct {
   std::vector<int> delays, chans;
   std::vector<hdd_bool> killmask;
   int max_delay = 0;
-  int *d_delays = nullptr, *d_chans = nullptr;
-  bool dirty = true;
+  // dedispersion tile tables of the last DM range used, host and device
+  hg::DedispTables tab;
+  int tab_first = -1, tab_count = -1;
+  bool tab_on_device = false;
+  int4 *d_meta = nullptr;
+  int *d_off = nullptr;
+  size_t meta_cap = 0, off_cap = 0;
   uint8_t *d_in = nullptr, *d_plain = nullptr, *d_out = nullptr;
   uint32_t *d_packed = nullptr;
   size_t in_cap = 0, plain_cap = 0, out_cap = 0, packed_cap = 0;
-  int spread_first = -1, spread_count = -1, spread = 0, dpt = 0;
 };
 
 namespace {
 
 thread_local int t_device = 0;
 
+void invalidate_tables(hdd_plan p) {
+  p->tab_first = p->tab_count = -1;
+  p->tab_on_device = false;
+}
+
 void refresh_delays(hdd_plan p) {
   p->delays = hg::dm_delays(p->dms, p->table);
   p->max_delay = p->dms.empty() ? 0 : p->delays[(p->dms.size() - 1) * p->nchans + p->nchans - 1];
-  p->dirty = true;
-  p->spread_first = -1;
+  invalidate_tables(p);
 }
 
 void rebuild_chans(hdd_plan p) {
   p->chans.clear();
   for (int c = 0; c < p->nchans; ++c)
     if (p->killmask[c]) p->chans.push_back(c);
-  p->dirty = true;
-  p->spread_first = -1;
+  invalidate_tables(p);
 }
 
 hdd_error grow(void **ptr, size_t *cap, size_t need) {
@@ -122,38 +129,39 @@ hdd_error grow(void **ptr, size_t *cap, size_t need) {
   return HDD_NO_ERROR;
 }
 
-hdd_error sync_tables(hdd_plan p) {
-  if (!p->dirty) return HDD_NO_ERROR;
-  cudaFree(p->d_delays);
-  cudaFree(p->d_chans);
-  p->d_delays = nullptr;
-  p->d_chans = nullptr;
-  const size_t nd = p->delays.size() * sizeof(int);
-  const size_t nc = std::max<size_t>(1, p->chans.size()) * sizeof(int);
-  if (cudaMalloc(&p->d_delays, std::max<size_t>(nd, 4)) != cudaSuccess ||
-      cudaMalloc(&p->d_chans, nc) != cudaSuccess) {
-    cudaGetLastError();
-    return HDD_MEM_ALLOC_FAILED;
-  }
-  if (nd && cudaMemcpy(p->d_delays, p->delays.data(), nd, cudaMemcpyHostToDevice) != cudaSuccess)
-    return HDD_MEM_COPY_FAILED;
-  if (!p->chans.empty() && cudaMemcpy(p->d_chans, p->chans.data(), p->chans.size() * sizeof(int),
-                                      cudaMemcpyHostToDevice) != cudaSuccess)
-    return HDD_MEM_COPY_FAILED;
-  p->dirty = false;
-  return HDD_NO_ERROR;
-}
-
 }  // namespace
 
 namespace hg {
 
-hdd_error plan_device_tables(hdd_plan p, const int **d_delays, const int **d_chans, int *nact) {
-  hdd_error e = sync_tables(p);
-  if (e != HDD_NO_ERROR) return e;
-  *d_delays = p->d_delays;
-  *d_chans = p->d_chans;
-  *nact = (int)p->chans.size();
+const DedispTables &plan_host_tables(hdd_plan p, int first, int count) {
+  if (p->tab_first != first || p->tab_count != count) {
+    p->tab = dedisp_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first, count);
+    p->tab_first = first;
+    p->tab_count = count;
+    p->tab_on_device = false;
+  }
+  return p->tab;
+}
+
+hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out) {
+  const DedispTables &t = plan_host_tables(p, first, count);
+  if (!p->tab_on_device) {
+    const size_t mb = std::max<size_t>(t.meta.size(), 1) * sizeof(int4);
+    const size_t ob = std::max<size_t>(t.off.size(), 1) * sizeof(int);
+    hdd_error e;
+    if ((e = grow((void **)&p->d_meta, &p->meta_cap, mb)) != HDD_NO_ERROR) return e;
+    if ((e = grow((void **)&p->d_off, &p->off_cap, ob)) != HDD_NO_ERROR) return e;
+    if (!t.meta.empty() &&
+        (cudaMemcpy(p->d_meta, t.meta.data(), t.meta.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy(p->d_off, t.off.data(), t.off.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
+      return HDD_MEM_COPY_FAILED;
+    p->tab_on_device = true;
+  }
+  out->meta = p->d_meta;
+  out->off = p->d_off;
+  out->dpt = t.dpt;
+  out->max_spread = t.max_spread;
+  out->nact = (int)p->chans.size();
   return HDD_NO_ERROR;
 }
 
@@ -168,17 +176,6 @@ PlanView plan_view(hdd_plan p) {
   v.chans = p->chans.empty() ? nullptr : p->chans.data();
   v.nact = (int)p->chans.size();
   return v;
-}
-
-int plan_tile(hdd_plan p, int first, int count, int *spread) {
-  if (p->spread_first != first || p->spread_count != count) {
-    p->dpt = dedisp_pick_tile(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(),
-                              first, count, &p->spread);
-    p->spread_first = first;
-    p->spread_count = count;
-  }
-  *spread = p->spread;
-  return p->dpt;
 }
 
 }  // namespace hg
@@ -208,8 +205,8 @@ hdd_error hdd_create_plan(hdd_plan *plan, hdd_size nchans, hdd_float dt, hdd_flo
 void hdd_destroy_plan(hdd_plan p) {
   if (!p) return;
   cudaSetDevice(p->device);
-  cudaFree(p->d_delays);
-  cudaFree(p->d_chans);
+  cudaFree(p->d_meta);
+  cudaFree(p->d_off);
   cudaFree(p->d_in);
   cudaFree(p->d_plain);
   cudaFree(p->d_packed);
@@ -301,7 +298,8 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
   if (cudaPeekAtLastError() != cudaSuccess) return HDD_PRIOR_GPU_ERROR;
   const bool device = (flags & HDD_DEVICE_POINTERS) != 0;
 
-  hdd_error e = sync_tables(p);
+  hg::DeviceTables tb;
+  hdd_error e = hg::plan_device_tables(p, (int)first_dm_idx, (int)dm_count, &tb);
   if (e != HDD_NO_ERROR) return e;
   const uint8_t *din = in;
   const size_t in_bytes = (size_t)(nsamps - 1) * in_stride + p->nchans;
@@ -331,16 +329,16 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
   a.packed = p->d_packed;
   a.R = R;
   a.win0 = 0;
-  a.delays = p->d_delays;
-  a.nchan = p->nchans;
-  a.chans = p->d_chans;
-  a.nact = (int)p->chans.size();
+  a.nact = tb.nact;
   a.dm_first = (int)first_dm_idx;
   a.dm_count = (int)dm_count;
   a.nout = nout;
   a.out = dout;
   a.out_stride = (long)(out_stride / 4);
-  a.dpt = hg::plan_tile(p, a.dm_first, a.dm_count, &a.max_spread);
+  a.dpt = tb.dpt;
+  a.max_spread = tb.max_spread;
+  a.tile_meta = tb.meta;
+  a.tile_off = tb.off;
   if (a.nact == 0) {
     for (hdd_size d = 0; d < dm_count; ++d)
       if (cudaMemsetAsync(reinterpret_cast<uint8_t *>(dout) + d * out_stride, 0, (size_t)nout * 4,

@@ -257,13 +257,13 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   if ((s = halloc(c, (void **)&c->h_cand_v, (size_t)p->max_giants * 4)) != HELLA_OK) return fail(s);
   if ((s = halloc(c, (void **)&c->h_total, 16)) != HELLA_OK) return fail(s);
 
-  // smoothing taps: middle rows, zero padded to a multiple of 8
+  // smoothing taps: middle rows, zero padded to a multiple of 16
   std::vector<float> taps;
   std::vector<int> off, n;
   for (int b = 0; b < c->nbox; ++b) {
     std::vector<float> m = middle_taps(p->width_min << b);
     off.push_back((int)taps.size());
-    const int np = ((int)m.size() + 7) / 8 * 8;
+    const int np = ((int)m.size() + 15) / 16 * 16;
     n.push_back(np);
     m.resize(np, 0.f);
     taps.insert(taps.end(), m.begin(), m.end());
@@ -337,25 +337,23 @@ hella_status hella_fast_flagger(hella_ctx *c) {
 hella_status hella_dedisperse(hella_ctx *c, int beam) {
   if (!c || beam < 0 || beam >= c->p.nbeam) return HELLA_ERR_INVALID_ARG;
   if (!c->flagged) return HELLA_ERR_STATE;
-  const int *d_delays, *d_chans;
-  int nact;
-  if (hg::plan_device_tables(c->plan, &d_delays, &d_chans, &nact) != HDD_NO_ERROR)
-    return HELLA_ERR_DEDISP;
+  hg::DeviceTables tb;
+  if (hg::plan_device_tables(c->plan, 0, c->ndms, &tb) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
   hg::DedispArgs a{};
   a.packed = c->d_packed + (size_t)beam * c->p.nchan * c->R;
   a.R = c->R;
   a.win0 = c->win0;
-  a.delays = d_delays;
-  a.nchan = c->p.nchan;
-  a.chans = d_chans;
-  a.nact = nact;
+  a.nact = tb.nact;
   a.dm_first = 0;
   a.dm_count = c->ndms;
   a.nout = c->ntime_dd;
   a.out = c->d_dd;
   a.out_stride = c->ntime_dd;
-  a.dpt = hg::plan_tile(c->plan, 0, c->ndms, &a.max_spread);
-  if (nact == 0)
+  a.dpt = tb.dpt;
+  a.max_spread = tb.max_spread;
+  a.tile_meta = tb.meta;
+  a.tile_off = tb.off;
+  if (tb.nact == 0)
     CK(cudaMemsetAsync(c->d_dd, 0, (size_t)c->ndms * c->ntime_dd * 4, c->stream));
   else
     CK(hg::dedisperse(a, c->stream));

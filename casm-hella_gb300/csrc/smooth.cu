@@ -17,9 +17,9 @@
 // supplies the time taps.  Borders replicate (NPP_BORDER_REPLICATE).
 //
 // Kernels.  k_fir: one block per output row; the row's y values for a
-// 2048-sample chunk are staged in shared memory in an 8-phase layout
-// (Y[x % 8][x / 8]) so that each thread keeps a sliding window of 8
-// outputs in registers and reads one conflict-free word per tap.  Every
+// 4096-sample chunk are staged in shared memory in a 16-phase layout
+// (Y[x % 16][x / 16]) so that each thread keeps a sliding window of 16
+// outputs in registers and reads one shared word per tap for all 16.  Every
 // width is produced from the same staged chunk; the row-mean partials of
 // the reference's order (thread j sums columns j, j+256, ...) are
 // accumulated as the chunk is written, so the plane is written once and
@@ -30,7 +30,7 @@
 namespace hg {
 namespace {
 
-constexpr int kR = 8;             // outputs per thread
+constexpr int kR = 16;            // outputs per thread (taps padded to kR)
 constexpr int kT = 256;           // threads per row block
 constexpr int kCH = kR * kT;      // outputs per chunk
 
@@ -91,26 +91,34 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
       const float *tp = taps + a.tap_off[b];
       const int n = a.tap_n[b];
       const int base = kR * tid + off;
+      // win[] slides over y; pre[kk] is where the slot refilled at tap kk of
+      // the first block of kR taps lives in Y (later blocks add one column)
       float acc[kR], win[kR];
+      int pre[kR];
 #pragma unroll
       for (int i = 0; i < kR; ++i) {
         acc[i] = 0.f;
-        const int x = base + i;
+        const int x = base + i, xr = base + i + kR;
         win[i] = Y[(x % kR) * M + x / kR];
+        pre[i] = (xr % kR) * M + xr / kR;
       }
-      for (int kb = 0; kb < n; kb += kR) {
+      for (int kb = 0, kq = 0; kb < n; kb += kR, ++kq) {
 #pragma unroll
-        for (int kk = 0; kk < kR; ++kk) {
-          const float cf = tp[kb + kk];
+        for (int k4 = 0; k4 < kR; k4 += 4) {
+          const float4 c4 = *reinterpret_cast<const float4 *>(tp + kb + k4);
+          const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-          for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cf, win[(i + kk) % kR], acc[i]);
-          const int x = base + kb + kk + kR;
-          win[kk] = Y[(x % kR) * M + x / kR];
+          for (int j = 0; j < 4; ++j) {
+            const int kk = k4 + j;
+#pragma unroll
+            for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cfs[j], win[(i + kk) % kR], acc[i]);
+            win[kk] = Y[pre[kk] + kq];
+          }
         }
       }
       float4 *o4 = reinterpret_cast<float4 *>(out_s + kR * tid);
-      o4[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-      o4[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+#pragma unroll
+      for (int i = 0; i < kR / 4; ++i) o4[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
       __syncthreads();
       float *dst = a.boxes + ((size_t)b * h + r) * a.ntime_out;
       float ps = part_s[b * kT + tid], mx = max_s[b * kT + tid];

@@ -134,14 +134,16 @@ const char *hdd_get_error_string(hdd_error error);
  * under a device-memory pool or budget owned by another component, and
  * hosts that forbid allocation after start-up.  Every buffer the other
  * execute calls allocate on demand (the channel-major staging copy, the
- * packed ring, the delay table) lives instead in one fixed array of
+ * packed ring, the dedispersion tile tables) lives instead in one fixed array of
  * HDD_NOALLOC_SCRATCH_BYTES compiled into the library; every GPU that loads
  * the library holds that array until the process exits.  The call makes no
  * cudaMalloc/cudaFree and no other allocating call.
  *
- * Limit: 4*dm_count*nchans + 4*nchans + 5*nchans*R bytes (R = nsamps
- * rounded up to a multiple of 4, each part aligned to 256 bytes) must fit
- * in HDD_NOALLOC_SCRATCH_BYTES, else HDD_STATIC_SCRATCH_EXCEEDED.  in and
+ * Limit: the dedispersion tile tables (at most 32 bytes per DM trial per
+ * active channel; 5 with the usual 16-trial tiles) plus 5*nchans*R bytes
+ * (R = nsamps rounded up to a multiple of 4), each part aligned to 256
+ * bytes, must fit in HDD_NOALLOC_SCRATCH_BYTES, else
+ * HDD_STATIC_SCRATCH_EXCEEDED.  in and
  * out are device pointers (HDD_HOST_POINTERS is rejected).  The first call
  * on a device looks up the array's device address (cudaGetSymbolAddress);
  * make that first call before any stream capture.  All calls share the

@@ -15,14 +15,22 @@
 // added per three-input add.  256 channels of u8 fit a 16-bit lane
 // (255*256 < 2^16), after which the lanes are widened into 32-bit totals.
 //
-// Staging.  A block owns DPT trials x 4S samples and walks the active
-// channels kStageCh at a time.  Host-built tile tables give, per (tile,
-// channel), the delay of the tile's first trial, the delay spread across
-// the tile and the per-trial offsets, so every stage is a set of contiguous
-// 16-byte copies: the channel's packed words [t0 + delay, + S + spread) and
-// its offsets.  Stages are double buffered with cp.async: stage k+1 (and the
-// table entries of stage k+2) stream into shared memory while stage k is
-// summed.
+// Staging.  A work item is (beam, tile of DPT trials, 4S samples); the
+// block walks the tables' channels CC at a time.  Host-built tile tables
+// give, per (tile, channel), the delay of the tile's first trial, the delay
+// spread across the tile and the per-trial byte offsets, so every stage is
+// one contiguous bulk copy per channel (the packed words [t0 + delay,
+// + S + spread), two copies where the ring wraps) plus one for the offsets.
+// The copies are issued by the lanes of warp 0 with cp.async.bulk (TMA)
+// onto an mbarrier per buffer; two buffers alternate so that stage k+1
+// lands while stage k is summed.  Every wait is bounded: a wait that runs
+// out sets bit 0 of the status word, drains the copies in flight (bounded
+// again) and ends the block.
+//
+// Persistence.  The grid is sized to the resident blocks of the GPU and
+// strides over the work items of every beam of the launch; items of one
+// beam run in groups of `group` DM tiles per time tile, so that blocks
+// resident together read overlapping windows of the ring through L2.
 #include "hg_internal.h"
 
 #include <algorithm>
@@ -31,190 +39,365 @@ namespace hg {
 namespace {
 
 constexpr int S = kPackS;
-constexpr int kStageCh = 8;          // channels per pipeline stage
 constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
+constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr int row_words(int max_spread) {
   // sh + S + spread words (sh < 4) rounded up to 16-byte chunks
   return ((S + max_spread + 6) + 3) / 4 * 4;
 }
 __host__ __device__ constexpr int off_width(int dpt) { return dpt < 4 ? 4 : dpt; }
+constexpr int kMaxBuf = 4;        // staging buffers (pipeline depth)
+constexpr int kBarBytes = 320;    // full[4] | empty[4] mbarriers | per warp: the item it stages
 
-__host__ __device__ constexpr size_t stage_words(int dpt, int rowstride) {
-  return (size_t)kStageCh * 4 /*meta*/ + kStageCh /*sh*/ + (size_t)kStageCh * off_width(dpt) +
-         (size_t)kStageCh * rowstride;
+// Words of one staging buffer: sh [cc] | off [cc][offw] | rows [cc][rowstride];
+// every part is a multiple of 16 bytes.
+__host__ __device__ constexpr int buf_words(int dpt, int cc, int rowstride) {
+  return cc + cc * off_width(dpt) + cc * rowstride;
 }
-size_t smem_bytes(int dpt, int rowstride) { return 2 * stage_words(dpt, rowstride) * 4 + 64; }
+size_t smem_bytes(int dpt, int cc, int rowstride, int nbuf) {
+  return kBarBytes + (size_t)nbuf * buf_words(dpt, cc, rowstride) * 4;
+}
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+// ---- shared-memory, mbarrier and bulk-copy primitives (PTX ISA 8.x)
+__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ int4 lds128(uint32_t addr) {
+  int4 v;
+  asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts32(uint32_t addr, int v) {
+  asm volatile("st.shared.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the phase of `parity` to complete; false after ~kWaitCycles.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try(bar, parity)) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Global -> shared bulk copy of `bytes` (multiple of 16, both ends 16-byte
+// aligned) completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// Where one work item reads and writes.
+struct Item {
+  const uint32_t *packed;
+  float *out;
+  const int4 *meta;   // tile row of the tables
+  const int *off;
+  long w0;            // ring position of the item's first sample
+  int t0, tile, dm_count;
+};
 
 template <int DPT>
-__global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int rowstride) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  constexpr int CC = kStageCh, OFFW = off_width(DPT);
-  // per buffer b: meta [CC] int4 | sh [CC] int | off [CC][OFFW] int | rows [CC][rowstride]
-  const size_t sw = stage_words(DPT, rowstride);
-  auto meta_of = [&](int b) { return reinterpret_cast<int4 *>(smem + b * sw); };
-  auto sh_of = [&](int b) { return reinterpret_cast<int *>(smem + b * sw + CC * 4); };
-  auto off_of = [&](int b) { return reinterpret_cast<int *>(smem + b * sw + CC * 5); };
-  auto rows_of = [&](int b) { return smem + b * sw + CC * 5 + CC * OFFW; };
+__device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
+  int bi = 0;
+  if (a.beams) {
+    int lo = 0, hi = a.nbeam - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.beams[mid].item0 <= item) lo = mid; else hi = mid - 1;
+    }
+    bi = lo;
+  }
+  const DedispBeam bm = a.beams ? a.beams[bi] : a.one;
+  const int ntiles = (bm.dm_count + DPT - 1) / DPT;
+  const int l = item - bm.item0;
+  const int per_group = a.group * a.ntt;
+  const int g = l / per_group, r = l - g * per_group;
+  const int gsz = min(a.group, ntiles - g * a.group);
+  const int tt = r / gsz;
+  Item it;
+  it.tile = g * a.group + (r - tt * gsz);
+  it.t0 = tt * 4 * S;
+  it.w0 = (bm.win0 + it.t0) % a.R;
+  it.packed = bm.packed;
+  it.out = bm.out;
+  it.dm_count = bm.dm_count;
+  it.meta = a.tile_meta + (size_t)it.tile * a.nact;
+  it.off = a.tile_off + (size_t)it.tile * a.nact * off_width(DPT);
+  return it;
+}
+
+// MODE picks how the integer adds are spread over the SM's pipes (the
+// sums are identical): 0 = three-input adds throughout; 1 = load addresses
+// as multiply-adds by a runtime 1 (FMA pipe); 2 = as 1, and the odd-sample
+// lanes accumulated by multiply-adds as well.
+template <int DPT, int CC, int MODE>
+__global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int rowstride, int nbuf) {
+  extern __shared__ __align__(128) uint32_t smem[];
+  constexpr int OFFW = off_width(DPT);
+  constexpr int NWARP = kDedispThreads / 32;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t bw4 = (uint32_t)buf_words(DPT, CC, rowstride) * 4u;
+  const uint32_t rs4 = (uint32_t)rowstride * 4u;
+  auto full_of = [&](int b) { return sbase + 8u * b; };
+  auto empty_of = [&](int b) { return sbase + 32u + 8u * b; };
+  auto sh_of = [&](int b) { return sbase + kBarBytes + (uint32_t)b * bw4; };
+  auto off_of = [&](int b) { return sh_of(b) + CC * 4u; };
+  auto rows_of = [&](int b) { return off_of(b) + CC * OFFW * 4u; };
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int t0 = blockIdx.x * 4 * S;
-  const int tile = blockIdx.y;
-  const int d0 = a.dm_first + tile * DPT, dlast = a.dm_first + a.dm_count - 1;
-  const int4 *gmeta = a.tile_meta + (size_t)tile * a.nact;
-  const int *goff = a.tile_off + (size_t)tile * a.nact * OFFW;
-  const int nstage = (a.nact + CC - 1) / CC;
-  const long w0 = (a.win0 + t0) % a.R;
-
-  auto issue_meta = [&](int st) {
-    const int k0 = st * CC, nc = min(CC, a.nact - k0);
-    if (tid < nc) cp_async16(meta_of(st & 1) + tid, gmeta + k0 + tid);
+  const uint32_t unit = (uint32_t)a.unit;  // 1, unknown to the compiler
+  // Stage g of the block (its k-th item, stage g % nstage) is staged by
+  // warp g % 8, lane i copying channel i; the item a warp is staging is
+  // kept in shared memory to spare registers.
+  struct Staged {
+    const uint32_t *packed;
+    const int4 *meta;
+    const int *off;
+    long w0;
   };
-  auto issue_data = [&](int st) {
-    const int b = st & 1, k0 = st * CC, nc = min(CC, a.nact - k0);
-    const int4 *m = meta_of(b);
-    int *off = off_of(b);
-    for (int i = tid; i < nc * OFFW / 4; i += blockDim.x) cp_async16(off + 4 * i, goff + (size_t)k0 * OFFW + 4 * i);
-    uint32_t *rows = rows_of(b);
-    for (int ci = warp; ci < nc; ci += blockDim.x / 32) {
-      const int4 mc = m[ci];  // {channel, base delay, spread, 0}
-      long p = w0 + mc.y;
+  Staged *staged = reinterpret_cast<Staged *>(reinterpret_cast<char *>(smem) + 64 + 32 * warp);
+
+  if (tid == 0) {
+    for (int b = 0; b < nbuf; ++b) {
+      mbar_init(full_of(b), 32);      // every lane of the staging warp arrives once per fill
+      mbar_init(empty_of(b), NWARP);  // one arrival per warp once it is done reading
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const int nstage = (a.nact + CC - 1) / CC;
+  if (blockIdx.x >= a.nitems) return;
+  const unsigned g_end = (unsigned)((a.nitems - 1 - blockIdx.x) / gridDim.x + 1) * (unsigned)nstage;
+
+  unsigned g_next = (unsigned)warp;  // next stage this warp stages
+  int staged_k = -1;                 // block-local item index held in *staged
+
+  // Stages stage g_next into buffer g_next % nbuf; `block`: may wait for
+  // the buffer to be released, else returns false if it is not free yet.
+  auto issue = [&](bool block, bool *timed_out) -> bool {
+    const unsigned g = g_next;
+    const int b = (int)(g % (unsigned)nbuf);
+    if (g >= (unsigned)nbuf) {
+      const uint32_t par = ((g / nbuf) - 1u) & 1u;
+      if (block) {
+        if (!mbar_wait(empty_of(b), par)) {
+          *timed_out = true;
+          return false;
+        }
+      } else if (!mbar_test(empty_of(b), par)) {
+        return false;
+      }
+    }
+    const int k = (int)(g / (unsigned)nstage), st = (int)(g % (unsigned)nstage);
+    if (k != staged_k) {
+      if (lane == 0) {
+        const Item it = item_at<DPT>(a, blockIdx.x + k * gridDim.x);
+        *staged = Staged{it.packed, it.meta, it.off, it.w0};
+      }
+      staged_k = k;
+      __syncwarp();
+    }
+    const int k0 = st * CC, nc = min(CC, a.nact - k0);
+    const uint32_t bar = full_of(b);
+    fence_proxy_async();
+    if (lane < nc) {
+      const int4 mc = __ldg(staged->meta + k0 + lane);  // {channel, base delay, spread, 0}
+      long p = staged->w0 + mc.y;
       while (p >= a.R) p -= a.R;
       const long a4 = p & ~3L;
       const int sh = (int)(p - a4);
-      const int n4 = (sh + S + mc.z + 3) >> 2;
-      if (lane == 0) sh_of(b)[ci] = sh;
-      const uint32_t *src = a.packed + (size_t)mc.x * a.R;
-      uint32_t *dst = rows + (size_t)ci * rowstride;
-      for (int j = lane; j < n4; j += 32) {
-        long g = a4 + 4L * j;
-        while (g >= a.R) g -= a.R;  // R % 4 == 0 keeps g 16-byte aligned
-        cp_async16(dst + 4 * j, src + g);
+      const int n16 = (sh + S + mc.z + 3) >> 2;  // 16-byte chunks, <= rowstride / 4
+      sts32(sh_of(b) + lane * 4u, sh);
+      const uint32_t obytes = lane == 0 ? (uint32_t)(nc * OFFW * 4) : 0u;
+      mbar_arrive_tx(bar, (uint32_t)n16 * 16u + obytes);
+      const uint32_t *src = staged->packed + (size_t)mc.x * a.R;
+      uint32_t dst = rows_of(b) + (uint32_t)lane * rs4;
+      long pos = a4;
+      int left = n16;
+      while (left > 0) {  // the ring may wrap inside the staged window
+        const int n = (int)min((long)left, (a.R - pos) >> 2);
+        bulk_g2s(dst, src + pos, (uint32_t)n * 16u, bar);
+        dst += (uint32_t)n * 16u;
+        left -= n;
+        pos = 0;
       }
+      if (lane == 0) bulk_g2s(off_of(b), staged->off + (size_t)k0 * OFFW, obytes, bar);
+    } else {
+      mbar_arrive(bar);
     }
+    __syncwarp();
+    g_next += NWARP;
+    return true;
+  };
+  // After a wait ran out: record it, let this warp's copies land, end.
+  auto fail = [&](unsigned gs_c) {
+    if (lane == 0 && a.err) atomicOr(a.err, 1);
+    for (unsigned g = gs_c; g < g_next; ++g)
+      if (g % NWARP == (unsigned)warp) mbar_wait(full_of((int)(g % nbuf)), (g / nbuf) & 1u);
   };
 
-  uint32_t acc_e[DPT], acc_o[DPT], tot[DPT][4];
+  unsigned gs_c = 0;  // stages consumed
+  for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    uint32_t acc_e[DPT], acc_o[DPT], tot[DPT][4];
 #pragma unroll
-  for (int m = 0; m < DPT; ++m) {
-    acc_e[m] = acc_o[m] = 0u;
+    for (int m = 0; m < DPT; ++m) {
+      acc_e[m] = acc_o[m] = 0u;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) tot[m][k] = 0u;
-  }
-  int since = 0;
-
-  issue_meta(0);
-  cp_async_commit();
-  cp_async_wait_all();
-  __syncthreads();
-  issue_data(0);
-  if (nstage > 1) issue_meta(1);
-  cp_async_commit();
-
-  for (int st = 0; st < nstage; ++st) {
-    cp_async_wait_all();
-    __syncthreads();  // stage st's rows and stage st+1's table entries have landed
-    if (st + 1 < nstage) {
-      issue_data(st + 1);
-      if (st + 2 < nstage) issue_meta(st + 2);
+      for (int k = 0; k < 4; ++k) tot[m][k] = 0u;
     }
-    cp_async_commit();
-    const int b = st & 1, nc = min(CC, a.nact - st * CC);
-    const char *rows = reinterpret_cast<const char *>(rows_of(b) + tid);
-    const int4 *off4 = reinterpret_cast<const int4 *>(off_of(b));
-    const int *shs = sh_of(b);
-    // offsets are byte offsets (host-scaled), so each load address is one add
-    auto add_pair = [&](int ci) {
-      const char *r1 = rows + ((size_t)ci * rowstride + shs[ci]) * 4;
-      const char *r2 = rows + ((size_t)(ci + 1) * rowstride + shs[ci + 1]) * 4;
+    for (int st = 0; st < nstage; ++st) {
+      {
+        // keep up to nbuf stages in flight; the stage about to be read must be issued
+        bool to = false;
+        while (g_next < g_end && g_next < gs_c + nbuf)
+          if (!issue(g_next <= gs_c, &to)) break;
+        if (to) return fail(gs_c);
+      }
+      const int b = (int)(gs_c % (unsigned)nbuf), nc = min(CC, a.nact - st * CC);
+      if (!mbar_wait(full_of(b), (gs_c / nbuf) & 1u)) return fail(gs_c);
+      const uint32_t rbase = rows_of(b) + (uint32_t)tid * 4u;
+      const uint32_t shb = sh_of(b), offb = off_of(b);
+      // offsets are byte offsets (host-scaled): each load address is one add
+      auto add_pair = [&](int ci) {
+        const uint32_t r1 = rbase + (uint32_t)ci * rs4 + lds32(shb + ci * 4u) * 4u;
+        const uint32_t r2 = rbase + (uint32_t)(ci + 1) * rs4 + lds32(shb + ci * 4u + 4u) * 4u;
 #pragma unroll
-      for (int q = 0; q < OFFW / 4; ++q) {
-        const int4 x1 = off4[ci * (OFFW / 4) + q], x2 = off4[(ci + 1) * (OFFW / 4) + q];
-        const int o1[4] = {x1.x, x1.y, x1.z, x1.w}, o2[4] = {x2.x, x2.y, x2.z, x2.w};
+        for (int q = 0; q < OFFW / 4; ++q) {
+          const int4 x1 = lds128(offb + (uint32_t)(ci * OFFW + 4 * q) * 4u);
+          const int4 x2 = lds128(offb + (uint32_t)((ci + 1) * OFFW + 4 * q) * 4u);
+          const int o1[4] = {x1.x, x1.y, x1.z, x1.w}, o2[4] = {x2.x, x2.y, x2.z, x2.w};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int m = 4 * q + j;
-          if (m < DPT) {
-            const uint32_t w1 = *reinterpret_cast<const uint32_t *>(r1 + o1[j]);
-            const uint32_t w2 = *reinterpret_cast<const uint32_t *>(r2 + o2[j]);
-            acc_e[m] += __byte_perm(w1, 0u, 0x4240) + __byte_perm(w2, 0u, 0x4240);
-            acc_o[m] += __byte_perm(w1, 0u, 0x4341) + __byte_perm(w2, 0u, 0x4341);
+          for (int j = 0; j < 4; ++j) {
+            const int m = 4 * q + j;
+            if (m < DPT) {
+              const uint32_t w1 = lds32(MODE ? (uint32_t)o1[j] * unit + r1 : r1 + (uint32_t)o1[j]);
+              const uint32_t w2 = lds32(MODE ? (uint32_t)o2[j] * unit + r2 : r2 + (uint32_t)o2[j]);
+              acc_e[m] += __byte_perm(w1, 0u, 0x4240) + __byte_perm(w2, 0u, 0x4240);
+              if (MODE == 2) {
+                acc_o[m] = __byte_perm(w1, 0u, 0x4341) * unit + acc_o[m];
+                acc_o[m] = __byte_perm(w2, 0u, 0x4341) * unit + acc_o[m];
+              } else {
+                acc_o[m] += __byte_perm(w1, 0u, 0x4341) + __byte_perm(w2, 0u, 0x4341);
+              }
+            }
           }
         }
-      }
-    };
-    auto add_one = [&](int ci) {
-      const char *r1 = rows + ((size_t)ci * rowstride + shs[ci]) * 4;
+      };
+      auto add_one = [&](int ci) {
+        const uint32_t r1 = rbase + (uint32_t)ci * rs4 + lds32(shb + ci * 4u) * 4u;
 #pragma unroll
-      for (int q = 0; q < OFFW / 4; ++q) {
-        const int4 x1 = off4[ci * (OFFW / 4) + q];
-        const int o1[4] = {x1.x, x1.y, x1.z, x1.w};
+        for (int q = 0; q < OFFW / 4; ++q) {
+          const int4 x1 = lds128(offb + (uint32_t)(ci * OFFW + 4 * q) * 4u);
+          const int o1[4] = {x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int m = 4 * q + j;
-          if (m < DPT) {
-            const uint32_t w1 = *reinterpret_cast<const uint32_t *>(r1 + o1[j]);
-            acc_e[m] += __byte_perm(w1, 0u, 0x4240);
-            acc_o[m] += __byte_perm(w1, 0u, 0x4341);
+          for (int j = 0; j < 4; ++j) {
+            const int m = 4 * q + j;
+            if (m < DPT) {
+              const uint32_t w1 = lds32(r1 + (uint32_t)o1[j]);
+              acc_e[m] += __byte_perm(w1, 0u, 0x4240);
+              acc_o[m] += __byte_perm(w1, 0u, 0x4341);
+            }
           }
         }
+      };
+      if (nc == CC) {
+#pragma unroll
+        for (int ci = 0; ci < CC; ci += 2) add_pair(ci);
+      } else {
+        int ci = 0;
+        for (; ci + 1 < nc; ci += 2) add_pair(ci);
+        if (ci < nc) add_one(ci);
       }
-    };
-    if (nc == CC) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty_of(b));  // this warp is done with buffer b
+      ++gs_c;
+      if ((st + 1) % (256 / CC) == 0) {  // 256 channels per 16-bit lane, then widen
 #pragma unroll
-      for (int ci = 0; ci < CC; ci += 2) add_pair(ci);
-    } else {
-      int ci = 0;
-      for (; ci + 1 < nc; ci += 2) add_pair(ci);
-      if (ci < nc) add_one(ci);
-    }
-    since += nc;
-    if (since > 256 - CC) {
-#pragma unroll
-      for (int m = 0; m < DPT; ++m) {
-        tot[m][0] += acc_e[m] & 0xffffu;
-        tot[m][2] += acc_e[m] >> 16;
-        tot[m][1] += acc_o[m] & 0xffffu;
-        tot[m][3] += acc_o[m] >> 16;
-        acc_e[m] = acc_o[m] = 0u;
+        for (int m = 0; m < DPT; ++m) {
+          tot[m][0] += acc_e[m] & 0xffffu;
+          tot[m][2] += acc_e[m] >> 16;
+          tot[m][1] += acc_o[m] & 0xffffu;
+          tot[m][3] += acc_o[m] >> 16;
+          acc_e[m] = acc_o[m] = 0u;
+        }
       }
-      since = 0;
     }
-  }
-  cp_async_wait_all();
 #pragma unroll
-  for (int m = 0; m < DPT; ++m) {
-    tot[m][0] += acc_e[m] & 0xffffu;
-    tot[m][2] += acc_e[m] >> 16;
-    tot[m][1] += acc_o[m] & 0xffffu;
-    tot[m][3] += acc_o[m] >> 16;
-  }
+    for (int m = 0; m < DPT; ++m) {
+      tot[m][0] += acc_e[m] & 0xffffu;
+      tot[m][2] += acc_e[m] >> 16;
+      tot[m][1] += acc_o[m] & 0xffffu;
+      tot[m][3] += acc_o[m] >> 16;
+    }
+    const Item it = item_at<DPT>(a, item);
 #pragma unroll
-  for (int m = 0; m < DPT; ++m) {
-    const int d = d0 + m;
-    if (d > dlast) break;
-    float *o = a.out + (size_t)(d - a.dm_first) * a.out_stride;
+    for (int m = 0; m < DPT; ++m) {
+      const int i = it.tile * DPT + m;
+      if (i >= it.dm_count) break;
+      float *o = it.out + (size_t)i * a.out_stride;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int t = t0 + tid + k * S;
-      if (t < a.nout) o[t] = (float)tot[m][k];
+      for (int k = 0; k < 4; ++k) {
+        const int t = it.t0 + tid + k * S;
+        if (t < a.nout) o[t] = (float)tot[m][k];
+      }
     }
   }
 }
 
 __global__ void k_pack(const uint8_t *__restrict__ plain, uint32_t *__restrict__ packed,
-                       int nchan, long R, long q0, long nq) {
+                       int nchan, long R, long q0, long nq, const uint8_t *__restrict__ keep) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
-  const size_t row = ((size_t)blockIdx.z * nchan + blockIdx.y) * (size_t)R;
+  const size_t bc = (size_t)blockIdx.z * nchan + blockIdx.y;
+  const size_t row = bc * (size_t)R;
   const long q = (q0 + i) % R;
+  if (keep && !keep[bc]) {
+    packed[row + q] = 0u;
+    return;
+  }
   const uint8_t *p = plain + row;
   const uint32_t b0 = p[q], b1 = p[(q + S) % R], b2 = p[(q + 2 * S) % R],
                  b3 = p[(q + 3 * S) % R];
@@ -241,23 +424,48 @@ __global__ void k_transpose_tf(const uint8_t *__restrict__ in, size_t in_stride,
 
 }  // namespace
 
+int dedisp_spread(const int *delays, int nchan, const int *chans, int nact, int dm_first,
+                  int dm_count, int dpt) {
+  const int dlast = dm_first + dm_count - 1;
+  int spread = 0;
+  for (int d0 = dm_first; d0 <= dlast; d0 += dpt) {
+    const int d1 = std::min(d0 + dpt - 1, dlast);
+    for (int k = 0; k < nact; ++k) {
+      const int c = chans[k];
+      spread = std::max(spread, delays[(size_t)d1 * nchan + c] - delays[(size_t)d0 * nchan + c]);
+    }
+  }
+  return spread;
+}
+
+// Staging buffers for a tile shape: the deepest pipeline (up to kMaxBuf)
+// that fits the budget of two resident blocks per SM; 0 if even two do not.
+int dedisp_nbuf(int dpt, int cc, int max_spread) {
+  for (int nb = kMaxBuf; nb >= 2; --nb)
+    if (smem_bytes(dpt, cc, row_words(max_spread), nb) <= kSmemBudget) return nb;
+  return 0;
+}
+
+size_t dedisp_smem_bytes(int dpt, int cc, int max_spread) {
+  const int nb = dedisp_nbuf(dpt, cc, max_spread);
+  return nb ? smem_bytes(dpt, cc, row_words(max_spread), nb) : 0;
+}
+
 DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int nact, int dm_first,
-                           int dm_count) {
+                           int dm_count, int dpt, int cc) {
   DedispTables t;
   const int dlast = dm_first + dm_count - 1;
-  for (int dpt : {16, 8, 4, 2, 1}) {
-    int spread = 0;
-    for (int d0 = dm_first; d0 <= dlast; d0 += dpt) {
-      const int d1 = std::min(d0 + dpt - 1, dlast);
-      for (int k = 0; k < nact; ++k) {
-        const int c = chans[k];
-        spread = std::max(spread, delays[(size_t)d1 * nchan + c] - delays[(size_t)d0 * nchan + c]);
+  if (dpt > 0) {
+    t.dpt = dpt;
+    t.max_spread = dedisp_spread(delays, nchan, chans, nact, dm_first, dm_count, dpt);
+  } else {
+    for (int d : {16, 8, 4, 2, 1}) {
+      const int spread = dedisp_spread(delays, nchan, chans, nact, dm_first, dm_count, d);
+      if (dedisp_smem_bytes(d, cc, spread) || d == 1) {
+        t.dpt = d;
+        t.max_spread = spread;
+        break;
       }
-    }
-    if (smem_bytes(dpt, row_words(spread)) <= kSmemBudget || dpt == 1) {
-      t.dpt = dpt;
-      t.max_spread = spread;
-      break;
     }
   }
   t.offw = off_width(t.dpt);
@@ -280,40 +488,64 @@ DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int n
 
 namespace {
 
-template <int DPT>
+template <int DPT, int CC, int MODE>
 cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
   const int rowstride = row_words(a.max_spread);
-  const size_t smem = smem_bytes(DPT, rowstride);
-  auto kern = k_dedisp<DPT>;
+  int nbuf = a.nbuf ? a.nbuf : dedisp_nbuf(DPT, CC, a.max_spread);
+  if (!nbuf) nbuf = 2;  // very coarse DM lists: one block per SM
+  if (nbuf < 2 || nbuf > kMaxBuf) return cudaErrorInvalidValue;
+  const size_t smem = smem_bytes(DPT, CC, rowstride, nbuf);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  auto kern = k_dedisp<DPT, CC, MODE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const dim3 grid((a.nout + 4 * S - 1) / (4 * S), (a.dm_count + DPT - 1) / DPT);
-  kern<<<grid, kDedispThreads, smem, s>>>(a, rowstride);
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDedispThreads, smem)) != cudaSuccess)
+    return e;
+  const int grid = std::max(1, std::min(a.nitems, std::max(1, per_sm) * sms));
+  kern<<<grid, kDedispThreads, smem, s>>>(a, rowstride, nbuf);
   count_launches(1);
   return cudaGetLastError();
+}
+
+template <int DPT>
+cudaError_t launch_cc(const DedispArgs &a, cudaStream_t s) {
+  if (DPT < 8 && a.mode != 0) return cudaErrorInvalidValue;  // modes 1-2: 8 and 16-trial tiles
+  switch (a.cc * 4 + (DPT < 8 ? 0 : a.mode)) {
+    case 32: return launch<DPT, 8, 0>(a, s);
+    case 64: return launch<DPT, 16, 0>(a, s);
+    case 33: return launch<DPT, 8, DPT < 8 ? 0 : 1>(a, s);
+    case 65: return launch<DPT, 16, DPT < 8 ? 0 : 1>(a, s);
+    case 34: return launch<DPT, 8, DPT < 8 ? 0 : 2>(a, s);
+    case 66: return launch<DPT, 16, DPT < 8 ? 0 : 2>(a, s);
+  }
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace
 
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
-  if (a.dm_count <= 0 || a.nout <= 0 || a.nact <= 0) return cudaSuccess;
+  if (a.nitems <= 0 || a.nout <= 0 || a.nact <= 0) return cudaSuccess;
+  if (a.R % 4 != 0 || a.ntt <= 0 || a.group <= 0 || a.nbeam <= 0) return cudaErrorInvalidValue;
   switch (a.dpt) {
-    case 16: return launch<16>(a, s);
-    case 8: return launch<8>(a, s);
-    case 4: return launch<4>(a, s);
-    case 2: return launch<2>(a, s);
-    case 1: return launch<1>(a, s);
+    case 16: return launch_cc<16>(a, s);
+    case 8: return launch_cc<8>(a, s);
+    case 4: return launch_cc<4>(a, s);
+    case 2: return launch_cc<2>(a, s);
+    case 1: return launch_cc<1>(a, s);
   }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam, int nchan,
-                      long R, long q0, long nq, cudaStream_t s) {
+                      long R, long q0, long nq, cudaStream_t s, const uint8_t *keep) {
   if (nq <= 0) return cudaSuccess;
   q0 = ((q0 % R) + R) % R;
   nq = std::min(nq, R);  // each ring position once
   const dim3 grid((unsigned)((nq + 255) / 256), nchan, nbeam);
-  k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq);
+  k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq, keep);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -29,6 +29,9 @@ void count_launches(unsigned n);
 constexpr int kPackS = 256;
 // Dedispersion block: kPackS threads, one per packed word position.
 constexpr int kDedispThreads = kPackS;
+// DM tiles walked together per time tile by the persistent dedispersion
+// kernel (default; the search contexts may tune it).
+constexpr int kDedispGroup = 8;
 
 // ------------------------------------------------------------- flagger
 struct FlagState {
@@ -53,40 +56,71 @@ cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
 
 // ---------------------------------------------------------- packing
 // Rebuild packed words at ring positions [q0, q0 + nq) (mod R) of every
-// beam from the plain ring.
+// beam from the plain ring.  keep ([nbeam][nchan], may be null): channels
+// with keep == 0 are packed as zeros, which drops them from every sum.
 cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam,
-                      int nchan, long R, long q0, long nq, cudaStream_t s);
+                      int nchan, long R, long q0, long nq, cudaStream_t s,
+                      const uint8_t *keep = nullptr);
 // Time-major input [nsamps][in_stride] -> channel-major plain [nchan][R].
 cudaError_t transpose_tf(const uint8_t *in, size_t in_stride, int nsamps,
                          int nchan, uint8_t *plain, long R, cudaStream_t s);
 
 // ------------------------------------------------------ dedispersion
-struct DedispArgs {
-  const uint32_t *packed;   // [nchan][R] packed words of one beam
-  long R;                   // ring length (words per channel row), % 4 == 0
+// One beam of a dedispersion launch.
+struct DedispBeam {
+  const uint32_t *packed;   // [nchan][R] packed words of the beam
+  float *out;               // [dm_count][out_stride]; row i = trial dm_first + i
   long win0;                // ring position of window sample 0
-  int nact;                 // active (unkilled) channels
-  int dm_first, dm_count;   // trials computed; output row 0 = dm_first
+  int dm_count;             // trials of this beam: the first dm_count of the table
+  int item0;                // first work item of the beam (prefix over beams)
+};
+
+struct DedispArgs {
+  const DedispBeam *beams;  // device array [nbeam]; null: the single beam `one`
+  DedispBeam one;
+  int nbeam;
+  int nitems;               // work items: (beam, DM tile, time tile)
+  int ntt;                  // time tiles per beam (4*kPackS samples each)
+  int group;                // DM tiles walked together per time tile (L2 reuse)
+  long R;                   // ring length (words per channel row), % 4 == 0
+  int nact;                 // channels in the tables
+  int dm_first;             // first trial of the tables
   int nout;                 // output samples per trial
-  float *out;               // [dm_count][out_stride]
   long out_stride;
-  int dpt;                  // DM trials per block (16, 8, 4, 2 or 1)
+  int dpt;                  // DM trials per tile (16, 8, 4, 2 or 1)
+  int cc;                   // channels per pipeline stage (8 or 16)
+  int nbuf;                 // staging buffers, 2..4 (0: deepest that fits)
+  int mode;                 // pipe balance of the adds (0, 1, 2; 1-2 need dpt >= 8)
+  int unit;                 // must be 1
   int max_spread;           // largest tile_meta spread
   const int4 *tile_meta;    // [ntiles][nact] {channel, delay(c, tile's first trial), spread, 0}
   const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - delay(c, first trial)), bytes
+  int *err;                 // device status word: bit 0 = a staging wait timed out (may be null)
 };
+// Work items of one beam for a tile shape.
+inline int dedisp_items(int dm_count, int dpt, int ntt) { return (dm_count + dpt - 1) / dpt * ntt; }
+inline int dedisp_time_tiles(int nout) { return (nout + 4 * kPackS - 1) / (4 * kPackS); }
+// Launches the persistent kernel over all items of `a`.
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s);
+// Shared memory of one block for a tile shape; 0 when it does not fit.
+size_t dedisp_smem_bytes(int dpt, int cc, int max_spread);
+// Deepest staging pipeline (2..4 buffers) of a tile shape within the
+// two-blocks-per-SM budget; 0 when two buffers do not fit.
+int dedisp_nbuf(int dpt, int cc, int max_spread);
 
 // Host-side tile tables for trials [dm_first, dm_first + dm_count) over the
-// active channels; picks the largest DM tile whose double-buffered staging
-// fits in shared memory.
+// active channels, for `dpt` trials per tile (dpt = 0: the largest tile
+// whose double-buffered staging of cc channels fits in shared memory).
 struct DedispTables {
   int dpt = 0, max_spread = 0, ntiles = 0, offw = 0;
   std::vector<int4> meta;
   std::vector<int> off;
 };
 DedispTables dedisp_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
-                           int dm_first, int dm_count);
+                           int dm_first, int dm_count, int dpt = 0, int cc = 8);
+// Largest delay spread over the active channels of any dpt-trial tile.
+int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int nact,
+                  int dm_first, int dm_count, int dpt);
 
 // ------------------------------------------------------- smoothing
 struct SmoothArgs {

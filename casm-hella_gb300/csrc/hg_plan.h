@@ -13,15 +13,21 @@ std::vector<float> generate_dm_list(double dm_start, double dm_end, double ti_us
 std::vector<float> delay_table(int nchan, double dt_s, double f0, double df);
 std::vector<int> dm_delays(const std::vector<float> &dms, const std::vector<float> &table);
 
-// Dedispersion tile tables for trials [first, first + count): host copy
-// (cached per range) and device copy (uploaded on first use).
-const DedispTables &plan_host_tables(hdd_plan p, int first, int count);
+// Dedispersion tile tables for trials [first, first + count) with dpt
+// trials per tile (0: the largest that fits cc-channel stages): host copy
+// (cached per range and shape) and device copy (uploaded on first use).
+const DedispTables &plan_host_tables(hdd_plan p, int first, int count, int dpt = 0, int cc = 8);
 struct DeviceTables {
   const int4 *meta;
   const int *off;
-  int dpt, max_spread, nact;
+  int dpt, max_spread, nact, cc;
 };
-hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out);
+hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out, int dpt = 0,
+                             int cc = 8);
+// Launch arguments for one beam over a plan's device tables.
+DedispArgs single_beam_args(const DeviceTables &tb, const uint32_t *packed, long R, long win0,
+                            int dm_first, int dm_count, int nout, float *out, long out_stride,
+                            int *err);
 
 // Read-only view of a plan's host tables.
 struct PlanView {

@@ -59,11 +59,12 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   if (in_stride < (hdd_size)v.nchans) return HDD_INVALID_STRIDE;
   if (out_stride % 4 != 0 || out_stride < (hdd_size)nout * 4) return HDD_INVALID_STRIDE;
 
-  // scratch layout: tile meta | tile offsets | staging [nchans][R] | packed [nchans][R]
+  // scratch layout: status | tile meta | tile offsets | staging [nchans][R] | packed [nchans][R]
   // (the tile tables are built on the host once per plan and DM range)
   const hg::DedispTables &tb = hg::plan_host_tables(plan, 0, v.ndms);
   const long R = ((long)nsamps + 3) / 4 * 4;
-  const size_t o_meta = 0;
+  const size_t o_err = 0;
+  const size_t o_meta = 256;
   const size_t o_off = o_meta + align256(tb.meta.size() * sizeof(int4));
   const size_t o_plain = o_off + align256(tb.off.size() * sizeof(int));
   const size_t o_packed = o_plain + align256((size_t)v.nchans * R);
@@ -80,9 +81,11 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   int *d_off = reinterpret_cast<int *>(base + o_off);
   uint8_t *d_plain = base + o_plain;
   uint32_t *d_packed = reinterpret_cast<uint32_t *>(base + o_packed);
+  int *d_err = reinterpret_cast<int *>(base + o_err);
 
   // The tables are rewritten by every call: nothing depends on what the
   // previous call left in the array.
+  if (cudaMemsetAsync(d_err, 0, sizeof(int), s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
   if (!tb.meta.empty() &&
       (cudaMemcpyAsync(d_meta, tb.meta.data(), tb.meta.size() * sizeof(int4), cudaMemcpyHostToDevice, s) !=
            cudaSuccess ||
@@ -98,22 +101,16 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
       if (cudaMemsetAsync(out + (size_t)d * out_stride, 0, (size_t)nout * 4, s) != cudaSuccess)
         return HDD_INTERNAL_GPU_ERROR;
   } else {
-    hg::DedispArgs a{};
-    a.packed = d_packed;
-    a.R = R;
-    a.win0 = 0;
-    a.nact = v.nact;
-    a.dm_first = 0;
-    a.dm_count = v.ndms;
-    a.nout = nout;
-    a.out = dout;
-    a.out_stride = (long)(out_stride / 4);
-    a.dpt = tb.dpt;
-    a.max_spread = tb.max_spread;
-    a.tile_meta = d_meta;
-    a.tile_off = d_off;
+    hg::DeviceTables dt{d_meta, d_off, tb.dpt, tb.max_spread, v.nact, 8};
+    const hg::DedispArgs a =
+        hg::single_beam_args(dt, d_packed, R, 0, 0, v.ndms, nout, dout, (long)(out_stride / 4), d_err);
     if (hg::dedisperse(a, s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
   }
-  if (!(flags & HDD_ASYNC) && cudaStreamSynchronize(s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+  if (!(flags & HDD_ASYNC)) {
+    if (cudaStreamSynchronize(s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+    int err = 0;
+    if (cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || err)
+      return HDD_INTERNAL_GPU_ERROR;  // err != 0: a staging wait timed out
+  }
   return HDD_NO_ERROR;
 }

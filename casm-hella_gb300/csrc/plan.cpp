@@ -84,8 +84,9 @@ struct hdd_plan_struct {
   int max_delay = 0;
   // dedispersion tile tables of the last DM range used, host and device
   hg::DedispTables tab;
-  int tab_first = -1, tab_count = -1;
+  int tab_first = -1, tab_count = -1, tab_dpt = -1, tab_cc = -1;
   bool tab_on_device = false;
+  int *d_err = nullptr;  // dedispersion status word
   int4 *d_meta = nullptr;
   int *d_off = nullptr;
   size_t meta_cap = 0, off_cap = 0;
@@ -99,7 +100,7 @@ namespace {
 thread_local int t_device = 0;
 
 void invalidate_tables(hdd_plan p) {
-  p->tab_first = p->tab_count = -1;
+  p->tab_first = p->tab_count = p->tab_dpt = p->tab_cc = -1;
   p->tab_on_device = false;
 }
 
@@ -133,18 +134,21 @@ hdd_error grow(void **ptr, size_t *cap, size_t need) {
 
 namespace hg {
 
-const DedispTables &plan_host_tables(hdd_plan p, int first, int count) {
-  if (p->tab_first != first || p->tab_count != count) {
-    p->tab = dedisp_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first, count);
+const DedispTables &plan_host_tables(hdd_plan p, int first, int count, int dpt, int cc) {
+  if (p->tab_first != first || p->tab_count != count || p->tab_dpt != dpt || p->tab_cc != cc) {
+    p->tab = dedisp_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first,
+                           count, dpt, cc);
     p->tab_first = first;
     p->tab_count = count;
+    p->tab_dpt = dpt;
+    p->tab_cc = cc;
     p->tab_on_device = false;
   }
   return p->tab;
 }
 
-hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out) {
-  const DedispTables &t = plan_host_tables(p, first, count);
+hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out, int dpt, int cc) {
+  const DedispTables &t = plan_host_tables(p, first, count, dpt, cc);
   if (!p->tab_on_device) {
     const size_t mb = std::max<size_t>(t.meta.size(), 1) * sizeof(int4);
     const size_t ob = std::max<size_t>(t.off.size(), 1) * sizeof(int);
@@ -162,7 +166,37 @@ hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out
   out->dpt = t.dpt;
   out->max_spread = t.max_spread;
   out->nact = (int)p->chans.size();
+  out->cc = cc;
   return HDD_NO_ERROR;
+}
+
+DedispArgs single_beam_args(const DeviceTables &tb, const uint32_t *packed, long R, long win0,
+                            int dm_first, int dm_count, int nout, float *out, long out_stride,
+                            int *err) {
+  DedispArgs a{};
+  a.beams = nullptr;
+  a.one.packed = packed;
+  a.one.out = out;
+  a.one.win0 = win0;
+  a.one.dm_count = dm_count;
+  a.one.item0 = 0;
+  a.nbeam = 1;
+  a.ntt = dedisp_time_tiles(nout);
+  a.nitems = dedisp_items(dm_count, tb.dpt, a.ntt);
+  a.group = kDedispGroup;
+  a.R = R;
+  a.nact = tb.nact;
+  a.dm_first = dm_first;
+  a.nout = nout;
+  a.out_stride = out_stride;
+  a.dpt = tb.dpt;
+  a.cc = tb.cc;
+  a.max_spread = tb.max_spread;
+  a.tile_meta = tb.meta;
+  a.tile_off = tb.off;
+  a.err = err;
+  a.unit = 1;
+  return a;
 }
 
 PlanView plan_view(hdd_plan p) {
@@ -207,6 +241,7 @@ void hdd_destroy_plan(hdd_plan p) {
   cudaSetDevice(p->device);
   cudaFree(p->d_meta);
   cudaFree(p->d_off);
+  cudaFree(p->d_err);
   cudaFree(p->d_in);
   cudaFree(p->d_plain);
   cudaFree(p->d_packed);
@@ -325,20 +360,15 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
     return HDD_INTERNAL_GPU_ERROR;
   if (hg::pack_ring(p->d_plain, p->d_packed, 1, p->nchans, R, 0, R, p->stream) != cudaSuccess)
     return HDD_INTERNAL_GPU_ERROR;
-  hg::DedispArgs a{};
-  a.packed = p->d_packed;
-  a.R = R;
-  a.win0 = 0;
-  a.nact = tb.nact;
-  a.dm_first = (int)first_dm_idx;
-  a.dm_count = (int)dm_count;
-  a.nout = nout;
-  a.out = dout;
-  a.out_stride = (long)(out_stride / 4);
-  a.dpt = tb.dpt;
-  a.max_spread = tb.max_spread;
-  a.tile_meta = tb.meta;
-  a.tile_off = tb.off;
+  if (!p->d_err) {
+    if (cudaMalloc((void **)&p->d_err, sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return HDD_MEM_ALLOC_FAILED;
+    }
+    if (cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+  }
+  const hg::DedispArgs a = hg::single_beam_args(tb, p->d_packed, R, 0, (int)first_dm_idx, (int)dm_count,
+                                                nout, dout, (long)(out_stride / 4), p->d_err);
   if (a.nact == 0) {
     for (hdd_size d = 0; d < dm_count; ++d)
       if (cudaMemsetAsync(reinterpret_cast<uint8_t *>(dout) + d * out_stride, 0, (size_t)nout * 4,
@@ -352,8 +382,16 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
                           cudaMemcpyDeviceToHost, p->stream) != cudaSuccess)
       return HDD_MEM_COPY_FAILED;
   }
-  if (!(flags & HDD_ASYNC) && cudaStreamSynchronize(p->stream) != cudaSuccess)
-    return HDD_INTERNAL_GPU_ERROR;
+  if (!(flags & HDD_ASYNC)) {
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+    int err = 0;
+    if (cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return HDD_INTERNAL_GPU_ERROR;
+    if (err) {
+      cudaMemset(p->d_err, 0, sizeof(int));
+      return HDD_INTERNAL_GPU_ERROR;  // a staging wait timed out
+    }
+  }
   return HDD_NO_ERROR;
 }
 

@@ -43,6 +43,8 @@ struct hella_ctx {
   std::vector<int> tap_n;
   bool loaded = false, flagged = false, smoothed = false;
   int dd_beam = -1;
+  int *d_err = nullptr;  // device status word of the staging waits
+  hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
 };
 
 namespace {
@@ -137,6 +139,132 @@ hella_status validate(const hella_params *p) {
   if (p->max_giants < 1) return HELLA_ERR_INVALID_ARG;
   if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
   if (p->nscrunch != 0) return HELLA_ERR_INVALID_ARG;  // scrunch flagging: not in this build
+  return HELLA_OK;
+}
+
+// Rejects shapes the kernels do not implement.
+bool tuning_ok(const hella_tuning &t) {
+  const bool dpt_ok = t.dm_per_block == 0 || t.dm_per_block == 1 || t.dm_per_block == 2 ||
+                      t.dm_per_block == 4 || t.dm_per_block == 8 || t.dm_per_block == 16;
+  return dpt_ok && (t.chan_chunk == 8 || t.chan_chunk == 16) &&
+         (t.stages == 0 || (t.stages >= 2 && t.stages <= 4)) && t.group >= 1 && t.group <= 4096 &&
+         t.add_mode >= 0 && t.add_mode <= 2;
+}
+
+// Dedisperses `beam`'s window into the plane with tile shape t.
+hella_status dedisperse_beam(hella_ctx *c, int beam, const hella_tuning &t) {
+  if (!tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  hg::DeviceTables tb;
+  if (hg::plan_device_tables(c->plan, 0, c->ndms, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
+    return HELLA_ERR_DEDISP;
+  if (t.add_mode && tb.dpt < 8) return HELLA_ERR_INVALID_ARG;
+  hg::DedispArgs a = hg::single_beam_args(tb, c->d_packed + (size_t)beam * c->p.nchan * c->R, c->R,
+                                          c->win0, 0, c->ndms, c->ntime_dd, c->d_dd, c->ntime_dd,
+                                          c->d_err);
+  a.group = t.group;
+  a.nbuf = t.stages;
+  a.mode = t.add_mode;
+  if (tb.nact == 0)
+    CK(cudaMemsetAsync(c->d_dd, 0, (size_t)c->ndms * c->ntime_dd * 4, c->stream));
+  else
+    CK(hg::dedisperse(a, c->stream));
+  return HELLA_OK;
+}
+
+// Best of `reps` timed dedispersions of beam 0 with shape t, in ms; the
+// first run (table upload, warm-up) is not timed.
+hella_status time_shape(hella_ctx *c, const hella_tuning &t, int reps, float *ms) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    cudaGetLastError();
+    return HELLA_ERR_CUDA;
+  }
+  float best = 3.4e38f;
+  hella_status s = HELLA_OK;
+  for (int r = 0; r <= reps && s == HELLA_OK; ++r) {
+    if (cudaEventRecord(e0, c->stream) != cudaSuccess) { s = HELLA_ERR_CUDA; break; }
+    s = dedisperse_beam(c, 0, t);
+    if (s != HELLA_OK) break;
+    if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+      s = HELLA_ERR_CUDA;
+      break;
+    }
+    float m = 0.f;
+    cudaEventElapsedTime(&m, e0, e1);
+    if (r > 0) best = std::min(best, m);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != HELLA_OK) {
+    cudaGetLastError();
+    return s;
+  }
+  int err = 0;
+  CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(c->d_err, 0, sizeof(int));
+    return HELLA_ERR_TIMEOUT;
+  }
+  *ms = best;
+  return HELLA_OK;
+}
+
+// Coordinate search: add mode, channel chunk, DM tile, pipeline depth,
+// group, each with the others held at the best so far.
+hella_status autotune(hella_ctx *c, int reps, hella_tuning *out, float *out_ms) {
+  hella_tuning best = c->tune;
+  float best_ms = 3.4e38f;
+  hella_status s = time_shape(c, best, reps, &best_ms);
+  if (s != HELLA_OK) return s;
+  auto try_shape = [&](hella_tuning t) -> hella_status {
+    if (!tuning_ok(t)) return HELLA_OK;
+    float ms = 0.f;
+    const hella_status r = time_shape(c, t, reps, &ms);
+    if (r == HELLA_ERR_INVALID_ARG) return HELLA_OK;  // not a shape for this DM list
+    if (r == HELLA_ERR_CUDA) {                       // e.g. staging beyond shared memory
+      cudaGetLastError();
+      return HELLA_OK;
+    }
+    if (r != HELLA_OK) return r;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = t;
+    }
+    return HELLA_OK;
+  };
+  const int dpts[] = {16, 8};
+  for (int round = 0; round < 2; ++round) {
+    for (int m = 0; m <= 2; ++m) {
+      hella_tuning t = best;
+      t.add_mode = m;
+      if ((s = try_shape(t)) != HELLA_OK) return s;
+    }
+    for (int cc : {8, 16}) {
+      hella_tuning t = best;
+      t.chan_chunk = cc;
+      if ((s = try_shape(t)) != HELLA_OK) return s;
+    }
+    for (int d : dpts) {
+      hella_tuning t = best;
+      t.dm_per_block = d;
+      if ((s = try_shape(t)) != HELLA_OK) return s;
+    }
+    for (int nb : {2, 3, 4}) {
+      hella_tuning t = best;
+      t.stages = nb;
+      if ((s = try_shape(t)) != HELLA_OK) return s;
+    }
+    for (int g : {2, 4, 8, 16, 32}) {
+      hella_tuning t = best;
+      t.group = g;
+      if ((s = try_shape(t)) != HELLA_OK) return s;
+    }
+  }
+  c->tune = best;
+  if (out) *out = best;
+  if (out_ms) *out_ms = best_ms;
   return HELLA_OK;
 }
 
@@ -252,6 +380,7 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   DA(c->d_total, 16);
   DA(c->d_cand_i, (size_t)p->max_giants * 16);
   DA(c->d_cand_v, (size_t)p->max_giants * 4);
+  DA(c->d_err, 16);
 #undef DA
   if ((s = halloc(c, (void **)&c->h_cand_i, (size_t)p->max_giants * 16)) != HELLA_OK) return fail(s);
   if ((s = halloc(c, (void **)&c->h_cand_v, (size_t)p->max_giants * 4)) != HELLA_OK) return fail(s);
@@ -278,10 +407,12 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
       cudaMemset(c->d_plain, 0, nb * nch * R) != cudaSuccess ||
       cudaMemset(c->d_packed, 0, nb * nch * R * 4) != cudaSuccess ||
       cudaMemset(c->d_flagspec, 0, nch * 4) != cudaSuccess ||
+      cudaMemset(c->d_err, 0, 16) != cudaSuccess ||
       cudaDeviceSynchronize() != cudaSuccess) {
     cudaGetLastError();
     return fail(HELLA_ERR_CUDA);
   }
+  if (p->autotune && (s = autotune(c, 2, nullptr, nullptr)) != HELLA_OK) return fail(s);
   *out = c;
   return HELLA_OK;
 }
@@ -337,26 +468,8 @@ hella_status hella_fast_flagger(hella_ctx *c) {
 hella_status hella_dedisperse(hella_ctx *c, int beam) {
   if (!c || beam < 0 || beam >= c->p.nbeam) return HELLA_ERR_INVALID_ARG;
   if (!c->flagged) return HELLA_ERR_STATE;
-  hg::DeviceTables tb;
-  if (hg::plan_device_tables(c->plan, 0, c->ndms, &tb) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
-  hg::DedispArgs a{};
-  a.packed = c->d_packed + (size_t)beam * c->p.nchan * c->R;
-  a.R = c->R;
-  a.win0 = c->win0;
-  a.nact = tb.nact;
-  a.dm_first = 0;
-  a.dm_count = c->ndms;
-  a.nout = c->ntime_dd;
-  a.out = c->d_dd;
-  a.out_stride = c->ntime_dd;
-  a.dpt = tb.dpt;
-  a.max_spread = tb.max_spread;
-  a.tile_meta = tb.meta;
-  a.tile_off = tb.off;
-  if (tb.nact == 0)
-    CK(cudaMemsetAsync(c->d_dd, 0, (size_t)c->ndms * c->ntime_dd * 4, c->stream));
-  else
-    CK(hg::dedisperse(a, c->stream));
+  hella_status s = dedisperse_beam(c, beam, c->tune);
+  if (s != HELLA_OK) return s;
   c->dd_beam = beam;
   c->smoothed = false;
   return HELLA_OK;
@@ -393,7 +506,12 @@ hella_status hella_find_peaks(hella_ctx *c, int beam) {
   pk.cand_v = c->d_cand_v;
   CK(hg::find_peaks(pk, c->stream));
   CK(cudaMemcpyAsync(c->h_total, c->d_total, 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(c->h_total + 1, c->d_err, 4, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (c->h_total[1]) {  // a dedispersion staging wait timed out
+    cudaMemsetAsync(c->d_err, 0, 4, c->stream);
+    return HELLA_ERR_TIMEOUT;
+  }
   const int n = std::min(*c->h_total, cap);
   if (n > 0) {
     CK(cudaMemcpyAsync(c->h_cand_i, c->d_cand_i, (size_t)n * 16, cudaMemcpyDeviceToHost, c->stream));
@@ -538,6 +656,31 @@ hella_status hella_get_flag_spec(hella_ctx *c, float *out) {
   CK(cudaMemcpyAsync(out, c->d_flagspec, (size_t)c->p.nchan * 4, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return HELLA_OK;
+}
+
+hella_status hella_get_tuning(const hella_ctx *c, hella_tuning *t) {
+  if (!c || !t) return HELLA_ERR_INVALID_ARG;
+  *t = c->tune;
+  return HELLA_OK;
+}
+
+hella_status hella_set_tuning(hella_ctx *c, const hella_tuning *t) {
+  if (!c || !t || !tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
+  c->tune = *t;
+  c->tune.samples_per_thread = 4;
+  return HELLA_OK;
+}
+
+hella_status hella_time_dedisp(hella_ctx *c, const hella_tuning *t, int reps, float *ms) {
+  if (!c || !ms || reps < 1) return HELLA_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->p.device));
+  return time_shape(c, t ? *t : c->tune, reps, ms);
+}
+
+hella_status hella_autotune(hella_ctx *c, int reps, hella_tuning *best, float *best_ms) {
+  if (!c || reps < 1) return HELLA_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->p.device));
+  return autotune(c, reps, best, best_ms);
 }
 
 const char *hella_status_string(hella_status s) {

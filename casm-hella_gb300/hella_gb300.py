@@ -48,8 +48,16 @@ class HellaParams(C.Structure):
         ("spec_min", C.c_float), ("spec_max", C.c_float), ("flag1", C.c_int), ("flag2", C.c_int),
         ("nscrunch", C.c_int), ("scrunch", HellaScrunch * HELLA_MAX_SCRUNCH),
         ("max_giants", C.c_int), ("beam0", C.c_int), ("smooth_anchor", C.c_int), ("device", C.c_int),
-        ("hbm_budget", C.c_size_t),
+        ("hbm_budget", C.c_size_t), ("autotune", C.c_int),
     ]
+
+
+class HellaTuning(C.Structure):
+    _fields_ = [("dm_per_block", C.c_int), ("samples_per_thread", C.c_int), ("chan_chunk", C.c_int),
+                ("stages", C.c_int), ("group", C.c_int), ("add_mode", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class HellaInfo(C.Structure):
@@ -132,6 +140,10 @@ def lib() -> C.CDLL:
     _sig(L, "hella_get_flag_stats", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP])
     _sig(L, "hella_get_flag_spec", C.c_int, [_VP, _VP])
     _sig(L, "hella_status_string", C.c_char_p, [C.c_int])
+    _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
+    _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
+    _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
+    _sig(L, "hella_autotune", C.c_int, [_VP, C.c_int, C.POINTER(HellaTuning), C.POINTER(C.c_float)])
     _sig(L, "hella_fp16_selftest", C.c_int, [C.c_int, C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint32)])
     _sig(L, "hella_int_add_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)])
     _sig(L, "hella_kernel_launches", C.c_ulonglong, [])
@@ -369,6 +381,24 @@ class Search:
         _chk(self.L.hella_get_flag_stats(self.h, beam, bp1.ctypes.data, bp2.ctypes.data, bp3.ctypes.data,
                                          sc.ctypes.data, ts.ctypes.data))
         return dict(bp1=bp1, bp2=bp2, bp3=bp3, mean1=sc[0], std1=sc[1], mean2=sc[2], std2=sc[3], ts=ts)
+
+    def get_tuning(self) -> HellaTuning:
+        t = HellaTuning()
+        _chk(self.L.hella_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, t: HellaTuning):
+        _chk(self.L.hella_set_tuning(self.h, C.byref(t)))
+
+    def time_dedisp(self, t: HellaTuning | None = None, reps: int = 3) -> float:
+        ms = C.c_float()
+        _chk(self.L.hella_time_dedisp(self.h, None if t is None else C.byref(t), reps, C.byref(ms)))
+        return ms.value
+
+    def autotune(self, reps: int = 2):
+        t, ms = HellaTuning(), C.c_float()
+        _chk(self.L.hella_autotune(self.h, reps, C.byref(t), C.byref(ms)))
+        return t, ms.value
 
     def flag_spec(self) -> np.ndarray:
         out = np.zeros(self.params.nchan, np.float32)

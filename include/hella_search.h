@@ -80,7 +80,24 @@ typedef struct {
   int device;       /* GPU */
   size_t hbm_budget;/* 0 = unlimited; otherwise creation fails with
                        HELLA_ERR_BUDGET if the context would need more */
+  int autotune;     /* 1: hella_create times dedispersion tile shapes on the
+                       context's own buffers and keeps the fastest */
 } hella_params;
+
+/* Dedispersion tile shape (no counterpart in the reference, whose dedisp
+ * library fixes its own).  Every shape computes the same exact sums. */
+typedef struct {
+  int dm_per_block;       /* DM trials per tile: 16, 8, 4, 2, 1; 0 = largest
+                             whose staging fits two blocks per SM */
+  int samples_per_thread; /* 4: fixed by the packed ring (reported only) */
+  int chan_chunk;         /* channels per staging step: 8 or 16 */
+  int stages;             /* staging buffers in flight: 2..4; 0 = deepest
+                             that fits two blocks per SM */
+  int group;              /* DM tiles walked together per time tile (L2) */
+  int add_mode;           /* 0: three-input adds; 1: load addresses as
+                             multiply-adds (FMA pipe); 2: 1 + odd lanes too
+                             (1 and 2 need dm_per_block >= 8) */
+} hella_tuning;
 
 /* Derived sizes (casm_hella_refactored.cu:184-224). */
 typedef struct {
@@ -132,6 +149,19 @@ hella_status hella_get_peaks(hella_ctx *ctx, hella_cand *out, int max,
 hella_status hella_process_gulp(hella_ctx *ctx, const uint8_t *gulp,
                                 int on_device, hella_cand *out, int max,
                                 int *n, int *searched);
+
+/* Tile shape of the context's dedispersion (see hella_tuning). */
+hella_status hella_get_tuning(const hella_ctx *ctx, hella_tuning *t);
+hella_status hella_set_tuning(hella_ctx *ctx, const hella_tuning *t);
+/* Times one dedispersion of the context's ring with shape t (the current
+ * shape if t is NULL): best of `reps` runs, milliseconds.  Overwrites the
+ * dedispersed plane; call between gulps.  Synchronous. */
+hella_status hella_time_dedisp(hella_ctx *ctx, const hella_tuning *t, int reps,
+                               float *ms);
+/* Coordinate search over the tile shape, keeping the fastest; *best and
+ * *best_ms (may be NULL) receive it.  Call between gulps.  Synchronous. */
+hella_status hella_autotune(hella_ctx *ctx, int reps, hella_tuning *best,
+                            float *best_ms);
 
 /* Inspection (host copies, synchronous). */
 /* The beam's search window, u8 [ntime][nchan] time-major, oldest first. */

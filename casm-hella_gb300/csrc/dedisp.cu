@@ -388,9 +388,11 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
 }
 
 __global__ void k_pack(const uint8_t *__restrict__ plain, uint32_t *__restrict__ packed,
-                       int nchan, long R, long q0, long nq, const uint8_t *__restrict__ keep) {
+                       int nchan, long R, long q0, long nq, const uint8_t *__restrict__ keep,
+                       const GulpPos *dpos) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nq) return;
+  if (dpos) q0 = ((dpos->wpos - 3L * S) % R + R) % R;
   const size_t bc = (size_t)blockIdx.z * nchan + blockIdx.y;
   const size_t row = bc * (size_t)R;
   const long q = (q0 + i) % R;
@@ -545,7 +547,16 @@ cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam, int nch
   q0 = ((q0 % R) + R) % R;
   nq = std::min(nq, R);  // each ring position once
   const dim3 grid((unsigned)((nq + 255) / 256), nchan, nbeam);
-  k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq, keep);
+  k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq, keep, nullptr);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t pack_gulp_dev(const uint8_t *plain, uint32_t *packed, int nbeam, int nchan, long R,
+                          int gulp, const GulpPos *pos, cudaStream_t s, const uint8_t *keep) {
+  const long nq = std::min((long)gulp + 3L * S, R);  // each ring position once
+  const dim3 grid((unsigned)((nq + 255) / 256), nchan, nbeam);
+  k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, 0, nq, keep, pos);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -230,7 +230,8 @@ __device__ __forceinline__ uint8_t requant(__half h) {
 // Final stage: divide_by_ts, normalize_data, requantise, and write the
 // channel-major ring (32 x 32 tiles transposed through shared memory).
 __global__ void k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
-                           uint8_t *__restrict__ plain, long R, long wpos) {
+                           uint8_t *__restrict__ plain, long R, long wpos, const GulpPos *dpos) {
+  if (dpos) wpos = dpos->wpos;
   __shared__ uint8_t tile[32][33];
   const int b = blockIdx.z, c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y, nchan = st.nchan, w = st.gulp;
@@ -258,8 +259,9 @@ __global__ void k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
 
 }  // namespace
 
-cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
-                      long R, long wpos, cudaStream_t s) {
+namespace {
+cudaError_t flag_impl(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+                      const GulpPos *dpos, cudaStream_t s) {
   const dim3 lutg(st.nchan, st.nbeam);
   const dim3 laneg(st.nchan / kCT, 32 / 8, st.nbeam);
   const dim3 rowg(st.nchan / kCT, 256 / 8, st.nbeam);
@@ -298,9 +300,20 @@ cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
   k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 1);
   // transpose_output into the ring
   k_flag_out<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(gulp, st, plain,
-                                                                                 R, wpos);
+                                                                                 R, wpos, dpos);
   count_launches(24);
   return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+                      cudaStream_t s) {
+  return flag_impl(st, gulp, plain, R, wpos, nullptr, s);
+}
+
+cudaError_t flag_gulp_dev(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R,
+                          const GulpPos *pos, cudaStream_t s) {
+  return flag_impl(st, gulp, plain, R, 0, pos, s);
 }
 
 // ----------------------------------------------------------- self-check

@@ -53,6 +53,9 @@ struct FlagState {
 // position `wpos` (mod R) of every beam.
 cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
                       long R, long wpos, cudaStream_t s);
+// As above with the ring position read on the device from pos->wpos.
+cudaError_t flag_gulp_dev(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
+                          long R, const struct GulpPos *pos, cudaStream_t s);
 
 // ---------------------------------------------------------- packing
 // Rebuild packed words at ring positions [q0, q0 + nq) (mod R) of every
@@ -61,6 +64,11 @@ cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
 cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam,
                       int nchan, long R, long q0, long nq, cudaStream_t s,
                       const uint8_t *keep = nullptr);
+// Rebuilds the words a gulp written at pos->wpos changed:
+// [wpos - 3*kPackS, wpos + gulp) mod R.
+cudaError_t pack_gulp_dev(const uint8_t *plain, uint32_t *packed, int nbeam, int nchan,
+                          long R, int gulp, const struct GulpPos *pos, cudaStream_t s,
+                          const uint8_t *keep);
 // Time-major input [nsamps][in_stride] -> channel-major plain [nchan][R].
 cudaError_t transpose_tf(const uint8_t *in, size_t in_stride, int nsamps,
                          int nchan, uint8_t *plain, long R, cudaStream_t s);
@@ -123,40 +131,58 @@ int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int 
                   int dm_first, int dm_count, int dpt);
 
 // ------------------------------------------------------- smoothing
-struct SmoothArgs {
-  const float *dd;          // [ndms][dd_stride]
+// One beam of a smoothing / peak-finding launch (device array).
+struct SmoothBeam {
+  const float *dd;          // [ndms][dd_stride] dedispersed plane
   long dd_stride;
-  int ndms, ntime_dd, ntime_out;
-  int nbox, wmin, wmax, anchor;
-  const float *taps;        // middle-row taps of every width, padded
-  const int *tap_off;       // [nbox] offset into taps
-  const int *tap_n;         // [nbox] padded tap count (multiple of 8)
-  int max_taps;             // 2*sm_max + 1
-  float *boxes;             // [nbox][ndms-2][ntime_out]
-  float *rowmean;           // [nbox][ndms-2]
-  float *rowmax;            // [nbox][ndms-2]
-  float *rowvar;            // [nbox][ndms-2]
+  float *boxes;             // [nw][h][ntime_out]: the launch's widths w0.. (pre-normalise)
+  float *rowmean, *rowmax, *rowvar;  // [nbox][h]
   float *stats;             // [nbox][4] mean, std, -mean, 1/std
-  float *gate;              // [4]: mean0n, sigma0n, threshold, pass
-  float snr;
-};
-cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s);
-// scale = 1: per-width mean/std (normalisation); 0: planes left as they are.
-// Both then form the width-0 gate statistics.
-cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale);
-
-struct PeakArgs {
-  const SmoothArgs *sm;
-  int *counts;              // [nbox][ndms-2]
-  int *offsets;             // [nbox][ndms-2]
-  int *total;               // [1] candidates found (capped at cap)
-  int cap;
-  int beam;                 // reported beam index
+  float *gate;              // [4] mean0n, sigma0n, threshold, pass
+  int *counts, *offsets;    // [nbox][h]
   int4 *cand_i;             // [cap] beam, dm_idx, width, samp
   float *cand_v;            // [cap] normalised value
+  int *total;               // [1] candidates written so far (capped at cap)
+  const int *active;        // searched this gulp (0: every kernel skips the beam)
+  int h;                    // rows: ndms - 2
+  int row0;                 // first global row of the beam
+  int cap;                  // candidate cap of the beam
+  int beam_id;              // reported beam index
 };
-cudaError_t find_peaks(const PeakArgs &a, cudaStream_t s);
-// Normalised copy of the planes (inspection).
+
+struct SmoothArgs {
+  const SmoothBeam *beams;  // device [nbeam]
+  int nbeam;
+  const int *row_beam;      // device [nrows]: beam of each global row
+  int nrows;                // sum of the beams' h
+  int ntime_dd, ntime_out;
+  int nbox, wmin, wmax, anchor;
+  int w0, nw;               // widths of this launch: w0 .. w0 + nw - 1
+  const float *taps;        // middle-row taps of every width, padded
+  const int *tap_off;       // [nbox] offset into taps
+  const int *tap_n;         // [nbox] padded tap count (multiple of 16)
+  float snr;
+};
+// Shared memory of the FIR launch.
+size_t fir_smem_bytes(const SmoothArgs &a);
+cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s);
+// scale = 1: per-width mean/std (normalisation); 0: planes left as they
+// are.  A launch holding width 0 then forms the beams' gate statistics.
+cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale);
+// Candidates of the launch's widths, appended to each beam's list after
+// those of earlier widths (reset `total` before width 0).
+cudaError_t find_peaks(const SmoothArgs &a, cudaStream_t s);
+// Normalised copy of beam 0's planes (inspection).
 cudaError_t normalise_copy(const SmoothArgs &a, float *dst, cudaStream_t s);
+
+// ----------------------------------------------------- ring position
+// Ring positions of the gulp being processed, kept in device memory so that
+// a captured CUDA graph can be replayed gulp after gulp.
+struct GulpPos {
+  long win0;                // window start of a full-ring (R-sample) window
+  long wpos;                // where the gulp is written: (win0 + R - gulp) % R
+  int gulp_index;           // gulps processed before this one
+  int pad;
+};
 
 }  // namespace hg

@@ -11,11 +11,70 @@
 #include "hella_dedisp.h"
 #include "hg_internal.h"
 #include "hg_plan.h"
+#include "hg_search.h"
+#include "hg_tune.h"
 
 #include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
+
+namespace hg {
+
+// smooth.cpp:42-58: 3 x (2sm+1) taps, v from a double expression stored as
+// float, products and normalising sum in float.  Returns the middle row.
+std::vector<float> middle_taps(int sm) {
+  const float wt[3] = {0.3f, 1.f, 0.3f};
+  const int n = 2 * sm + 1;
+  std::vector<float> k(3 * n);
+  float filtSum = 0.f;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double u = (j - sm) / (sm / 2.355);
+      const float v = (float)(1. - 0.5 * u * u + 0.25 * u * u * 0.25 * u * u -
+                              0.083 * u * u * 0.083 * u * u * 0.083 * u * u);
+      const float kv = wt[i] * v * v;
+      k[i * n + j] = kv;
+      filtSum += kv;
+    }
+  std::vector<float> mid(n);
+  for (int j = 0; j < n; ++j) mid[j] = k[n + j] / filtSum;
+  return mid;
+}
+
+void smoothing_taps(const hella_params &p, int nbox, std::vector<float> *taps, std::vector<int> *off,
+                    std::vector<int> *n) {
+  taps->clear();
+  off->clear();
+  n->clear();
+  for (int b = 0; b < nbox; ++b) {
+    std::vector<float> m = middle_taps(p.width_min << b);
+    off->push_back((int)taps->size());
+    const int np = ((int)m.size() + 15) / 16 * 16;  // zero padded to a multiple of 16
+    n->push_back(np);
+    m.resize(np, 0.f);
+    taps->insert(taps->end(), m.begin(), m.end());
+  }
+}
+
+hella_status validate_params(const hella_params *p) {
+  if (!p) return HELLA_ERR_INVALID_ARG;
+  if (p->nchan < 32 || p->nchan % 32 != 0 || p->nchan > 8192) return HELLA_ERR_INVALID_ARG;
+  if (p->nbeam < 1 || p->nbeam > 65535) return HELLA_ERR_INVALID_ARG;
+  if (p->gulp < 256 || p->gulp % 32 != 0) return HELLA_ERR_INVALID_ARG;
+  if (!(p->tsamp > 0) || !(p->plan_dt > 0) || !(p->f0_mhz > 0) || !(p->df_mhz != 0))
+    return HELLA_ERR_INVALID_ARG;
+  if (p->f0_mhz - p->nchan * std::abs(p->df_mhz) <= 0) return HELLA_ERR_INVALID_ARG;
+  if (!(p->dm_max >= p->dm_min) || p->dm_min < 0 || !(p->dm_tol > 1)) return HELLA_ERR_INVALID_ARG;
+  if (p->width_min < 1 || p->width_max <= p->width_min || p->width_max > 4096)
+    return HELLA_ERR_INVALID_ARG;
+  if (p->max_giants < 1) return HELLA_ERR_INVALID_ARG;
+  if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
+  if (p->nscrunch != 0) return HELLA_ERR_INVALID_ARG;  // scrunch flagging: not in this build
+  return HELLA_OK;
+}
+
+}  // namespace hg
 
 struct hella_ctx {
   hella_params p{};
@@ -34,6 +93,9 @@ struct hella_ctx {
   float *d_rowmean = nullptr, *d_rowmax = nullptr, *d_rowvar = nullptr, *d_stats = nullptr,
         *d_gate = nullptr, *d_flagspec = nullptr;
   int *d_counts = nullptr, *d_offsets = nullptr, *d_total = nullptr;
+  // one-beam table of the smoothing kernels (updated before each peak pass)
+  hg::SmoothBeam *d_sbeam = nullptr, *h_sbeam = nullptr;
+  int *d_row_beam = nullptr, *d_active = nullptr;
   int4 *d_cand_i = nullptr;
   float *d_cand_v = nullptr;
   int4 *h_cand_i = nullptr;
@@ -48,6 +110,8 @@ struct hella_ctx {
 };
 
 namespace {
+
+const int kOne = 1;
 
 #define CK(x)                                      \
   do {                                             \
@@ -80,80 +144,61 @@ hella_status halloc(hella_ctx *c, void **ptr, size_t bytes) {
   return HELLA_OK;
 }
 
-// smooth.cpp:42-58: 3 x (2sm+1) taps, v from a double expression stored as
-// float, products and normalising sum in float.  Returns the middle row.
-std::vector<float> middle_taps(int sm) {
-  const float wt[3] = {0.3f, 1.f, 0.3f};
-  const int n = 2 * sm + 1;
-  std::vector<float> k(3 * n);
-  float filtSum = 0.f;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < n; ++j) {
-      const double u = (j - sm) / (sm / 2.355);
-      const float v = (float)(1. - 0.5 * u * u + 0.25 * u * u * 0.25 * u * u -
-                              0.083 * u * u * 0.083 * u * u * 0.083 * u * u);
-      const float kv = wt[i] * v * v;
-      k[i * n + j] = kv;
-      filtSum += kv;
-    }
-  std::vector<float> mid(n);
-  for (int j = 0; j < n; ++j) mid[j] = k[n + j] / filtSum;
-  return mid;
-}
-
 hg::SmoothArgs smooth_args(hella_ctx *c) {
   hg::SmoothArgs a{};
-  a.dd = c->d_dd;
-  a.dd_stride = c->ntime_dd;
-  a.ndms = c->ndms;
+  a.beams = c->d_sbeam;
+  a.nbeam = 1;
+  a.row_beam = c->d_row_beam;
+  a.nrows = c->ndms - 2;
   a.ntime_dd = c->ntime_dd;
   a.ntime_out = c->ntime_out;
   a.nbox = c->nbox;
   a.wmin = c->p.width_min;
   a.wmax = c->p.width_max;
   a.anchor = c->p.smooth_anchor;
+  a.w0 = 0;
+  a.nw = c->nbox;
   a.taps = c->d_taps;
   a.tap_off = c->d_tapoff;
   a.tap_n = c->d_tapn;
-  a.boxes = c->d_boxes;
-  a.rowmean = c->d_rowmean;
-  a.rowmax = c->d_rowmax;
-  a.rowvar = c->d_rowvar;
-  a.stats = c->d_stats;
-  a.gate = c->d_gate;
   a.snr = c->p.snr;
   return a;
 }
 
-hella_status validate(const hella_params *p) {
-  if (!p) return HELLA_ERR_INVALID_ARG;
-  if (p->nchan < 32 || p->nchan % 32 != 0 || p->nchan > 8192) return HELLA_ERR_INVALID_ARG;
-  if (p->nbeam < 1 || p->nbeam > 65535) return HELLA_ERR_INVALID_ARG;
-  if (p->gulp < 256 || p->gulp % 32 != 0) return HELLA_ERR_INVALID_ARG;
-  if (!(p->tsamp > 0) || !(p->plan_dt > 0) || !(p->f0_mhz > 0) || !(p->df_mhz != 0))
-    return HELLA_ERR_INVALID_ARG;
-  if (p->f0_mhz - p->nchan * std::abs(p->df_mhz) <= 0) return HELLA_ERR_INVALID_ARG;
-  if (!(p->dm_max >= p->dm_min) || p->dm_min < 0 || !(p->dm_tol > 1)) return HELLA_ERR_INVALID_ARG;
-  if (p->width_min < 1 || p->width_max <= p->width_min || p->width_max > 4096)
-    return HELLA_ERR_INVALID_ARG;
-  if (p->max_giants < 1) return HELLA_ERR_INVALID_ARG;
-  if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
-  if (p->nscrunch != 0) return HELLA_ERR_INVALID_ARG;  // scrunch flagging: not in this build
+// The context's one-beam smoothing table with candidate cap `cap` and
+// reported beam `beam_id`, copied to the device on the context's stream.
+hella_status upload_beam(hella_ctx *c, int cap, int beam_id) {
+  hg::SmoothBeam &B = *c->h_sbeam;
+  B.dd = c->d_dd;
+  B.dd_stride = c->ntime_dd;
+  B.boxes = c->d_boxes;
+  B.rowmean = c->d_rowmean;
+  B.rowmax = c->d_rowmax;
+  B.rowvar = c->d_rowvar;
+  B.stats = c->d_stats;
+  B.gate = c->d_gate;
+  B.counts = c->d_counts;
+  B.offsets = c->d_offsets;
+  B.cand_i = c->d_cand_i;
+  B.cand_v = c->d_cand_v;
+  B.total = c->d_total;
+  B.active = c->d_active;
+  B.h = c->ndms - 2;
+  B.row0 = 0;
+  B.cap = cap;
+  B.beam_id = beam_id;
+  if (cudaMemcpyAsync(c->d_sbeam, c->h_sbeam, sizeof(hg::SmoothBeam), cudaMemcpyHostToDevice,
+                      c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return HELLA_ERR_CUDA;
+  }
   return HELLA_OK;
 }
 
-// Rejects shapes the kernels do not implement.
-bool tuning_ok(const hella_tuning &t) {
-  const bool dpt_ok = t.dm_per_block == 0 || t.dm_per_block == 1 || t.dm_per_block == 2 ||
-                      t.dm_per_block == 4 || t.dm_per_block == 8 || t.dm_per_block == 16;
-  return dpt_ok && (t.chan_chunk == 8 || t.chan_chunk == 16) &&
-         (t.stages == 0 || (t.stages >= 2 && t.stages <= 4)) && t.group >= 1 && t.group <= 4096 &&
-         t.add_mode >= 0 && t.add_mode <= 2;
-}
 
 // Dedisperses `beam`'s window into the plane with tile shape t.
 hella_status dedisperse_beam(hella_ctx *c, int beam, const hella_tuning &t) {
-  if (!tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
   hg::DeviceTables tb;
   if (hg::plan_device_tables(c->plan, 0, c->ndms, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
     return HELLA_ERR_DEDISP;
@@ -171,97 +216,26 @@ hella_status dedisperse_beam(hella_ctx *c, int beam, const hella_tuning &t) {
   return HELLA_OK;
 }
 
-// Best of `reps` timed dedispersions of beam 0 with shape t, in ms; the
-// first run (table upload, warm-up) is not timed.
+// Best of `reps` timed dedispersions of beam 0 with shape t, in ms.
 hella_status time_shape(hella_ctx *c, const hella_tuning &t, int reps, float *ms) {
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  if (cudaEventCreate(&e1) != cudaSuccess) {
-    cudaEventDestroy(e0);
-    cudaGetLastError();
-    return HELLA_ERR_CUDA;
-  }
-  float best = 3.4e38f;
-  hella_status s = HELLA_OK;
-  for (int r = 0; r <= reps && s == HELLA_OK; ++r) {
-    if (cudaEventRecord(e0, c->stream) != cudaSuccess) { s = HELLA_ERR_CUDA; break; }
-    s = dedisperse_beam(c, 0, t);
-    if (s != HELLA_OK) break;
-    if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-      s = HELLA_ERR_CUDA;
-      break;
-    }
-    float m = 0.f;
-    cudaEventElapsedTime(&m, e0, e1);
-    if (r > 0) best = std::min(best, m);
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (s != HELLA_OK) {
-    cudaGetLastError();
-    return s;
-  }
+  hella_status s = hg::time_runs(c->stream, reps, [&] { return dedisperse_beam(c, 0, t); }, ms);
+  if (s != HELLA_OK) return s;
   int err = 0;
   CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     cudaMemset(c->d_err, 0, sizeof(int));
     return HELLA_ERR_TIMEOUT;
   }
-  *ms = best;
   return HELLA_OK;
 }
 
-// Coordinate search: add mode, channel chunk, DM tile, pipeline depth,
-// group, each with the others held at the best so far.
 hella_status autotune(hella_ctx *c, int reps, hella_tuning *out, float *out_ms) {
-  hella_tuning best = c->tune;
-  float best_ms = 3.4e38f;
-  hella_status s = time_shape(c, best, reps, &best_ms);
+  hella_tuning best;
+  float best_ms = 0.f;
+  const hella_status s = hg::tune_shapes(
+      c->tune, [&](const hella_tuning &t, float *ms) { return time_shape(c, t, reps, ms); }, &best,
+      &best_ms);
   if (s != HELLA_OK) return s;
-  auto try_shape = [&](hella_tuning t) -> hella_status {
-    if (!tuning_ok(t)) return HELLA_OK;
-    float ms = 0.f;
-    const hella_status r = time_shape(c, t, reps, &ms);
-    if (r == HELLA_ERR_INVALID_ARG) return HELLA_OK;  // not a shape for this DM list
-    if (r == HELLA_ERR_CUDA) {                       // e.g. staging beyond shared memory
-      cudaGetLastError();
-      return HELLA_OK;
-    }
-    if (r != HELLA_OK) return r;
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = t;
-    }
-    return HELLA_OK;
-  };
-  const int dpts[] = {16, 8};
-  for (int round = 0; round < 2; ++round) {
-    for (int m = 0; m <= 2; ++m) {
-      hella_tuning t = best;
-      t.add_mode = m;
-      if ((s = try_shape(t)) != HELLA_OK) return s;
-    }
-    for (int cc : {8, 16}) {
-      hella_tuning t = best;
-      t.chan_chunk = cc;
-      if ((s = try_shape(t)) != HELLA_OK) return s;
-    }
-    for (int d : dpts) {
-      hella_tuning t = best;
-      t.dm_per_block = d;
-      if ((s = try_shape(t)) != HELLA_OK) return s;
-    }
-    for (int nb : {2, 3, 4}) {
-      hella_tuning t = best;
-      t.stages = nb;
-      if ((s = try_shape(t)) != HELLA_OK) return s;
-    }
-    for (int g : {2, 4, 8, 16, 32}) {
-      hella_tuning t = best;
-      t.group = g;
-      if ((s = try_shape(t)) != HELLA_OK) return s;
-    }
-  }
   c->tune = best;
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
@@ -309,7 +283,7 @@ void hella_destroy(hella_ctx *c) {
 hella_status hella_create(hella_ctx **out, const hella_params *p) {
   if (!out) return HELLA_ERR_INVALID_ARG;
   *out = nullptr;
-  hella_status st = validate(p);
+  hella_status st = hg::validate_params(p);
   if (st != HELLA_OK) return st;
   if (cudaSetDevice(p->device) != cudaSuccess) {
     cudaGetLastError();
@@ -381,22 +355,19 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   DA(c->d_cand_i, (size_t)p->max_giants * 16);
   DA(c->d_cand_v, (size_t)p->max_giants * 4);
   DA(c->d_err, 16);
+  DA(c->d_sbeam, sizeof(hg::SmoothBeam));
+  DA(c->d_row_beam, (size_t)c->ndms * 4);
+  DA(c->d_active, 16);
 #undef DA
   if ((s = halloc(c, (void **)&c->h_cand_i, (size_t)p->max_giants * 16)) != HELLA_OK) return fail(s);
   if ((s = halloc(c, (void **)&c->h_cand_v, (size_t)p->max_giants * 4)) != HELLA_OK) return fail(s);
   if ((s = halloc(c, (void **)&c->h_total, 16)) != HELLA_OK) return fail(s);
+  if ((s = halloc(c, (void **)&c->h_sbeam, sizeof(hg::SmoothBeam))) != HELLA_OK) return fail(s);
 
   // smoothing taps: middle rows, zero padded to a multiple of 16
   std::vector<float> taps;
   std::vector<int> off, n;
-  for (int b = 0; b < c->nbox; ++b) {
-    std::vector<float> m = middle_taps(p->width_min << b);
-    off.push_back((int)taps.size());
-    const int np = ((int)m.size() + 15) / 16 * 16;
-    n.push_back(np);
-    m.resize(np, 0.f);
-    taps.insert(taps.end(), m.begin(), m.end());
-  }
+  hg::smoothing_taps(*p, c->nbox, &taps, &off, &n);
   c->tap_n = n;
   if ((s = dalloc(c, (void **)&c->d_taps, taps.size() * 4)) != HELLA_OK) return fail(s);
   if ((s = dalloc(c, (void **)&c->d_tapoff, off.size() * 4)) != HELLA_OK) return fail(s);
@@ -408,10 +379,14 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
       cudaMemset(c->d_packed, 0, nb * nch * R * 4) != cudaSuccess ||
       cudaMemset(c->d_flagspec, 0, nch * 4) != cudaSuccess ||
       cudaMemset(c->d_err, 0, 16) != cudaSuccess ||
+      cudaMemset(c->d_row_beam, 0, (size_t)c->ndms * 4) != cudaSuccess ||
+      cudaMemcpy(c->d_active, &kOne, 4, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaDeviceSynchronize() != cudaSuccess) {
     cudaGetLastError();
     return fail(HELLA_ERR_CUDA);
   }
+  if ((s = upload_beam(c, p->max_giants, p->beam0)) != HELLA_OK) return fail(s);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(HELLA_ERR_CUDA);
   if (p->autotune && (s = autotune(c, 2, nullptr, nullptr)) != HELLA_OK) return fail(s);
   *out = c;
   return HELLA_OK;
@@ -478,7 +453,7 @@ hella_status hella_dedisperse(hella_ctx *c, int beam) {
 hella_status hella_smooth(hella_ctx *c, int scale) {
   if (!c) return HELLA_ERR_INVALID_ARG;
   if (c->dd_beam < 0) return HELLA_ERR_STATE;
-  hg::SmoothArgs a = smooth_args(c);
+  const hg::SmoothArgs a = smooth_args(c);
   CK(hg::smooth_planes(a, c->stream));
   if (scale) {
     CK(hg::smooth_stats(a, c->stream, 1));
@@ -494,17 +469,10 @@ hella_status hella_find_peaks(hella_ctx *c, int beam) {
   if (!c->smoothed) return HELLA_ERR_STATE;
   const int cap = c->p.max_giants - (int)c->peaks.size();
   if (cap <= 0) return HELLA_OK;
-  hg::SmoothArgs a = smooth_args(c);
-  hg::PeakArgs pk{};
-  pk.sm = &a;
-  pk.counts = c->d_counts;
-  pk.offsets = c->d_offsets;
-  pk.total = c->d_total;
-  pk.cap = cap;
-  pk.beam = beam + c->p.beam0;
-  pk.cand_i = c->d_cand_i;
-  pk.cand_v = c->d_cand_v;
-  CK(hg::find_peaks(pk, c->stream));
+  hella_status st = upload_beam(c, cap, beam + c->p.beam0);
+  if (st != HELLA_OK) return st;
+  CK(cudaMemsetAsync(c->d_total, 0, 4, c->stream));
+  CK(hg::find_peaks(smooth_args(c), c->stream));
   CK(cudaMemcpyAsync(c->h_total, c->d_total, 4, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaMemcpyAsync(c->h_total + 1, c->d_err, 4, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -665,7 +633,7 @@ hella_status hella_get_tuning(const hella_ctx *c, hella_tuning *t) {
 }
 
 hella_status hella_set_tuning(hella_ctx *c, const hella_tuning *t) {
-  if (!c || !t || !tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
+  if (!c || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
   c->tune = *t;
   c->tune.samples_per_thread = 4;
   return HELLA_OK;

@@ -52,29 +52,41 @@ __device__ __forceinline__ float normv(float x, const float *st) {
   return st[1] > 0.f ? __fmul_rn(__fadd_rn(x, st[2]), st[3]) : x;
 }
 
+// Beam and beam-local row of global row `gr` of a launch.
+__device__ __forceinline__ const SmoothBeam &row_beam(const SmoothArgs &a, int gr, int *r) {
+  const SmoothBeam &B = a.beams[a.row_beam[gr]];
+  *r = gr - B.row0;
+  return B;
+}
+
+// One block per (beam, row): widths w0..w0+nw-1 of the row from one staged
+// chunk of y values.  taps of those widths are copied to shared memory.
 __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
   extern __shared__ __align__(16) float sm[];
-  const int nbox = a.nbox, h = a.ndms - 2, tid = threadIdx.x;
-  const int span = 2 * (a.wmin << (nbox - 1));
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  if (!*B.active) return;
+  const int w0 = a.w0, nw = a.nw, h = B.h, tid = threadIdx.x;
+  const int span = 2 * (a.wmin << (w0 + nw - 1));
   const int ylen = kCH + span + 2 * kR;
   const int M = (ylen + kR - 1) / kR;
+  const int tap0 = a.tap_off[w0];
   int ntaps_total = 0;
-  for (int b = 0; b < nbox; ++b) ntaps_total += a.tap_n[b];
+  for (int b = w0; b < w0 + nw; ++b) ntaps_total += a.tap_n[b];
   float *taps = sm;
   float *Y = taps + ((ntaps_total + 3) / 4) * 4;
   float *out_s = Y + kR * M;
   float *part_s = out_s + kCH;
-  float *max_s = part_s + nbox * kT;
-  for (int i = tid; i < ntaps_total; i += kT) taps[i] = a.taps[i];
-  for (int b = 0; b < nbox; ++b) {
-    part_s[b * kT + tid] = 0.f;
-    max_s[b * kT + tid] = -INFINITY;
+  float *max_s = part_s + nw * kT;
+  for (int i = tid; i < ntaps_total; i += kT) taps[i] = a.taps[tap0 + i];
+  for (int j = 0; j < nw; ++j) {
+    part_s[j * kT + tid] = 0.f;
+    max_s[j * kT + tid] = -INFINITY;
   }
-  const int r = blockIdx.x;
-  const float *ra = a.dd + (size_t)r * a.dd_stride;
-  const float *rb = ra + a.dd_stride;
-  const float *rc = rb + a.dd_stride;
-  const int nw = 256 * (a.ntime_out / 256);
+  const float *ra = B.dd + (size_t)r * B.dd_stride;
+  const float *rb = ra + B.dd_stride;
+  const float *rc = rb + B.dd_stride;
+  const int nwcol = 256 * (a.ntime_out / 256);
   const int org = a.wmax / 2 - (a.anchor ? span : 0);
 
   for (int cs = 0; cs < a.ntime_out; cs += kCH) {
@@ -85,10 +97,11 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
       Y[(x % kR) * M + x / kR] = __fmaf_rn(0.3f, __fadd_rn(ra[col], rc[col]), rb[col]);
     }
     __syncthreads();
-    for (int b = 0; b < nbox; ++b) {
+    for (int j = 0; j < nw; ++j) {
+      const int b = w0 + j;
       const int smw = a.wmin << b;
       const int off = a.anchor ? span - 2 * smw : 0;
-      const float *tp = taps + a.tap_off[b];
+      const float *tp = taps + a.tap_off[b] - tap0;
       const int n = a.tap_n[b];
       const int base = kR * tid + off;
       // win[] slides over y; pre[kk] is where the slot refilled at tap kk of
@@ -108,10 +121,10 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
           const float4 c4 = *reinterpret_cast<const float4 *>(tp + kb + k4);
           const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int kk = k4 + j;
+          for (int jj = 0; jj < 4; ++jj) {
+            const int kk = k4 + jj;
 #pragma unroll
-            for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cfs[j], win[(i + kk) % kR], acc[i]);
+            for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cfs[jj], win[(i + kk) % kR], acc[i]);
             win[kk] = Y[pre[kk] + kq];
           }
         }
@@ -120,59 +133,64 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
 #pragma unroll
       for (int i = 0; i < kR / 4; ++i) o4[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
       __syncthreads();
-      float *dst = a.boxes + ((size_t)b * h + r) * a.ntime_out;
-      float ps = part_s[b * kT + tid], mx = max_s[b * kT + tid];
+      float *dst = B.boxes + ((size_t)j * h + r) * a.ntime_out;
+      float ps = part_s[j * kT + tid], mx = max_s[j * kT + tid];
 #pragma unroll
       for (int m = 0; m < kR; ++m) {
-        const int j = tid + kT * m, col = cs + j;
+        const int jc = tid + kT * m, col = cs + jc;
         if (col < a.ntime_out) {
-          const float v = out_s[j];
+          const float v = out_s[jc];
           dst[col] = v;
           mx = fmaxf(mx, v);
-          if (col < nw) ps = __fadd_rn(ps, v);
+          if (col < nwcol) ps = __fadd_rn(ps, v);
         }
       }
-      part_s[b * kT + tid] = ps;
-      max_s[b * kT + tid] = mx;
+      part_s[j * kT + tid] = ps;
+      max_s[j * kT + tid] = mx;
       __syncthreads();
     }
   }
   __syncthreads();
-  for (int b = tid >> 5; b < nbox; b += kT / 32) {
-    const float tot = block256_tree(part_s + b * kT);
+  for (int j = tid >> 5; j < nw; j += kT / 32) {
+    const float tot = block256_tree(part_s + j * kT);
     float mx = -INFINITY;
-    for (int i = threadIdx.x & 31; i < kT; i += 32) mx = fmaxf(mx, max_s[b * kT + i]);
+    for (int i = threadIdx.x & 31; i < kT; i += 32) mx = fmaxf(mx, max_s[j * kT + i]);
     for (int off = 16; off > 0; off /= 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     if ((tid & 31) == 0) {
-      a.rowmean[(size_t)b * h + r] = __fdiv_rn(tot, (float)nw);
-      a.rowmax[(size_t)b * h + r] = mx;
+      B.rowmean[(size_t)(w0 + j) * h + r] = __fdiv_rn(tot, (float)nwcol);
+      B.rowmax[(size_t)(w0 + j) * h + r] = mx;
     }
   }
 }
 
 // Host loop of calculate_stddev (normalization.cu:138-142): sequential over
-// rows, / height.  One thread per width.
+// rows, / height.  Block = beam, thread = width of the launch.
 __global__ void k_mean_finish(SmoothArgs a) {
-  const int b = threadIdx.x;
-  if (b >= a.nbox) return;
-  const int h = a.ndms - 2;
+  const SmoothBeam &B = a.beams[blockIdx.x];
+  const int j = threadIdx.x;
+  if (j >= a.nw || !*B.active) return;
+  const int b = a.w0 + j, h = B.h;
   float s = 0.f;
-  for (int r = 0; r < h; ++r) s = __fadd_rn(s, a.rowmean[(size_t)b * h + r]);
-  a.stats[b * 4 + 0] = __fdiv_rn(s, (float)h);
+  for (int r = 0; r < h; ++r) s = __fadd_rn(s, B.rowmean[(size_t)b * h + r]);
+  B.stats[b * 4 + 0] = __fdiv_rn(s, (float)h);
 }
 
 // computeRowVariances over one row of one width plane.  NORM0: the
-// normalised width-0 plane (find_peaks' sigma, peaks.cu:171-178).
+// normalised width-0 plane (find_peaks' sigma, peaks.cu:171-178), which
+// needs width 0 in the launch (w0 == 0).
 template <bool NORM0, bool VAR>
 __global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
   __shared__ float p_s[kT];
-  const int r = blockIdx.x, b = NORM0 ? 0 : blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
-  const float *x = a.boxes + ((size_t)b * h + r) * a.ntime_out;
-  const int nw = 256 * (a.ntime_out / 256);
-  const float *st = a.stats + b * 4;
-  const float mean = NORM0 ? a.gate[0] : st[0];
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  if (!*B.active) return;
+  const int j = NORM0 ? 0 : blockIdx.y, b = a.w0 + j, h = B.h, tid = threadIdx.x;
+  const float *x = B.boxes + ((size_t)j * h + r) * a.ntime_out;
+  const int nwcol = 256 * (a.ntime_out / 256);
+  const float *st = B.stats + b * 4;
+  const float mean = NORM0 ? B.gate[0] : st[0];
   float s = 0.f;
-  for (int col = tid; col < nw; col += kT) {
+  for (int col = tid; col < nwcol; col += kT) {
     float v = NORM0 ? normv(x[col], st) : x[col];
     if (VAR) {
       const float d = __fsub_rn(v, mean);
@@ -185,49 +203,60 @@ __global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
   __syncthreads();
   if (tid < 32) {
     const float tot = block256_tree(p_s);
-    if (tid == 0) a.rowvar[(size_t)b * h + r] = __fdiv_rn(tot, (float)nw);
+    if (tid == 0) B.rowvar[(size_t)b * h + r] = __fdiv_rn(tot, (float)nwcol);
   }
 }
 
-// Per width: variance -> std and the normalisation constants.  NORM0: the
-// gate statistics of the normalised width-0 plane.
+// Per (beam, width): variance -> std and the normalisation constants.
+// NORM0: the gate statistics of the normalised width-0 plane.
 template <bool NORM0, bool VAR>
 __global__ void k_stat_finish(SmoothArgs a) {
-  const int b = threadIdx.x;
-  if (b >= (NORM0 ? 1 : a.nbox)) return;
-  const int h = a.ndms - 2;
+  const SmoothBeam &B = a.beams[blockIdx.x];
+  const int j = threadIdx.x;
+  if (j >= (NORM0 ? 1 : a.nw) || !*B.active) return;
+  const int b = NORM0 ? 0 : a.w0 + j, h = B.h;
   float s = 0.f;
-  for (int r = 0; r < h; ++r) s = __fadd_rn(s, a.rowvar[(size_t)b * h + r]);
+  for (int r = 0; r < h; ++r) s = __fadd_rn(s, B.rowvar[(size_t)b * h + r]);
   s = __fdiv_rn(s, (float)h);
   if (NORM0) {
     if (!VAR) {
-      a.gate[0] = s;
+      B.gate[0] = s;
     } else {
       const float sig = __fsqrt_rn(s);
-      a.gate[1] = sig;
-      a.gate[2] = __fmul_rn(a.snr, sig);
-      a.gate[3] = (sig < 5 && (double)sig > 0.1) ? 1.f : 0.f;  // definitions.h:71-72
+      B.gate[1] = sig;
+      B.gate[2] = __fmul_rn(a.snr, sig);
+      B.gate[3] = (sig < 5 && (double)sig > 0.1) ? 1.f : 0.f;  // definitions.h:71-72
     }
   } else {
-    const float sd = __fsqrt_rn(s), mean = a.stats[b * 4 + 0];
-    a.stats[b * 4 + 1] = sd;
-    a.stats[b * 4 + 2] = -1.0f * mean;
-    a.stats[b * 4 + 3] = __fdiv_rn(1.0f, sd);
+    const float sd = __fsqrt_rn(s), mean = B.stats[b * 4 + 0];
+    B.stats[b * 4 + 1] = sd;
+    B.stats[b * 4 + 2] = -1.0f * mean;
+    B.stats[b * 4 + 3] = __fdiv_rn(1.0f, sd);
   }
 }
 
-__global__ void __launch_bounds__(kT) k_count(PeakArgs p, SmoothArgs a) {
+// Unnormalised planes (hella_smooth(ctx, 0)): stats zero for the widths.
+__global__ void k_stat_zero(SmoothArgs a) {
+  const SmoothBeam &B = a.beams[blockIdx.x];
+  const int j = threadIdx.x;
+  if (j >= a.nw || !*B.active) return;
+  for (int q = 0; q < 4; ++q) B.stats[(a.w0 + j) * 4 + q] = 0.f;
+}
+
+__global__ void __launch_bounds__(kT) k_count(SmoothArgs a) {
   __shared__ int c_s[kT / 32];
-  const int r = blockIdx.x, b = blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  const int j = blockIdx.y, b = a.w0 + j, h = B.h, tid = threadIdx.x;
   const size_t row = (size_t)b * h + r;
-  const float *st = a.stats + b * 4;
-  const float thr = a.gate[2];
+  const float *st = B.stats + b * 4;
+  const float thr = B.gate[2];
   // normalisation is monotonic, so the row maximum decides the whole row
-  if (a.gate[3] == 0.f || !(normv(a.rowmax[row], st) > thr)) {
-    if (tid == 0) p.counts[row] = 0;
+  if (!*B.active || B.gate[3] == 0.f || !(normv(B.rowmax[row], st) > thr)) {
+    if (tid == 0) B.counts[row] = 0;
     return;
   }
-  const float *x = a.boxes + row * a.ntime_out;
+  const float *x = B.boxes + ((size_t)j * h + r) * a.ntime_out;
   int n = 0;
   for (int col = tid; col < a.ntime_out; col += kT) n += normv(x[col], st) > thr;
   for (int off = 16; off > 0; off /= 2) n += __shfl_xor_sync(0xffffffffu, n, off);
@@ -236,18 +265,25 @@ __global__ void __launch_bounds__(kT) k_count(PeakArgs p, SmoothArgs a) {
   if (tid == 0) {
     int t = 0;
     for (int i = 0; i < kT / 32; ++i) t += c_s[i];
-    p.counts[row] = t;
+    B.counts[row] = t;
   }
 }
 
-// Exclusive scan of the row counts in (width, row) order; total capped.
-__global__ void __launch_bounds__(1024) k_scan(PeakArgs p, int nrows) {
+// Per beam: exclusive scan of the row counts of the launch's widths in
+// (width, row) order, after the candidates of earlier widths; the beam's
+// total is capped at its cap.
+__global__ void __launch_bounds__(1024) k_scan(SmoothArgs a) {
   __shared__ int s_s[1024];
+  const SmoothBeam &B = a.beams[blockIdx.x];
+  if (!*B.active) return;
   const int tid = threadIdx.x;
+  const int nrows = a.nw * B.h;
+  int *counts = B.counts + (size_t)a.w0 * B.h, *offsets = B.offsets + (size_t)a.w0 * B.h;
+  const int base = B.total[0];
   const int per = (nrows + 1023) / 1024;
   const int lo = min(nrows, tid * per), hi = min(nrows, lo + per);
   int sum = 0;
-  for (int i = lo; i < hi; ++i) sum += p.counts[i];
+  for (int i = lo; i < hi; ++i) sum += counts[i];
   s_s[tid] = sum;
   __syncthreads();
   for (int off = 1; off < 1024; off *= 2) {
@@ -256,26 +292,29 @@ __global__ void __launch_bounds__(1024) k_scan(PeakArgs p, int nrows) {
     s_s[tid] += v;
     __syncthreads();
   }
-  int run = s_s[tid] - sum;
+  int run = base + s_s[tid] - sum;
   for (int i = lo; i < hi; ++i) {
-    p.offsets[i] = run;
-    run += p.counts[i];
+    offsets[i] = run;
+    run += counts[i];
   }
-  if (tid == 1023) p.total[0] = min(s_s[1023], p.cap);
+  __syncthreads();
+  if (tid == 1023) B.total[0] = min(base + s_s[1023], B.cap);
 }
 
 // Ordered compaction of one row's candidates.
-__global__ void __launch_bounds__(kT) k_write(PeakArgs p, SmoothArgs a) {
+__global__ void __launch_bounds__(kT) k_write(SmoothArgs a) {
   __shared__ int w_s[kT / 32];
   __shared__ int base_s;
-  const int r = blockIdx.x, b = blockIdx.y, h = a.ndms - 2, tid = threadIdx.x;
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  const int j = blockIdx.y, b = a.w0 + j, h = B.h, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const size_t row = (size_t)b * h + r;
-  if (p.counts[row] == 0 || p.offsets[row] >= p.cap) return;
-  const float *st = a.stats + b * 4;
-  const float thr = a.gate[2];
-  const float *x = a.boxes + row * a.ntime_out;
-  if (tid == 0) base_s = p.offsets[row];
+  if (!*B.active || B.counts[row] == 0 || B.offsets[row] >= B.cap) return;
+  const float *st = B.stats + b * 4;
+  const float thr = B.gate[2];
+  const float *x = B.boxes + ((size_t)j * h + r) * a.ntime_out;
+  if (tid == 0) base_s = B.offsets[row];
   for (int cs = 0; cs < a.ntime_out; cs += kT) {
     const int col = cs + tid;
     float v = 0.f;
@@ -291,9 +330,9 @@ __global__ void __launch_bounds__(kT) k_write(PeakArgs p, SmoothArgs a) {
     int before = base_s;
     for (int i = 0; i < warp; ++i) before += w_s[i];
     before += __popc(bal & ((1u << lane) - 1u));
-    if (hit && before < p.cap) {
-      p.cand_i[before] = make_int4(p.beam, r + 1, b, col);
-      p.cand_v[before] = v;
+    if (hit && before < B.cap) {
+      B.cand_i[before] = make_int4(B.beam_id, r + 1, b, col);
+      B.cand_v[before] = v;
     }
     __syncthreads();
     if (tid == 0) {
@@ -304,59 +343,65 @@ __global__ void __launch_bounds__(kT) k_write(PeakArgs p, SmoothArgs a) {
   }
 }
 
+// Normalised copy of beam 0's planes of the launch's widths (inspection).
 __global__ void k_normalise_copy(SmoothArgs a, float *dst) {
-  const size_t plane = (size_t)(a.ndms - 2) * a.ntime_out;
-  const size_t n = plane * a.nbox;
+  const SmoothBeam &B = a.beams[0];
+  const size_t plane = (size_t)B.h * a.ntime_out;
+  const size_t n = plane * a.nw;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = normv(a.boxes[i], a.stats + (i / plane) * 4);
+    dst[i] = normv(B.boxes[i], B.stats + (a.w0 + i / plane) * 4);
 }
 
 }  // namespace
 
-size_t fir_smem_bytes(const SmoothArgs &a, int ntaps_total) {
-  const int span = 2 * (a.wmin << (a.nbox - 1));
+size_t fir_smem_bytes(const SmoothArgs &a) {
+  int ntot = 0;
+  for (int b = a.w0; b < a.w0 + a.nw; ++b) ntot += ((2 * (a.wmin << b) + 1 + kR - 1) / kR) * kR;
+  const int span = 2 * (a.wmin << (a.w0 + a.nw - 1));
   const int ylen = kCH + span + 2 * kR;
   const int M = (ylen + kR - 1) / kR;
-  return sizeof(float) * ((size_t)(ntaps_total + 3) / 4 * 4 + (size_t)kR * M + kCH +
-                          (size_t)2 * a.nbox * kT);
+  return sizeof(float) * ((size_t)(ntot + 3) / 4 * 4 + (size_t)kR * M + kCH + (size_t)2 * a.nw * kT);
 }
 
 cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s) {
-  int ntot = 0;  // the kernel re-derives this total from tap_n
-  for (int b = 0; b < a.nbox; ++b) ntot += ((2 * (a.wmin << b) + 1 + kR - 1) / kR) * kR;
-  const size_t smem = fir_smem_bytes(a, ntot);
+  if (a.nrows <= 0 || a.nw <= 0) return cudaSuccess;
+  const size_t smem = fir_smem_bytes(a);
   cudaError_t e = cudaFuncSetAttribute(k_fir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_fir<<<a.ndms - 2, kT, smem, s>>>(a);
+  k_fir<<<a.nrows, kT, smem, s>>>(a);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale) {
-  const int h = a.ndms - 2;
+  if (a.nrows <= 0 || a.nw <= 0) return cudaSuccess;
+  unsigned n = 0;
   if (scale) {
-    k_mean_finish<<<1, 32, 0, s>>>(a);
-    k_row_stat<false, true><<<dim3(h, a.nbox), kT, 0, s>>>(a);
-    k_stat_finish<false, true><<<1, 32, 0, s>>>(a);
+    k_mean_finish<<<a.nbeam, 32, 0, s>>>(a);
+    k_row_stat<false, true><<<dim3(a.nrows, a.nw), kT, 0, s>>>(a);
+    k_stat_finish<false, true><<<a.nbeam, 32, 0, s>>>(a);
+    n += 3;
   } else {
-    cudaError_t e = cudaMemsetAsync(a.stats, 0, sizeof(float) * 4 * a.nbox, s);
-    if (e != cudaSuccess) return e;
+    k_stat_zero<<<a.nbeam, 32, 0, s>>>(a);
+    n += 1;
   }
-  k_row_stat<true, false><<<dim3(h, 1), kT, 0, s>>>(a);
-  k_stat_finish<true, false><<<1, 32, 0, s>>>(a);
-  k_row_stat<true, true><<<dim3(h, 1), kT, 0, s>>>(a);
-  k_stat_finish<true, true><<<1, 32, 0, s>>>(a);
-  count_launches(scale ? 7 : 4);
+  if (a.w0 == 0) {  // the gate statistics of the normalised width-0 plane
+    k_row_stat<true, false><<<dim3(a.nrows, 1), kT, 0, s>>>(a);
+    k_stat_finish<true, false><<<a.nbeam, 32, 0, s>>>(a);
+    k_row_stat<true, true><<<dim3(a.nrows, 1), kT, 0, s>>>(a);
+    k_stat_finish<true, true><<<a.nbeam, 32, 0, s>>>(a);
+    n += 4;
+  }
+  count_launches(n);
   return cudaGetLastError();
 }
 
-cudaError_t find_peaks(const PeakArgs &p, cudaStream_t s) {
-  const SmoothArgs &a = *p.sm;
-  const int h = a.ndms - 2;
-  k_count<<<dim3(h, a.nbox), kT, 0, s>>>(p, a);
-  k_scan<<<1, 1024, 0, s>>>(p, h * a.nbox);
-  k_write<<<dim3(h, a.nbox), kT, 0, s>>>(p, a);
+cudaError_t find_peaks(const SmoothArgs &a, cudaStream_t s) {
+  if (a.nrows <= 0 || a.nw <= 0) return cudaSuccess;
+  k_count<<<dim3(a.nrows, a.nw), kT, 0, s>>>(a);
+  k_scan<<<a.nbeam, 1024, 0, s>>>(a);
+  k_write<<<dim3(a.nrows, a.nw), kT, 0, s>>>(a);
   count_launches(3);
   return cudaGetLastError();
 }

@@ -52,6 +52,11 @@ class HellaParams(C.Structure):
     ]
 
 
+class BatchParams(C.Structure):
+    _fields_ = [("base", HellaParams), ("dm_max", C.c_void_p), ("killmask", C.c_void_p),
+                ("widths_per_pass", C.c_int), ("use_graph", C.c_int)]
+
+
 class HellaTuning(C.Structure):
     _fields_ = [("dm_per_block", C.c_int), ("samples_per_thread", C.c_int), ("chan_chunk", C.c_int),
                 ("stages", C.c_int), ("group", C.c_int), ("add_mode", C.c_int)]
@@ -140,6 +145,18 @@ def lib() -> C.CDLL:
     _sig(L, "hella_get_flag_stats", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP])
     _sig(L, "hella_get_flag_spec", C.c_int, [_VP, _VP])
     _sig(L, "hella_status_string", C.c_char_p, [C.c_int])
+    _sig(L, "hella_batch_params_default", None, [C.POINTER(BatchParams)])
+    _sig(L, "hella_batch_create", C.c_int, [C.POINTER(_VP), C.POINTER(BatchParams)])
+    _sig(L, "hella_batch_destroy", None, [_VP])
+    _sig(L, "hella_batch_set_stream", C.c_int, [_VP, _VP])
+    _sig(L, "hella_batch_get_info", C.c_int, [_VP, C.c_int, C.POINTER(HellaInfo)])
+    _sig(L, "hella_batch_process_gulp", C.c_int, [_VP, _VP, C.c_int, _VP, C.c_int, C.POINTER(C.c_int), _VP, _VP])
+    _sig(L, "hella_batch_copy_dedisp", C.c_int, [_VP, C.c_int, _VP])
+    _sig(L, "hella_batch_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
+    _sig(L, "hella_batch_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
+    _sig(L, "hella_batch_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
+    _sig(L, "hella_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(HellaTuning), C.POINTER(C.c_float)])
+    _sig(L, "hella_batch_last_gulp_ms", C.c_int, [_VP, C.POINTER(C.c_float)])
     _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
@@ -404,3 +421,83 @@ class Search:
         out = np.zeros(self.params.nchan, np.float32)
         _chk(self.L.hella_get_flag_spec(self.h, out.ctypes.data))
         return out
+
+
+# ----------------------------------------------------------- batched search
+
+class Batch:
+    """All beams per launch (hella_batch_create ... hella_batch_destroy).
+    dm_max: per-beam DM ceilings; killmask: [nbeam][nchan] (0 = dropped)."""
+
+    def __init__(self, base: HellaParams, dm_max=None, killmask=None, widths_per_pass: int = 0,
+                 use_graph: bool = True):
+        self.L = lib()
+        bp = BatchParams()
+        self.L.hella_batch_params_default(C.byref(bp))
+        bp.base = base
+        self._dm = None if dm_max is None else np.ascontiguousarray(dm_max, dtype=np.float32)
+        self._km = None if killmask is None else np.ascontiguousarray(killmask, dtype=np.int32)
+        bp.dm_max = None if self._dm is None else self._dm.ctypes.data
+        bp.killmask = None if self._km is None else self._km.ctypes.data
+        bp.widths_per_pass = widths_per_pass
+        bp.use_graph = int(use_graph)
+        h = _VP()
+        _chk(self.L.hella_batch_create(C.byref(h), C.byref(bp)))
+        self.h = h
+        self.base = base
+        self.nbeam = base.nbeam
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def info(self, beam: int) -> HellaInfo:
+        i = HellaInfo()
+        _chk(self.L.hella_batch_get_info(self.h, beam, C.byref(i)))
+        return i
+
+    def set_stream(self, stream: int):
+        _chk(self.L.hella_batch_set_stream(self.h, stream))
+
+    def process_gulp(self, gulp, on_device=False):
+        """Returns (candidates, counts[nbeam], searched[nbeam])."""
+        cap = self.base.max_giants * self.nbeam
+        out = np.zeros(cap, CAND_DTYPE)
+        counts = np.zeros(self.nbeam, np.int32)
+        searched = np.zeros(self.nbeam, np.int32)
+        n = C.c_int()
+        _chk(self.L.hella_batch_process_gulp(self.h, _ptr(gulp), int(on_device), out.ctypes.data, cap,
+                                             C.byref(n), counts.ctypes.data, searched.ctypes.data))
+        return out[: n.value], counts, searched.astype(bool)
+
+    def copy_dedisp(self, beam: int) -> np.ndarray:
+        i = self.info(beam)
+        out = np.empty((i.ndms, i.ntime_dd), np.float32)
+        _chk(self.L.hella_batch_copy_dedisp(self.h, beam, out.ctypes.data))
+        return out
+
+    def get_tuning(self) -> HellaTuning:
+        t = HellaTuning()
+        _chk(self.L.hella_batch_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, t: HellaTuning):
+        _chk(self.L.hella_batch_set_tuning(self.h, C.byref(t)))
+
+    def time_dedisp(self, t: HellaTuning | None = None, reps: int = 3) -> float:
+        ms = C.c_float()
+        _chk(self.L.hella_batch_time_dedisp(self.h, None if t is None else C.byref(t), reps, C.byref(ms)))
+        return ms.value
+
+    def autotune(self, reps: int = 2):
+        t, ms = HellaTuning(), C.c_float()
+        _chk(self.L.hella_batch_autotune(self.h, reps, C.byref(t), C.byref(ms)))
+        return t, ms.value
+
+    def last_gulp_ms(self) -> float:
+        ms = C.c_float()
+        _chk(self.L.hella_batch_last_gulp_ms(self.h, C.byref(ms)))
+        return ms.value

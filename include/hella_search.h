@@ -181,6 +181,53 @@ hella_status hella_get_flag_stats(hella_ctx *ctx, int beam, float *bp1,
 /* Accumulated per-channel flag fractions (d_flagSpec, flagger.cu:334). */
 hella_status hella_get_flag_spec(hella_ctx *ctx, float *out);
 
+/* ---- Batched multi-beam search (no counterpart in the reference, whose
+ * gulp loop runs the stages beam after beam).  Every stage runs for all
+ * beams in one launch per pass; the per-gulp launches are captured once in a
+ * CUDA graph and replayed.  Beam b has its own DM ceiling and killmask, and
+ * its candidates are those of a single-beam context created with
+ * dm_max = dm_max[b] and that killmask, fed the same gulps. */
+typedef struct hella_batch hella_batch;
+
+typedef struct {
+  hella_params base;     /* base.nbeam beams; base.dm_max is ignored when
+                            dm_max is given; base.max_giants caps each beam */
+  const float *dm_max;   /* [nbeam] DM ceiling of each beam, or NULL */
+  const int *killmask;   /* [nbeam][nchan], 0 = channel dropped, or NULL */
+  int widths_per_pass;   /* smoothing widths held in HBM at once; 0: as
+                            many as base.hbm_budget (or free memory) allows */
+  int use_graph;         /* 1: capture the per-gulp launches in a CUDA graph */
+} hella_batch_params;
+
+void hella_batch_params_default(hella_batch_params *p);
+hella_status hella_batch_create(hella_batch **b, const hella_batch_params *p);
+void hella_batch_destroy(hella_batch *b);
+/* Stream of the batch's device work (a cudaStream_t other than the legacy
+ * default stream, which cannot be captured; NULL: the batch's own stream). */
+hella_status hella_batch_set_stream(hella_batch *b, void *stream);
+/* Sizes of beam `beam` (as hella_get_info of its single-beam context). */
+hella_status hella_batch_get_info(const hella_batch *b, int beam, hella_info *info);
+/* One gulp u8 [nbeam][gulp][nchan] of every beam: flag, dedisperse, smooth
+ * and find peaks for all beams.  out receives min(total, max) candidates,
+ * beam by beam, each beam's in the single-beam order; counts[b] (may be
+ * NULL) the number of beam b, searched[b] (may be NULL) whether beam b was
+ * searched.  *n = candidates written to out. */
+hella_status hella_batch_process_gulp(hella_batch *b, const uint8_t *gulp, int on_device,
+                                      hella_cand *out, int max, int *n, int *counts,
+                                      int *searched);
+/* Inspection: beam's last dedispersed plane, fp32 [ndms_b][ntime_dd]. */
+hella_status hella_batch_copy_dedisp(hella_batch *b, int beam, float *out);
+hella_status hella_batch_get_tuning(const hella_batch *b, hella_tuning *t);
+hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t);
+/* Times the all-beam dedispersion launch with shape t (NULL: current). */
+hella_status hella_batch_time_dedisp(hella_batch *b, const hella_tuning *t, int reps,
+                                     float *ms);
+hella_status hella_batch_autotune(hella_batch *b, int reps, hella_tuning *best,
+                                  float *best_ms);
+/* Per-gulp device time of the last processed gulp's stages, ms:
+ * [0] whole gulp (graph), recorded with CUDA events. */
+hella_status hella_batch_last_gulp_ms(const hella_batch *b, float *ms);
+
 const char *hella_status_string(hella_status s);
 
 /* Device self-check of the fp16 arithmetic the flagger relies on (no

@@ -111,6 +111,7 @@ struct hella_batch {
   int items_dpt = -1;  // DM tile of the work-item prefix held in d_dbeams
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
   bool use_graph = true;
+  cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_stale = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -238,9 +239,10 @@ hella_status build_graph(hella_batch *b, const hg::DedispArgs &da) {
     return s != HELLA_OK ? s : HELLA_ERR_CUDA;
   }
   if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
   b->exec = nullptr;
+  b->graph = g;
   const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
-  cudaGraphDestroy(g);
   if (ie != cudaSuccess) {
     cudaGetLastError();
     b->exec = nullptr;
@@ -297,6 +299,7 @@ void hella_batch_destroy(hella_batch *b) {
   cudaSetDevice(b->p.device);
   cudaStreamSynchronize(b->stream);
   if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   for (void *ptr : b->dallocs) cudaFree(ptr);
@@ -612,6 +615,22 @@ hella_status hella_batch_autotune(hella_batch *b, int reps, hella_tuning *best, 
   if (!b || reps < 1) return HELLA_ERR_INVALID_ARG;
   CK(cudaSetDevice(b->p.device));
   return autotune(b, reps, best, best_ms);
+}
+
+hella_status hella_batch_graph_kernels(const hella_batch *b, int *kernels) {
+  if (!b || !kernels) return HELLA_ERR_INVALID_ARG;
+  *kernels = 0;
+  if (!b->graph) return HELLA_ERR_STATE;
+  size_t n = 0;
+  CK(cudaGraphGetNodes(b->graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  CK(cudaGraphGetNodes(b->graph, nodes.data(), &n));
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    CK(cudaGraphNodeGetType(nd, &t));
+    *kernels += t == cudaGraphNodeTypeKernel;
+  }
+  return HELLA_OK;
 }
 
 hella_status hella_batch_last_gulp_ms(const hella_batch *b, float *ms) {

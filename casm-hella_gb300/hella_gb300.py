@@ -157,6 +157,7 @@ def lib() -> C.CDLL:
     _sig(L, "hella_batch_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
     _sig(L, "hella_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(HellaTuning), C.POINTER(C.c_float)])
     _sig(L, "hella_batch_last_gulp_ms", C.c_int, [_VP, C.POINTER(C.c_float)])
+    _sig(L, "hella_batch_graph_kernels", C.c_int, [_VP, C.POINTER(C.c_int)])
     _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
@@ -496,6 +497,11 @@ class Batch:
         t, ms = HellaTuning(), C.c_float()
         _chk(self.L.hella_batch_autotune(self.h, reps, C.byref(t), C.byref(ms)))
         return t, ms.value
+
+    def graph_kernels(self) -> int:
+        n = C.c_int()
+        _chk(self.L.hella_batch_graph_kernels(self.h, C.byref(n)))
+        return n.value
 
     def last_gulp_ms(self) -> float:
         ms = C.c_float()

@@ -96,6 +96,52 @@ class Sky:
         return x.astype(np.uint8)
 
 
+def gulp_device(sky: Sky, g: int, n: int, out=None):
+    """Samples [g*n, (g+1)*n) of `sky` as a u8 [n][nchan] CUDA tensor (into
+    `out` if given): the model of Sky.gulp drawn on the GPU with torch's
+    generator, for workloads too large to draw on the host.  Same
+    distribution, different random stream from Sky.gulp."""
+    import torch
+
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed((sky.seed * 1000003 + g) & 0x7FFFFFFFFFFFFFFF)
+    x = torch.randn((n, sky.nchan), generator=gen, device="cuda", dtype=torch.float32)
+    sd = torch.full((sky.nchan,), sky.sd, device="cuda")
+    if len(sky.rfi_chans):
+        sd[list(sky.rfi_chans)] = sky.rfi_sd
+    c = torch.arange(sky.nchan, device="cuda", dtype=torch.float32)
+    gain = 1.0 + sky.slope * (c / max(1, sky.nchan - 1) - 0.5)
+    x.mul_(sd).add_(sky.mean * gain)
+    a0 = g * n
+    for sp in sky.spikes:
+        lo, hi = max(sp.t0, a0), min(sp.t0 + sp.width, a0 + n)
+        if lo < hi:
+            x[lo - a0:hi - a0] += sp.amp
+    f = sky.freqs()
+    for b in sky.bursts:
+        dl = sky.delays(b.dm)
+        sig = max(1.0, b.fwhm_ms / 2.3548 / (sky.tsamp * 1000.0))
+        hw = int(math.ceil(4.0 * sig))
+        centers = b.t0 + dl
+        sel = np.nonzero((centers + hw >= a0) & (centers - hw < a0 + n))[0]
+        if sel.size == 0:
+            continue
+        spec = b.amp * (f[sel] / sky.f0) ** b.index
+        offs = np.arange(-hw, hw + 1)
+        prof = np.exp(-0.5 * (offs / sig) ** 2)
+        tt = centers[sel][:, None] + offs[None, :] - a0
+        ok = (tt >= 0) & (tt < n)
+        cc = np.broadcast_to(sel[:, None], tt.shape)
+        vals = (spec[:, None] * prof[None, :])[ok].astype(np.float32)
+        x.index_put_((torch.from_numpy(tt[ok]).cuda(), torch.from_numpy(np.ascontiguousarray(cc[ok])).cuda()),
+                     torch.from_numpy(vals).cuda(), accumulate=True)
+    x.round_().clamp_(0, 255)
+    if out is None:
+        return x.to(torch.uint8)
+    out.copy_(x)
+    return out
+
+
 def snr_amp(snr: float, sd: float, nchan: int, fwhm_ms: float, tsamp: float) -> float:
     """Per-channel amplitude of a flat-spectrum Gaussian with band-integrated
     matched-filter S/N `snr` in noise of `sd` counts."""
@@ -175,3 +221,30 @@ def config_full(seed: int = 2, nchan: int = 2048, gulp: int = 65536, dm_max: flo
 def multibeam_gulp(skies, g: int, n: int) -> np.ndarray:
     """u8 [nbeam][n][nchan] for gulp g of every beam's sky."""
     return np.stack([s.gulp(g, n) for s in skies])
+
+
+def config_batched(nbeam: int = 256, seed: int = 3, nchan: int = 1024, gulp: int = 32768):
+    """Batched multi-beam: nbeam beams of 1024 ch over 375-468.75 MHz, tsamp
+    1.048576 ms, gulp 32768; per-beam killmasks flagging 0-10% of channels,
+    DM ceilings uniform in 1000-2000, 0-3 bursts per beam as in the plain
+    configuration (FWHM 2 ms, S/N 20, flat spectrum, DM below the ceiling);
+    widths 1..32, 7 sigma.  Returns (params, ceilings, killmask, skies)."""
+    rng = np.random.default_rng(seed)
+    tsamp = 1.048576e-3
+    df = -(F0 - FLO) / nchan
+    ceilings = rng.uniform(1000.0, 2000.0, nbeam).astype(np.float32)
+    frac = rng.uniform(0.0, 0.10, nbeam)
+    kill = (rng.random((nbeam, nchan)) >= frac[:, None]).astype(np.int32)
+    skies = []
+    for b in range(nbeam):
+        rfi = tuple(int(c) for c in rng.choice(nchan, 4, replace=False))
+        sky = Sky(nchan, tsamp, F0, df, seed * 100000 + b, 128.0, 20.0, rfi, 80.0, 0.0, [], [])
+        for _ in range(int(rng.integers(0, 4))):
+            dm = float(rng.uniform(50.0, float(ceilings[b]) * 0.9))
+            sky.bursts.append(Burst(place(rng, sky, gulp, float(ceilings[b]), 64, dm, 2.0), dm, 2.0,
+                                    snr_amp(20.0, 20.0, nchan, 2.0, tsamp), 0.0))
+        skies.append(sky)
+    params = dict(nchan=nchan, nbeam=nbeam, gulp=gulp, tsamp=tsamp, plan_dt=tsamp, f0_mhz=F0, df_mhz=df,
+                  dm_min=0.0, dm_max=float(ceilings.max()), dm_tol=1.25, ti_us=40.0, width_min=1, width_max=64,
+                  snr=7.0)
+    return params, ceilings, kill, skies

@@ -224,6 +224,9 @@ hella_status hella_batch_time_dedisp(hella_batch *b, const hella_tuning *t, int 
                                      float *ms);
 hella_status hella_batch_autotune(hella_batch *b, int reps, hella_tuning *best,
                                   float *best_ms);
+/* Kernel launches in the captured per-gulp graph (HELLA_ERR_STATE before
+ * the first graph gulp). */
+hella_status hella_batch_graph_kernels(const hella_batch *b, int *kernels);
 /* Per-gulp device time of the last processed gulp's stages, ms:
  * [0] whole gulp (graph), recorded with CUDA events. */
 hella_status hella_batch_last_gulp_ms(const hella_batch *b, float *ms);

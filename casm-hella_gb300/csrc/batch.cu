@@ -1,4 +1,5 @@
-// batch.cu -- the batched multi-beam search (hella_batch_*, include/hella_search.h).
+// batch.cu -- the batched multi-beam search and its streaming form
+// (hella_batch_*, include/hella_search.h).
 //
 // What casm-hella's gulp loop does beam after beam
 // (src/apps/casm_hella_refactored.cu:701-797: fast_flagger for all beams,
@@ -17,6 +18,13 @@
 // trial up to the ceiling), so one set of dedispersion tables serves every
 // beam, each beam computing its own number of trials.  Killed channels are
 // packed as zeros, which drops them from the exact integer sums.
+//
+// Streaming.  Beams are slots: a dynamic batch sizes every slot for the
+// largest DM list, and slots join and leave between gulps (the layout of
+// rows and work items is rebuilt, the graph recaptured).  Up to two gulps
+// are in flight, each with its own input and candidate buffers ("lanes"):
+// the copy of gulp k+1 to the device runs on a copy stream while gulp k is
+// searched.
 #include "hella_dedisp.h"
 #include "hella_search.h"
 #include "hg_internal.h"
@@ -25,7 +33,9 @@
 #include "hg_tune.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
+#include <deque>
 #include <new>
 #include <vector>
 
@@ -33,15 +43,29 @@ namespace {
 
 // Ring positions and per-beam state of the gulp about to be processed.
 __global__ void k_advance(hg::GulpPos *pos, hg::DedispBeam *db, int *active, int *total,
-                          const int *ntime_b, const int *min_gulp_b, int nbeam, long R, int gulp) {
+                          const int *ntime_b, const int *min_gulp_b, const int *member,
+                          const int *join, int nbeam, long R, int gulp) {
   const long win0 = pos->win0;
   const int gi = pos->gulp_index;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b == 0) pos->wpos = (win0 + R - gulp) % R;
   if (b < nbeam) {
     db[b].win0 = (win0 + R - ntime_b[b]) % R;
-    active[b] = gi >= min_gulp_b[b];  // casm_hella_refactored.cu:705
+    active[b] = member[b] && gi - join[b] >= min_gulp_b[b];  // casm_hella_refactored.cu:705
     total[b] = 0;
+  }
+}
+
+// Running bandpass: ew += alpha * (bp - ew) per channel, the first gulp of a
+// slot taking bp itself.  bp = calc_bandpass_new of the raw gulp.
+__global__ void k_ew_bandpass(const float *bp, float *ew, const int *member, const int *join,
+                              const hg::GulpPos *pos, int nbeam, int nchan, float alpha) {
+  const int gi = pos->gulp_index;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (long)nbeam * nchan;
+       i += (long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / nchan);
+    if (!member[b]) continue;
+    ew[i] = gi == join[b] ? bp[i] : __fadd_rn(ew[i], __fmul_rn(alpha, __fsub_rn(bp[i], ew[i])));
   }
 }
 
@@ -77,44 +101,70 @@ __global__ void k_gather(const hg::SmoothBeam *sb, const int *total, int nbeam, 
   }
 }
 
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// One gulp in flight: its input, candidate buffers, events and graph.
+struct Lane {
+  uint8_t *d_gulp = nullptr;
+  hella_cand *d_out = nullptr;
+  int *h_total = nullptr;
+  cudaEvent_t copied = nullptr, t0 = nullptr, t1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool stale = true, busy = false;
+  double submitted = 0;
+  std::vector<int> searched;
+};
+
+// Sizes of a batch: DM lists per slot and the device bytes they imply.
+struct Sizes {
+  int ndms_all = 0, nbox = 0, ntime_dd = 0, ntime_out = 0;
+  long R = 0;
+  std::vector<int> cap_ndms;  // rows allocated per slot
+  size_t fixed = 0, per_width = 0;
+};
+
 }  // namespace
 
 struct hella_batch {
   hella_params p{};
   int nbeam = 0;
+  bool dynamic = false, use_graph = true;
+  float bp_alpha = 1.f;
   cudaStream_t stream = nullptr;  // graph capture needs a stream other than the legacy one
-  cudaStream_t own_stream = nullptr;
-  hdd_plan plan = nullptr;  // the longest DM list; all channels active
-  int ndms_all = 0, nbox = 0, ntime_dd = 0, ntime_out = 0, nwp = 1, nrows = 0;
-  long R = 0;
-  std::vector<int> ndms, max_delay, ntime, min_gulp;
-  int gulp_index = 0;
+  cudaStream_t own_stream = nullptr, copy_stream = nullptr;
+  hdd_plan plan = nullptr;        // the longest DM list; all channels active
+  Sizes z;
+  int nwp = 1, nrows = 0;
+  std::vector<int> ndms, max_delay, ntime, min_gulp, member, join;
+  std::vector<size_t> dd_off, box_off, row_off;
+  int gulp_index = 0;             // gulps submitted
   size_t dev_bytes = 0;
   std::vector<void *> dallocs, hallocs;
-  uint8_t *d_gulp = nullptr, *d_plain = nullptr, *d_keep = nullptr;
+  uint8_t *d_plain = nullptr, *d_keep = nullptr;
   uint32_t *d_packed = nullptr;
   hg::FlagState fs{};
-  float *d_dd = nullptr, *d_boxes = nullptr, *d_taps = nullptr;
+  float *d_dd = nullptr, *d_boxes = nullptr, *d_taps = nullptr, *d_ew = nullptr;
   int *d_tapoff = nullptr, *d_tapn = nullptr;
   float *d_rowmean = nullptr, *d_rowmax = nullptr, *d_rowvar = nullptr, *d_stats = nullptr,
         *d_gate = nullptr;
   int *d_counts = nullptr, *d_offsets = nullptr, *d_total = nullptr, *d_active = nullptr,
-      *d_row_beam = nullptr, *d_err = nullptr, *d_ntime = nullptr, *d_min_gulp = nullptr;
+      *d_row_beam = nullptr, *d_err = nullptr, *d_ntime = nullptr, *d_min_gulp = nullptr,
+      *d_member = nullptr, *d_join = nullptr;
   int4 *d_cand_i = nullptr;
   float *d_cand_v = nullptr;
-  hella_cand *d_out = nullptr;
   hg::DedispBeam *d_dbeams = nullptr;
   hg::SmoothBeam *d_sbeams = nullptr;
   hg::GulpPos *d_pos = nullptr;
-  int *h_total = nullptr;
   std::vector<hg::DedispBeam> dbeams;
-  int items_dpt = -1;  // DM tile of the work-item prefix held in d_dbeams
+  int items_dpt = -1;             // DM tile of the work-item prefix held in d_dbeams
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
-  bool use_graph = true;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  bool graph_stale = true;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<Lane> lanes;
+  std::deque<int> queue;          // lanes in submission order
+  int next_lane = 0;
   float last_ms = 0.f;
 };
 
@@ -140,22 +190,168 @@ hella_status dalloc(hella_batch *b, void **ptr, size_t bytes) {
   return HELLA_OK;
 }
 
+hella_status halloc(hella_batch *b, void **ptr, size_t bytes) {
+  if (cudaMallocHost(ptr, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return HELLA_ERR_ALLOC;
+  }
+  b->hallocs.push_back(*ptr);
+  return HELLA_OK;
+}
+
+// Number of trials of the DM list up to `ceiling`, which must be a prefix of
+// the plan's list (-1 otherwise).
+int prefix_trials(const hella_params &p, hdd_plan plan, float ceiling) {
+  const std::vector<float> mine =
+      hg::generate_dm_list((float)p.dm_min, ceiling, (float)p.ti_us, (float)p.dm_tol, p.nchan,
+                           (float)p.plan_dt, (float)p.f0_mhz, (float)p.df_mhz);
+  const int n = (int)hdd_get_dm_count(plan);
+  if ((int)mine.size() > n) return -1;
+  const float *all = hdd_get_dm_list(plan);
+  for (size_t k = 0; k < mine.size(); ++k)
+    if (mine[k] != all[k]) return -1;
+  return (int)mine.size();
+}
+
+int ntime_of(const hella_params &p, int max_delay) {
+  return 32 * ((p.gulp + max_delay + p.width_max) / 32 + 1);  // casm_hella_refactored.cu:217-219
+}
+
+// Plan and sizes of a batch (fixed slots: sized for their own ceilings;
+// dynamic slots: for base.dm_max).
+hella_status batch_sizes(const hella_batch_params *bp, hdd_plan *plan_out, Sizes *z) {
+  const hella_params &p = bp->base;
+  const int nb = p.nbeam, nch = p.nchan;
+  float top = p.dm_max;
+  if (bp->dm_max && !bp->dynamic) {
+    top = bp->dm_max[0];
+    for (int i = 0; i < nb; ++i) {
+      if (!(bp->dm_max[i] >= p.dm_min)) return HELLA_ERR_INVALID_ARG;
+      top = std::max(top, bp->dm_max[i]);
+    }
+  }
+  hdd_plan plan = nullptr;
+  if (hdd_create_plan(&plan, nch, (float)p.plan_dt, (float)p.f0_mhz, (float)p.df_mhz) != HDD_NO_ERROR ||
+      hdd_generate_dm_list(plan, p.dm_min, top, p.ti_us, p.dm_tol) != HDD_NO_ERROR) {
+    hdd_destroy_plan(plan);
+    return HELLA_ERR_DEDISP;
+  }
+  z->ndms_all = (int)hdd_get_dm_count(plan);
+  if (z->ndms_all < 3) {
+    hdd_destroy_plan(plan);
+    return HELLA_ERR_INVALID_ARG;
+  }
+  const int *delays = hdd_get_delay_table(plan);
+  z->cap_ndms.assign(nb, z->ndms_all);
+  z->R = 0;
+  for (int i = 0; i < nb; ++i) {
+    if (bp->dm_max && !bp->dynamic) {
+      const int n = prefix_trials(p, plan, bp->dm_max[i]);
+      if (n < 3) {
+        hdd_destroy_plan(plan);
+        return n < 0 ? HELLA_ERR_DEDISP : HELLA_ERR_INVALID_ARG;
+      }
+      z->cap_ndms[i] = n;
+    }
+    z->R = std::max<long>(z->R, ntime_of(p, delays[(size_t)(z->cap_ndms[i] - 1) * nch + nch - 1]));
+  }
+  z->ntime_dd = p.gulp + p.width_max;
+  z->ntime_out = p.gulp;
+  z->nbox = 0;
+  for (int sm = p.width_min; sm < p.width_max; sm *= 2) z->nbox++;
+  size_t dd_floats = 0, rows = 0;
+  for (int i = 0; i < nb; ++i) {
+    dd_floats += (size_t)z->cap_ndms[i] * z->ntime_dd;
+    rows += (size_t)z->cap_ndms[i] - 2;
+  }
+  const size_t R = z->R, cap = p.max_giants;
+  const size_t lanes = bp->inflight == 2 ? 2 : 1;
+  z->fixed = lanes * (size_t)nb * p.gulp * nch + (size_t)nb * nch * R * 5 + (size_t)nb * nch * 5 +
+             (size_t)nb * nch * (256 * 6 + 16) + (size_t)nb * p.gulp * 6 + dd_floats * 4 + rows * z->nbox * 20 +
+             (size_t)nb * cap * 20 + lanes * (size_t)nb * cap * sizeof(hella_cand) + (size_t)nb * 512;
+  z->per_width = rows * z->ntime_out * 4;
+  *plan_out = plan;
+  return HELLA_OK;
+}
+
+// Rows, smoothing table and dedispersion beams of the member slots, to the
+// device; the next gulp recaptures its graph.
+hella_status upload_layout(hella_batch *b) {
+  const int nb = b->nbeam;
+  const size_t cap = b->p.max_giants;
+  std::vector<int> row_beam;
+  std::vector<hg::SmoothBeam> sb(nb);
+  b->nrows = 0;
+  for (int i = 0; i < nb; ++i) {
+    const int h = b->member[i] ? b->ndms[i] - 2 : 0;
+    hg::SmoothBeam &B = sb[i];
+    B.dd = b->d_dd + b->dd_off[i];
+    B.dd_stride = b->z.ntime_dd;
+    B.boxes = b->d_boxes + b->box_off[i];
+    B.rowmean = b->d_rowmean + b->row_off[i];
+    B.rowmax = b->d_rowmax + b->row_off[i];
+    B.rowvar = b->d_rowvar + b->row_off[i];
+    B.counts = b->d_counts + b->row_off[i];
+    B.offsets = b->d_offsets + b->row_off[i];
+    B.stats = b->d_stats + (size_t)i * b->z.nbox * 4;
+    B.gate = b->d_gate + (size_t)i * 4;
+    B.cand_i = b->d_cand_i + (size_t)i * cap;
+    B.cand_v = b->d_cand_v + (size_t)i * cap;
+    B.total = b->d_total + i;
+    B.active = b->d_active + i;
+    B.h = b->ndms[i] - 2;
+    B.row0 = b->nrows;
+    B.cap = (int)cap;
+    B.beam_id = i + b->p.beam0;
+    for (int r = 0; r < h; ++r) row_beam.push_back(i);
+    b->nrows += h;
+    hg::DedispBeam &d = b->dbeams[i];
+    d.packed = b->d_packed + (size_t)i * b->p.nchan * b->z.R;
+    d.out = b->d_dd + b->dd_off[i];
+    d.win0 = 0;
+    d.dm_count = b->member[i] ? b->ndms[i] : 0;
+    d.item0 = 0;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  if (!row_beam.empty())
+    CK(cudaMemcpy(b->d_row_beam, row_beam.data(), row_beam.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_sbeams, sb.data(), sb.size() * sizeof(hg::SmoothBeam), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_ntime, b->ntime.data(), nb * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_min_gulp, b->min_gulp.data(), nb * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_member, b->member.data(), nb * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_join, b->join.data(), nb * 4, cudaMemcpyHostToDevice));
+  b->items_dpt = -1;  // dedisp_args re-uploads the beams with their item prefix
+  for (Lane &l : b->lanes) l.stale = true;
+  return HELLA_OK;
+}
+
+// Slot i's sizes for `ndms` trials.
+void set_slot_sizes(hella_batch *b, int i, int ndms) {
+  const int nch = b->p.nchan;
+  const int *delays = hdd_get_delay_table(b->plan);
+  b->ndms[i] = ndms;
+  b->max_delay[i] = delays[(size_t)(ndms - 1) * nch + nch - 1];
+  b->ntime[i] = ntime_of(b->p, b->max_delay[i]);
+  b->min_gulp[i] = b->ntime[i] / b->p.gulp;  // casm_hella_refactored.cu:632
+}
+
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
   hg::DeviceTables tb;
-  if (hg::plan_device_tables(b->plan, 0, b->ndms_all, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
+  if (hg::plan_device_tables(b->plan, 0, b->z.ndms_all, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
     return HELLA_ERR_DEDISP;
   if (t.add_mode && tb.dpt < 8) return HELLA_ERR_INVALID_ARG;
   hg::DedispArgs a{};
   a.beams = b->d_dbeams;
   a.nbeam = b->nbeam;
-  a.ntt = hg::dedisp_time_tiles(b->ntime_dd);
+  a.ntt = hg::dedisp_time_tiles(b->z.ntime_dd);
   // work-item prefix of this DM tile (win0 is rewritten on the device each gulp)
   int items = 0;
   for (int i = 0; i < b->nbeam; ++i) {
     b->dbeams[i].item0 = items;
-    items += hg::dedisp_items(b->ndms[i], tb.dpt, a.ntt);
+    items += hg::dedisp_items(b->dbeams[i].dm_count, tb.dpt, a.ntt);
   }
   if (b->items_dpt != tb.dpt) {
     CK(cudaStreamSynchronize(b->stream));
@@ -164,11 +360,11 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
   }
   a.nitems = items;
   a.group = t.group;
-  a.R = b->R;
+  a.R = b->z.R;
   a.nact = tb.nact;
   a.dm_first = 0;
-  a.nout = b->ntime_dd;
-  a.out_stride = b->ntime_dd;
+  a.nout = b->z.ntime_dd;
+  a.out_stride = b->z.ntime_dd;
   a.dpt = tb.dpt;
   a.cc = tb.cc;
   a.nbuf = t.stages;
@@ -188,9 +384,9 @@ hg::SmoothArgs smooth_args(hella_batch *b, int w0, int nw) {
   a.nbeam = b->nbeam;
   a.row_beam = b->d_row_beam;
   a.nrows = b->nrows;
-  a.ntime_dd = b->ntime_dd;
-  a.ntime_out = b->ntime_out;
-  a.nbox = b->nbox;
+  a.ntime_dd = b->z.ntime_dd;
+  a.ntime_out = b->z.ntime_out;
+  a.nbox = b->z.nbox;
   a.wmin = b->p.width_min;
   a.wmax = b->p.width_max;
   a.anchor = b->p.smooth_anchor;
@@ -204,51 +400,51 @@ hg::SmoothArgs smooth_args(hella_batch *b, int w0, int nw) {
 }
 
 // Every launch of one gulp, in order, on b->stream (captured or not).
-hella_status enqueue_gulp(hella_batch *b, const hg::DedispArgs &da) {
-  const int nb = b->nbeam;
+hella_status enqueue_gulp(hella_batch *b, const hg::DedispArgs &da, Lane &l) {
+  const int nb = b->nbeam, nch = b->p.nchan;
   k_advance<<<(nb + 255) / 256, 256, 0, b->stream>>>(b->d_pos, b->d_dbeams, b->d_active, b->d_total,
-                                                     b->d_ntime, b->d_min_gulp, nb, b->R, b->p.gulp);
-  CK(hg::flag_gulp_dev(b->fs, b->d_gulp, b->d_plain, b->R, b->d_pos, b->stream));
-  CK(hg::pack_gulp_dev(b->d_plain, b->d_packed, nb, b->p.nchan, b->R, b->p.gulp, b->d_pos, b->stream,
-                       b->d_keep));
-  CK(hg::dedisperse(da, b->stream));
-  for (int w0 = 0; w0 < b->nbox; w0 += b->nwp) {
-    const hg::SmoothArgs a = smooth_args(b, w0, std::min(b->nwp, b->nbox - w0));
+                                                     b->d_ntime, b->d_min_gulp, b->d_member, b->d_join, nb,
+                                                     b->z.R, b->p.gulp);
+  CK(hg::flag_gulp_dev(b->fs, l.d_gulp, b->d_plain, b->z.R, b->d_pos, b->stream));
+  k_ew_bandpass<<<std::min(1024, (nb * nch + 255) / 256), 256, 0, b->stream>>>(
+      b->fs.bp1, b->d_ew, b->d_member, b->d_join, b->d_pos, nb, nch, b->bp_alpha);
+  CK(hg::pack_gulp_dev(b->d_plain, b->d_packed, nb, nch, b->z.R, b->p.gulp, b->d_pos, b->stream, b->d_keep));
+  if (da.nitems > 0) CK(hg::dedisperse(da, b->stream));
+  for (int w0 = 0; w0 < b->z.nbox; w0 += b->nwp) {
+    const hg::SmoothArgs a = smooth_args(b, w0, std::min(b->nwp, b->z.nbox - w0));
     CK(hg::smooth_planes(a, b->stream));
     CK(hg::smooth_stats(a, b->stream, 1));
     CK(hg::find_peaks(a, b->stream));
   }
-  k_gather<<<nb, 256, 0, b->stream>>>(b->d_sbeams, b->d_total, nb, b->d_out);
-  CK(cudaMemcpyAsync(b->h_total, b->d_total, sizeof(int) * nb, cudaMemcpyDeviceToHost, b->stream));
-  k_rewind<<<1, 1, 0, b->stream>>>(b->d_pos, b->R, b->p.gulp);
-  hg::count_launches(3);
+  k_gather<<<nb, 256, 0, b->stream>>>(b->d_sbeams, b->d_total, nb, l.d_out);
+  CK(cudaMemcpyAsync(l.h_total, b->d_total, sizeof(int) * nb, cudaMemcpyDeviceToHost, b->stream));
+  k_rewind<<<1, 1, 0, b->stream>>>(b->d_pos, b->z.R, b->p.gulp);
+  hg::count_launches(4);
   CK(cudaGetLastError());
   return HELLA_OK;
 }
 
-// Captures the gulp sequence into the executable graph (first use, or after
-// the tile shape or stream changed).
-hella_status build_graph(hella_batch *b, const hg::DedispArgs &da) {
+// Captures lane l's gulp sequence into its executable graph.
+hella_status build_graph(hella_batch *b, const hg::DedispArgs &da, Lane &l) {
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  const hella_status s = enqueue_gulp(b, da);
+  const hella_status s = enqueue_gulp(b, da, l);
   const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (s != HELLA_OK || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
     return s != HELLA_OK ? s : HELLA_ERR_CUDA;
   }
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
-  b->exec = nullptr;
-  b->graph = g;
-  const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
-  if (ie != cudaSuccess) {
+  if (l.exec) cudaGraphExecDestroy(l.exec);
+  if (l.graph) cudaGraphDestroy(l.graph);
+  l.exec = nullptr;
+  l.graph = g;
+  if (cudaGraphInstantiate(&l.exec, g, 0) != cudaSuccess) {
     cudaGetLastError();
-    b->exec = nullptr;
+    l.exec = nullptr;
     return HELLA_ERR_CUDA;
   }
-  b->graph_stale = false;
+  l.stale = false;
   return HELLA_OK;
 }
 
@@ -256,6 +452,7 @@ hella_status time_shape(hella_batch *b, const hella_tuning &t, int reps, float *
   hg::DedispArgs da;
   hella_status s = dedisp_args(b, t, &da);
   if (s != HELLA_OK) return s;
+  if (da.nitems == 0) return HELLA_ERR_STATE;
   s = hg::time_runs(b->stream, reps, [&]() -> hella_status {
     CK(hg::dedisperse(da, b->stream));
     return HELLA_OK;
@@ -278,10 +475,16 @@ hella_status autotune(hella_batch *b, int reps, hella_tuning *out, float *out_ms
       &best_ms);
   if (s != HELLA_OK) return s;
   b->tune = best;
-  b->graph_stale = true;
+  for (Lane &l : b->lanes) l.stale = true;
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
   return HELLA_OK;
+}
+
+bool any_busy(const hella_batch *b) {
+  for (const Lane &l : b->lanes)
+    if (l.busy) return true;
+  return false;
 }
 
 }  // namespace
@@ -292,21 +495,41 @@ void hella_batch_params_default(hella_batch_params *p) {
   std::memset(p, 0, sizeof(*p));
   hella_params_default(&p->base);
   p->use_graph = 1;
+  p->inflight = 1;
+  p->bp_alpha = 0.1f;
 }
 
 void hella_batch_destroy(hella_batch *b) {
   if (!b) return;
   cudaSetDevice(b->p.device);
-  cudaStreamSynchronize(b->stream);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
-  if (b->ev0) cudaEventDestroy(b->ev0);
-  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
+  for (Lane &l : b->lanes) {
+    if (l.exec) cudaGraphExecDestroy(l.exec);
+    if (l.graph) cudaGraphDestroy(l.graph);
+    if (l.copied) cudaEventDestroy(l.copied);
+    if (l.t0) cudaEventDestroy(l.t0);
+    if (l.t1) cudaEventDestroy(l.t1);
+  }
   for (void *ptr : b->dallocs) cudaFree(ptr);
   for (void *ptr : b->hallocs) cudaFreeHost(ptr);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
   hdd_destroy_plan(b->plan);
   delete b;
+}
+
+hella_status hella_batch_bytes(const hella_batch_params *bp, size_t *bytes) {
+  if (!bp || !bytes) return HELLA_ERR_INVALID_ARG;
+  hella_status s = hg::validate_params(&bp->base);
+  if (s != HELLA_OK) return s;
+  hdd_plan plan = nullptr;
+  Sizes z;
+  if ((s = batch_sizes(bp, &plan, &z)) != HELLA_OK) return s;
+  hdd_destroy_plan(plan);
+  const int nw = bp->widths_per_pass ? std::min(bp->widths_per_pass, z.nbox) : z.nbox;
+  *bytes = z.fixed + z.per_width * nw;
+  return HELLA_OK;
 }
 
 hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp) {
@@ -315,7 +538,9 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   const hella_params *p = &bp->base;
   hella_status s = hg::validate_params(p);
   if (s != HELLA_OK) return s;
-  if (bp->widths_per_pass < 0) return HELLA_ERR_INVALID_ARG;
+  if (bp->widths_per_pass < 0 || (bp->inflight != 1 && bp->inflight != 2) || !(bp->bp_alpha > 0.f) ||
+      bp->bp_alpha > 1.f)
+    return HELLA_ERR_INVALID_ARG;
   if (cudaSetDevice(p->device) != cudaSuccess) {
     cudaGetLastError();
     return HELLA_ERR_CUDA;
@@ -325,84 +550,83 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   b->p = *p;
   b->nbeam = p->nbeam;
   b->use_graph = bp->use_graph != 0;
+  b->dynamic = bp->dynamic != 0;
+  b->bp_alpha = bp->bp_alpha;
   auto fail = [&](hella_status st) {
     hella_batch_destroy(b);
     return st;
   };
-  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     return fail(HELLA_ERR_CUDA);
   }
   b->stream = b->own_stream;
   const int nb = b->nbeam, nch = p->nchan;
+  if ((s = batch_sizes(bp, &b->plan, &b->z)) != HELLA_OK) return fail(s);
+  const Sizes &z = b->z;
 
-  // DM lists: beam b's is the prefix of the longest one up to its ceiling
-  std::vector<float> ceil(nb, p->dm_max);
-  if (bp->dm_max)
-    for (int i = 0; i < nb; ++i) ceil[i] = bp->dm_max[i];
-  float top = ceil[0];
-  for (float c : ceil) {
-    if (!(c >= p->dm_min)) return fail(HELLA_ERR_INVALID_ARG);
-    top = std::max(top, c);
-  }
-  if (hdd_create_plan(&b->plan, nch, (float)p->plan_dt, (float)p->f0_mhz, (float)p->df_mhz) != HDD_NO_ERROR ||
-      hdd_generate_dm_list(b->plan, p->dm_min, top, p->ti_us, p->dm_tol) != HDD_NO_ERROR)
-    return fail(HELLA_ERR_DEDISP);
-  b->ndms_all = (int)hdd_get_dm_count(b->plan);
-  const float *all = hdd_get_dm_list(b->plan);
-  const int *delays = hdd_get_delay_table(b->plan);
+  // slots: DM ceilings (dynamic slots take base.dm_max unless dm_max says otherwise)
   b->ndms.resize(nb);
   b->max_delay.resize(nb);
   b->ntime.resize(nb);
   b->min_gulp.resize(nb);
+  b->member.assign(nb, 1);
+  b->join.assign(nb, 0);
+  if (bp->member)
+    for (int i = 0; i < nb; ++i) b->member[i] = bp->member[i] != 0;
   for (int i = 0; i < nb; ++i) {
-    const std::vector<float> mine = hg::generate_dm_list(
-        (float)p->dm_min, (float)ceil[i], (float)p->ti_us, (float)p->dm_tol, nch, (float)p->plan_dt,
-        (float)p->f0_mhz, (float)p->df_mhz);
-    if ((int)mine.size() > b->ndms_all || (int)mine.size() < 3) return fail(HELLA_ERR_INVALID_ARG);
-    for (size_t k = 0; k < mine.size(); ++k)
-      if (mine[k] != all[k]) return fail(HELLA_ERR_DEDISP);  // not a prefix: cannot share tables
-    b->ndms[i] = (int)mine.size();
-    b->max_delay[i] = delays[(size_t)(b->ndms[i] - 1) * nch + nch - 1];
-    b->ntime[i] = 32 * ((p->gulp + b->max_delay[i] + p->width_max) / 32 + 1);  // :217-219
-    b->min_gulp[i] = b->ntime[i] / p->gulp;                                      // :632
-    b->R = std::max<long>(b->R, b->ntime[i]);
+    int n = z.cap_ndms[i];
+    if (b->dynamic && bp->dm_max) {
+      if (bp->dm_max[i] > p->dm_max) return fail(HELLA_ERR_BUDGET);
+      n = prefix_trials(*p, b->plan, bp->dm_max[i]);
+      if (n < 3) return fail(n < 0 ? HELLA_ERR_DEDISP : HELLA_ERR_INVALID_ARG);
+    }
+    set_slot_sizes(b, i, n);
   }
-  b->ntime_dd = p->gulp + p->width_max;
-  b->ntime_out = p->gulp;
-  for (int sm = p->width_min; sm < p->width_max; sm *= 2) b->nbox++;
-  std::vector<int> row0(nb);
-  for (int i = 0; i < nb; ++i) {
-    row0[i] = b->nrows;
-    b->nrows += b->ndms[i] - 2;
-  }
-  size_t dd_floats = 0;
-  for (int i = 0; i < nb; ++i) dd_floats += (size_t)b->ndms[i] * b->ntime_dd;
 
   // HBM: everything but the smoothed planes, then as many widths per pass
   // as the budget allows
-  const size_t R = b->R, cap = p->max_giants;
-  const size_t fixed = (size_t)nb * p->gulp * nch + (size_t)nb * nch * R * 5 + (size_t)nb * nch +
-                       (size_t)nb * nch * (256 * 6 + 16) + (size_t)nb * p->gulp * 6 + dd_floats * 4 +
-                       (size_t)b->nrows * b->nbox * 20 + (size_t)nb * (cap * 40 + 256);
-  const size_t per_width = (size_t)b->nrows * b->ntime_out * 4;
   size_t budget = p->hbm_budget;
   if (!budget) {
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return fail(HELLA_ERR_CUDA);
     budget = fr > (1ul << 30) ? fr - (1ul << 30) : 0;  // leave 1 GB to the runtime
   }
-  if (fixed + per_width > budget) return fail(HELLA_ERR_BUDGET);
-  b->nwp = bp->widths_per_pass ? std::min(bp->widths_per_pass, b->nbox)
-                               : (int)std::min<size_t>(b->nbox, (budget - fixed) / per_width);
-  if (b->nwp < 1 || fixed + per_width * b->nwp > budget) return fail(HELLA_ERR_BUDGET);
+  if (z.fixed + z.per_width > budget) return fail(HELLA_ERR_BUDGET);
+  b->nwp = bp->widths_per_pass ? std::min(bp->widths_per_pass, z.nbox)
+                               : (int)std::min<size_t>(z.nbox, (budget - z.fixed) / z.per_width);
+  if (b->nwp < 1 || z.fixed + z.per_width * b->nwp > budget) return fail(HELLA_ERR_BUDGET);
 
+  const size_t R = z.R, cap = p->max_giants;
+  size_t dd_floats = 0, rows = 0;
+  b->dd_off.resize(nb);
+  b->box_off.resize(nb);
+  b->row_off.resize(nb);
+  for (int i = 0; i < nb; ++i) {
+    b->dd_off[i] = dd_floats;
+    b->box_off[i] = rows * b->nwp * z.ntime_out;
+    b->row_off[i] = rows * z.nbox;
+    dd_floats += (size_t)z.cap_ndms[i] * z.ntime_dd;
+    rows += (size_t)z.cap_ndms[i] - 2;
+  }
 #define DA(ptr, bytes)                                                  \
   if ((s = dalloc(b, (void **)&(ptr), (bytes))) != HELLA_OK) return fail(s);
-  DA(b->d_gulp, (size_t)nb * p->gulp * nch);
+  b->lanes.resize(bp->inflight);
+  for (Lane &l : b->lanes) {
+    DA(l.d_gulp, (size_t)nb * p->gulp * nch);
+    DA(l.d_out, (size_t)nb * cap * sizeof(hella_cand));
+    if ((s = halloc(b, (void **)&l.h_total, (size_t)nb * 4)) != HELLA_OK) return fail(s);
+    if (cudaEventCreate(&l.copied) != cudaSuccess || cudaEventCreate(&l.t0) != cudaSuccess ||
+        cudaEventCreate(&l.t1) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(HELLA_ERR_CUDA);
+    }
+  }
   DA(b->d_plain, (size_t)nb * nch * R);
   DA(b->d_packed, (size_t)nb * nch * R * 4);
   DA(b->d_keep, (size_t)nb * nch);
+  DA(b->d_ew, (size_t)nb * nch * 4);
   hg::FlagState &f = b->fs;
   f.nbeam = nb;
   f.nchan = nch;
@@ -421,77 +645,37 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   DA(f.ts, (size_t)nb * p->gulp * 4);
   DA(f.hts, (size_t)nb * p->gulp * 2);
   DA(b->d_dd, dd_floats * 4);
-  DA(b->d_boxes, per_width * b->nwp);
-  const size_t rw = (size_t)b->nrows * b->nbox;
+  DA(b->d_boxes, z.per_width * b->nwp);
+  const size_t rw = rows * z.nbox;
   DA(b->d_rowmean, rw * 4);
   DA(b->d_rowmax, rw * 4);
   DA(b->d_rowvar, rw * 4);
   DA(b->d_counts, rw * 4);
   DA(b->d_offsets, rw * 4);
-  DA(b->d_stats, (size_t)nb * b->nbox * 16);
+  DA(b->d_stats, (size_t)nb * z.nbox * 16);
   DA(b->d_gate, (size_t)nb * 16);
   DA(b->d_total, (size_t)nb * 4);
   DA(b->d_active, (size_t)nb * 4);
-  DA(b->d_row_beam, (size_t)b->nrows * 4);
+  DA(b->d_row_beam, rows * 4);
   DA(b->d_err, 16);
   DA(b->d_ntime, (size_t)nb * 4);
   DA(b->d_min_gulp, (size_t)nb * 4);
+  DA(b->d_member, (size_t)nb * 4);
+  DA(b->d_join, (size_t)nb * 4);
   DA(b->d_cand_i, (size_t)nb * cap * 16);
   DA(b->d_cand_v, (size_t)nb * cap * 4);
-  DA(b->d_out, (size_t)nb * cap * sizeof(hella_cand));
   DA(b->d_dbeams, (size_t)nb * sizeof(hg::DedispBeam));
   DA(b->d_sbeams, (size_t)nb * sizeof(hg::SmoothBeam));
   DA(b->d_pos, sizeof(hg::GulpPos));
 #undef DA
-  if (cudaMallocHost((void **)&b->h_total, (size_t)nb * 4) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(HELLA_ERR_ALLOC);
-  }
-  b->hallocs.push_back(b->h_total);
 
-  // host tables
   std::vector<uint8_t> keep((size_t)nb * nch, 1);
   if (bp->killmask)
     for (size_t i = 0; i < keep.size(); ++i) keep[i] = bp->killmask[i] != 0;
-  std::vector<int> row_beam(b->nrows);
-  std::vector<hg::SmoothBeam> sb(nb);
   b->dbeams.resize(nb);
-  size_t dd_off = 0, box_off = 0;
-  for (int i = 0; i < nb; ++i) {
-    const int h = b->ndms[i] - 2;
-    for (int r = 0; r < h; ++r) row_beam[row0[i] + r] = i;
-    hg::DedispBeam &d = b->dbeams[i];
-    d.packed = b->d_packed + (size_t)i * nch * R;
-    d.out = b->d_dd + dd_off;
-    d.win0 = 0;
-    d.dm_count = b->ndms[i];
-    d.item0 = 0;
-    hg::SmoothBeam &B = sb[i];
-    B.dd = b->d_dd + dd_off;
-    B.dd_stride = b->ntime_dd;
-    B.boxes = b->d_boxes + box_off;
-    const size_t ro = (size_t)row0[i] * b->nbox;
-    B.rowmean = b->d_rowmean + ro;
-    B.rowmax = b->d_rowmax + ro;
-    B.rowvar = b->d_rowvar + ro;
-    B.counts = b->d_counts + ro;
-    B.offsets = b->d_offsets + ro;
-    B.stats = b->d_stats + (size_t)i * b->nbox * 4;
-    B.gate = b->d_gate + (size_t)i * 4;
-    B.cand_i = b->d_cand_i + (size_t)i * cap;
-    B.cand_v = b->d_cand_v + (size_t)i * cap;
-    B.total = b->d_total + i;
-    B.active = b->d_active + i;
-    B.h = h;
-    B.row0 = row0[i];
-    B.cap = (int)cap;
-    B.beam_id = i + p->beam0;
-    dd_off += (size_t)b->ndms[i] * b->ntime_dd;
-    box_off += (size_t)b->nwp * h * b->ntime_out;
-  }
   std::vector<float> taps;
   std::vector<int> toff, tn;
-  hg::smoothing_taps(*p, b->nbox, &taps, &toff, &tn);
+  hg::smoothing_taps(*p, z.nbox, &taps, &toff, &tn);
   if ((s = dalloc(b, (void **)&b->d_taps, taps.size() * 4)) != HELLA_OK) return fail(s);
   if ((s = dalloc(b, (void **)&b->d_tapoff, toff.size() * 4)) != HELLA_OK) return fail(s);
   if ((s = dalloc(b, (void **)&b->d_tapn, tn.size() * 4)) != HELLA_OK) return fail(s);
@@ -500,33 +684,28 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
       cudaMemcpy(b->d_tapoff, toff.data(), toff.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_tapn, tn.data(), tn.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_keep, keep.data(), keep.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_row_beam, row_beam.data(), row_beam.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_sbeams, sb.data(), sb.size() * sizeof(hg::SmoothBeam), cudaMemcpyHostToDevice) !=
-          cudaSuccess ||
-      cudaMemcpy(b->d_dbeams, b->dbeams.data(), nb * sizeof(hg::DedispBeam), cudaMemcpyHostToDevice) !=
-          cudaSuccess ||
-      cudaMemcpy(b->d_ntime, b->ntime.data(), nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_min_gulp, b->min_gulp.data(), nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_pos, &pos0, sizeof(pos0), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(b->d_plain, 0, (size_t)nb * nch * R) != cudaSuccess ||
       cudaMemset(b->d_packed, 0, (size_t)nb * nch * R * 4) != cudaSuccess ||
+      cudaMemset(b->d_ew, 0, (size_t)nb * nch * 4) != cudaSuccess ||
       cudaMemset(b->d_err, 0, 16) != cudaSuccess || cudaMemset(b->d_total, 0, (size_t)nb * 4) != cudaSuccess ||
-      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
       cudaDeviceSynchronize() != cudaSuccess) {
     cudaGetLastError();
     return fail(HELLA_ERR_CUDA);
   }
-  if (p->autotune && (s = autotune(b, 2, nullptr, nullptr)) != HELLA_OK) return fail(s);
+  if ((s = upload_layout(b)) != HELLA_OK) return fail(s);
+  if (p->autotune && b->nrows > 0 && (s = autotune(b, 2, nullptr, nullptr)) != HELLA_OK) return fail(s);
   *out = b;
   return HELLA_OK;
 }
 
 hella_status hella_batch_set_stream(hella_batch *b, void *stream) {
   if (!b) return HELLA_ERR_INVALID_ARG;
+  if (any_busy(b)) return HELLA_ERR_STATE;
   CK(cudaStreamSynchronize(b->stream));
   b->stream = stream ? (cudaStream_t)stream : b->own_stream;  // NULL: the batch's own stream
   hdd_set_stream(b->plan, b->stream);
-  b->graph_stale = true;
+  for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;
 }
 
@@ -535,35 +714,90 @@ hella_status hella_batch_get_info(const hella_batch *b, int beam, hella_info *i)
   i->ntime = b->ntime[beam];
   i->ndms = b->ndms[beam];
   i->max_delay = b->max_delay[beam];
-  i->ntime_dd = b->ntime_dd;
-  i->ntime_out = b->ntime_out;
-  i->nboxcar = b->nbox;
+  i->ntime_dd = b->z.ntime_dd;
+  i->ntime_out = b->z.ntime_out;
+  i->nboxcar = b->z.nbox;
   i->min_gulp = b->min_gulp[beam];
-  i->gulp_index = b->gulp_index;
+  i->gulp_index = b->gulp_index - b->join[beam];
   i->device_bytes = b->dev_bytes;
   return HELLA_OK;
 }
 
-hella_status hella_batch_process_gulp(hella_batch *b, const uint8_t *gulp, int on_device,
-                                      hella_cand *out, int max, int *n, int *counts, int *searched) {
-  if (!b || !gulp || max < 0 || (max > 0 && !out)) return HELLA_ERR_INVALID_ARG;
+hella_status hella_batch_set_beam(hella_batch *b, int beam, int member, float dm_max, const int *killmask) {
+  if (!b || beam < 0 || beam >= b->nbeam) return HELLA_ERR_INVALID_ARG;
+  if (!b->dynamic || any_busy(b)) return HELLA_ERR_STATE;
   CK(cudaSetDevice(b->p.device));
-  const size_t bytes = (size_t)b->nbeam * b->p.gulp * b->p.nchan;
-  CK(cudaMemcpyAsync(b->d_gulp, gulp, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                     b->stream));
+  const int nch = b->p.nchan;
+  if (member) {
+    if (dm_max > b->p.dm_max) return HELLA_ERR_BUDGET;
+    const int n = prefix_trials(b->p, b->plan, dm_max);
+    if (n < 3) return n < 0 ? HELLA_ERR_DEDISP : HELLA_ERR_INVALID_ARG;
+    set_slot_sizes(b, beam, n);
+    std::vector<uint8_t> keep(nch, 1);
+    if (killmask)
+      for (int c = 0; c < nch; ++c) keep[c] = killmask[c] != 0;
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaMemcpy(b->d_keep + (size_t)beam * nch, keep.data(), nch, cudaMemcpyHostToDevice));
+    // a fresh ring for the newcomer, as a new single-beam context starts with
+    CK(cudaMemset(b->d_plain + (size_t)beam * nch * b->z.R, 0, (size_t)nch * b->z.R));
+    CK(cudaMemset(b->d_packed + (size_t)beam * nch * b->z.R, 0, (size_t)nch * b->z.R * 4));
+    b->join[beam] = b->gulp_index;
+  }
+  b->member[beam] = member != 0;
+  return upload_layout(b);
+}
+
+hella_status hella_batch_get_bandpass(hella_batch *b, int beam, float *out) {
+  if (!b || !out || beam < 0 || beam >= b->nbeam) return HELLA_ERR_INVALID_ARG;
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaMemcpy(out, b->d_ew + (size_t)beam * b->p.nchan, (size_t)b->p.nchan * 4, cudaMemcpyDeviceToHost));
+  return HELLA_OK;
+}
+
+hella_status hella_batch_submit(hella_batch *b, const uint8_t *gulp, int on_device) {
+  if (!b || !gulp) return HELLA_ERR_INVALID_ARG;
+  CK(cudaSetDevice(b->p.device));
+  Lane &l = b->lanes[b->next_lane];
+  if (l.busy) return HELLA_ERR_STATE;
   hg::DedispArgs da;
   hella_status s = dedisp_args(b, b->tune, &da);
   if (s != HELLA_OK) return s;
-  CK(cudaEventRecord(b->ev0, b->stream));
+  l.submitted = now_ms();
+  // the input copy waits for the last search that read this lane's buffers
+  CK(cudaStreamWaitEvent(b->copy_stream, l.t1, 0));
+  const size_t bytes = (size_t)b->nbeam * b->p.gulp * b->p.nchan;
+  CK(cudaMemcpyAsync(l.d_gulp, gulp, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                     b->copy_stream));
+  CK(cudaEventRecord(l.copied, b->copy_stream));
+  CK(cudaStreamWaitEvent(b->stream, l.copied, 0));
+  CK(cudaEventRecord(l.t0, b->stream));
   if (b->use_graph) {
-    if (b->graph_stale && (s = build_graph(b, da)) != HELLA_OK) return s;
-    CK(cudaGraphLaunch(b->exec, b->stream));
-  } else if ((s = enqueue_gulp(b, da)) != HELLA_OK) {
+    if (l.stale && (s = build_graph(b, da, l)) != HELLA_OK) return s;
+    CK(cudaGraphLaunch(l.exec, b->stream));
+  } else if ((s = enqueue_gulp(b, da, l)) != HELLA_OK) {
     return s;
   }
-  CK(cudaEventRecord(b->ev1, b->stream));
-  CK(cudaStreamSynchronize(b->stream));
-  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  CK(cudaEventRecord(l.t1, b->stream));
+  l.searched.resize(b->nbeam);
+  for (int i = 0; i < b->nbeam; ++i)
+    l.searched[i] = b->member[i] && b->gulp_index - b->join[i] >= b->min_gulp[i];
+  l.busy = true;
+  b->queue.push_back(b->next_lane);
+  b->next_lane = (b->next_lane + 1) % (int)b->lanes.size();
+  b->gulp_index++;
+  return HELLA_OK;
+}
+
+hella_status hella_batch_poll(hella_batch *b, hella_cand *out, int max, int *n, int *counts, int *searched,
+                              float *latency_ms, float *device_ms) {
+  if (!b || max < 0 || (max > 0 && !out)) return HELLA_ERR_INVALID_ARG;
+  if (b->queue.empty()) return HELLA_ERR_STATE;
+  CK(cudaSetDevice(b->p.device));
+  Lane &l = b->lanes[b->queue.front()];
+  CK(cudaEventSynchronize(l.t1));
+  b->queue.pop_front();
+  l.busy = false;
+  cudaEventElapsedTime(&b->last_ms, l.t0, l.t1);
   int err = 0;
   CK(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
@@ -572,22 +806,32 @@ hella_status hella_batch_process_gulp(hella_batch *b, const uint8_t *gulp, int o
   }
   long total = 0;
   for (int i = 0; i < b->nbeam; ++i) {
-    total += b->h_total[i];
-    if (counts) counts[i] = b->h_total[i];
-    if (searched) searched[i] = b->gulp_index >= b->min_gulp[i];
+    total += l.h_total[i];
+    if (counts) counts[i] = l.h_total[i];
+    if (searched) searched[i] = l.searched[i];
   }
   const int k = (int)std::min<long>(total, max);
-  if (k > 0)
-    CK(cudaMemcpy(out, b->d_out, (size_t)k * sizeof(hella_cand), cudaMemcpyDeviceToHost));
+  if (k > 0) CK(cudaMemcpy(out, l.d_out, (size_t)k * sizeof(hella_cand), cudaMemcpyDeviceToHost));
   if (n) *n = k;
-  b->gulp_index++;
+  if (device_ms) *device_ms = b->last_ms;
+  if (latency_ms) *latency_ms = (float)(now_ms() - l.submitted);
   return HELLA_OK;
+}
+
+hella_status hella_batch_process_gulp(hella_batch *b, const uint8_t *gulp, int on_device, hella_cand *out,
+                                      int max, int *n, int *counts, int *searched) {
+  if (!b || !gulp || max < 0 || (max > 0 && !out)) return HELLA_ERR_INVALID_ARG;
+  if (!b->queue.empty()) return HELLA_ERR_STATE;
+  hella_status s = hella_batch_submit(b, gulp, on_device);
+  if (s != HELLA_OK) return s;
+  return hella_batch_poll(b, out, max, n, counts, searched, nullptr, nullptr);
 }
 
 hella_status hella_batch_copy_dedisp(hella_batch *b, int beam, float *out) {
   if (!b || !out || beam < 0 || beam >= b->nbeam) return HELLA_ERR_INVALID_ARG;
   CK(cudaStreamSynchronize(b->stream));
-  CK(cudaMemcpy(out, b->dbeams[beam].out, (size_t)b->ndms[beam] * b->ntime_dd * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(out, b->d_dd + b->dd_off[beam], (size_t)b->ndms[beam] * b->z.ntime_dd * 4,
+                cudaMemcpyDeviceToHost));
   return HELLA_OK;
 }
 
@@ -599,20 +843,23 @@ hella_status hella_batch_get_tuning(const hella_batch *b, hella_tuning *t) {
 
 hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t) {
   if (!b || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
+  if (any_busy(b)) return HELLA_ERR_STATE;
   b->tune = *t;
   b->tune.samples_per_thread = 4;
-  b->graph_stale = true;
+  for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;
 }
 
 hella_status hella_batch_time_dedisp(hella_batch *b, const hella_tuning *t, int reps, float *ms) {
   if (!b || !ms || reps < 1) return HELLA_ERR_INVALID_ARG;
+  if (any_busy(b)) return HELLA_ERR_STATE;
   CK(cudaSetDevice(b->p.device));
   return time_shape(b, t ? *t : b->tune, reps, ms);
 }
 
 hella_status hella_batch_autotune(hella_batch *b, int reps, hella_tuning *best, float *best_ms) {
   if (!b || reps < 1) return HELLA_ERR_INVALID_ARG;
+  if (any_busy(b)) return HELLA_ERR_STATE;
   CK(cudaSetDevice(b->p.device));
   return autotune(b, reps, best, best_ms);
 }
@@ -620,11 +867,12 @@ hella_status hella_batch_autotune(hella_batch *b, int reps, hella_tuning *best, 
 hella_status hella_batch_graph_kernels(const hella_batch *b, int *kernels) {
   if (!b || !kernels) return HELLA_ERR_INVALID_ARG;
   *kernels = 0;
-  if (!b->graph) return HELLA_ERR_STATE;
+  const cudaGraph_t g = b->lanes.empty() ? nullptr : b->lanes[0].graph;
+  if (!g) return HELLA_ERR_STATE;
   size_t n = 0;
-  CK(cudaGraphGetNodes(b->graph, nullptr, &n));
+  CK(cudaGraphGetNodes(g, nullptr, &n));
   std::vector<cudaGraphNode_t> nodes(n);
-  CK(cudaGraphGetNodes(b->graph, nodes.data(), &n));
+  CK(cudaGraphGetNodes(g, nodes.data(), &n));
   for (cudaGraphNode_t nd : nodes) {
     cudaGraphNodeType t;
     CK(cudaGraphNodeGetType(nd, &t));

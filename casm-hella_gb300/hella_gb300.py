@@ -54,7 +54,8 @@ class HellaParams(C.Structure):
 
 class BatchParams(C.Structure):
     _fields_ = [("base", HellaParams), ("dm_max", C.c_void_p), ("killmask", C.c_void_p),
-                ("widths_per_pass", C.c_int), ("use_graph", C.c_int)]
+                ("widths_per_pass", C.c_int), ("use_graph", C.c_int), ("dynamic", C.c_int),
+                ("member", C.c_void_p), ("inflight", C.c_int), ("bp_alpha", C.c_float)]
 
 
 class HellaTuning(C.Structure):
@@ -158,6 +159,12 @@ def lib() -> C.CDLL:
     _sig(L, "hella_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(HellaTuning), C.POINTER(C.c_float)])
     _sig(L, "hella_batch_last_gulp_ms", C.c_int, [_VP, C.POINTER(C.c_float)])
     _sig(L, "hella_batch_graph_kernels", C.c_int, [_VP, C.POINTER(C.c_int)])
+    _sig(L, "hella_batch_submit", C.c_int, [_VP, _VP, C.c_int])
+    _sig(L, "hella_batch_poll", C.c_int, [_VP, _VP, C.c_int, C.POINTER(C.c_int), _VP, _VP,
+                                           C.POINTER(C.c_float), C.POINTER(C.c_float)])
+    _sig(L, "hella_batch_set_beam", C.c_int, [_VP, C.c_int, C.c_int, C.c_float, _VP])
+    _sig(L, "hella_batch_get_bandpass", C.c_int, [_VP, C.c_int, _VP])
+    _sig(L, "hella_batch_bytes", C.c_int, [C.POINTER(BatchParams), C.POINTER(C.c_size_t)])
     _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
@@ -431,17 +438,12 @@ class Batch:
     dm_max: per-beam DM ceilings; killmask: [nbeam][nchan] (0 = dropped)."""
 
     def __init__(self, base: HellaParams, dm_max=None, killmask=None, widths_per_pass: int = 0,
-                 use_graph: bool = True):
+                 use_graph: bool = True, dynamic: bool = False, member=None, inflight: int = 1,
+                 bp_alpha: float = 0.1):
         self.L = lib()
-        bp = BatchParams()
-        self.L.hella_batch_params_default(C.byref(bp))
-        bp.base = base
-        self._dm = None if dm_max is None else np.ascontiguousarray(dm_max, dtype=np.float32)
-        self._km = None if killmask is None else np.ascontiguousarray(killmask, dtype=np.int32)
-        bp.dm_max = None if self._dm is None else self._dm.ctypes.data
-        bp.killmask = None if self._km is None else self._km.ctypes.data
-        bp.widths_per_pass = widths_per_pass
-        bp.use_graph = int(use_graph)
+        bp = batch_params(base, dm_max, killmask, widths_per_pass, use_graph, dynamic, member, inflight,
+                          bp_alpha)
+        self._keep = bp._keep
         h = _VP()
         _chk(self.L.hella_batch_create(C.byref(h), C.byref(bp)))
         self.h = h
@@ -454,6 +456,29 @@ class Batch:
             self.h = None
 
     __del__ = close
+
+    def submit(self, gulp, on_device=False):
+        _chk(self.L.hella_batch_submit(self.h, _ptr(gulp), int(on_device)))
+
+    def poll(self):
+        """(candidates, counts, searched, latency_ms, device_ms) of the oldest submitted gulp."""
+        cap = self.base.max_giants * self.nbeam
+        out = np.zeros(cap, CAND_DTYPE)
+        counts = np.zeros(self.nbeam, np.int32)
+        searched = np.zeros(self.nbeam, np.int32)
+        n, lat, dev = C.c_int(), C.c_float(), C.c_float()
+        _chk(self.L.hella_batch_poll(self.h, out.ctypes.data, cap, C.byref(n), counts.ctypes.data,
+                                     searched.ctypes.data, C.byref(lat), C.byref(dev)))
+        return out[: n.value], counts, searched.astype(bool), lat.value, dev.value
+
+    def set_beam(self, beam: int, member: bool, dm_max: float = 0.0, killmask=None):
+        km = None if killmask is None else np.ascontiguousarray(killmask, dtype=np.int32)
+        _chk(self.L.hella_batch_set_beam(self.h, beam, int(member), dm_max, None if km is None else km.ctypes.data))
+
+    def bandpass(self, beam: int) -> np.ndarray:
+        out = np.zeros(self.base.nchan, np.float32)
+        _chk(self.L.hella_batch_get_bandpass(self.h, beam, out.ctypes.data))
+        return out
 
     def info(self, beam: int) -> HellaInfo:
         i = HellaInfo()
@@ -507,3 +532,31 @@ class Batch:
         ms = C.c_float()
         _chk(self.L.hella_batch_last_gulp_ms(self.h, C.byref(ms)))
         return ms.value
+
+
+def batch_params(base: HellaParams, dm_max=None, killmask=None, widths_per_pass: int = 0, use_graph: bool = True,
+                 dynamic: bool = False, member=None, inflight: int = 1, bp_alpha: float = 0.1) -> BatchParams:
+    bp = BatchParams()
+    lib().hella_batch_params_default(C.byref(bp))
+    bp.base = base
+    keep = [None if dm_max is None else np.ascontiguousarray(dm_max, dtype=np.float32),
+            None if killmask is None else np.ascontiguousarray(killmask, dtype=np.int32),
+            None if member is None else np.ascontiguousarray(member, dtype=np.int32)]
+    bp.dm_max = None if keep[0] is None else keep[0].ctypes.data
+    bp.killmask = None if keep[1] is None else keep[1].ctypes.data
+    bp.member = None if keep[2] is None else keep[2].ctypes.data
+    bp.widths_per_pass = widths_per_pass
+    bp.use_graph = int(use_graph)
+    bp.dynamic = int(dynamic)
+    bp.inflight = inflight
+    bp.bp_alpha = bp_alpha
+    bp._keep = keep
+    return bp
+
+
+def batch_bytes(base: HellaParams, **kw) -> int:
+    """Device bytes a batch with these parameters holds (hella_batch_bytes)."""
+    bp = batch_params(base, **kw)
+    n = C.c_size_t()
+    _chk(lib().hella_batch_bytes(C.byref(bp), C.byref(n)))
+    return n.value

@@ -197,6 +197,12 @@ typedef struct {
   int widths_per_pass;   /* smoothing widths held in HBM at once; 0: as
                             many as base.hbm_budget (or free memory) allows */
   int use_graph;         /* 1: capture the per-gulp launches in a CUDA graph */
+  int dynamic;           /* 1: beams are slots that join and leave (each sized
+                            for base.dm_max); 0: fixed beams, exact sizes */
+  const int *member;     /* [nbeam] 1 = slot in use at creation (NULL: all) */
+  int inflight;          /* gulps in flight for submit/poll: 1 or 2 */
+  float bp_alpha;        /* weight of the newest gulp in the running
+                            (exponentially weighted) bandpass, 0 < a <= 1 */
 } hella_batch_params;
 
 void hella_batch_params_default(hella_batch_params *p);
@@ -215,6 +221,33 @@ hella_status hella_batch_get_info(const hella_batch *b, int beam, hella_info *in
 hella_status hella_batch_process_gulp(hella_batch *b, const uint8_t *gulp, int on_device,
                                       hella_cand *out, int max, int *n, int *counts,
                                       int *searched);
+/* Streaming (config keys of the serving loop; no counterpart in the
+ * reference).  submit enqueues one gulp (u8 [nbeam][gulp][nchan]; a host
+ * buffer must stay valid until its result is polled, and is best pinned):
+ * its copy to the device overlaps the search of the gulp before it.  poll
+ * returns the oldest submitted gulp's results, blocking until they are
+ * ready; latency_ms (may be NULL) receives the host time from submit to
+ * results, device_ms the device time of its search.  HELLA_ERR_STATE: no
+ * free in-flight buffer (submit) or nothing submitted (poll). */
+hella_status hella_batch_submit(hella_batch *b, const uint8_t *gulp, int on_device);
+hella_status hella_batch_poll(hella_batch *b, hella_cand *out, int max, int *n, int *counts,
+                              int *searched, float *latency_ms, float *device_ms);
+/* Slot `beam` joins (member = 1, with its DM ceiling and killmask
+ * [nchan] or NULL) or leaves (member = 0) from the next submitted gulp on;
+ * a joining slot starts as a fresh single-beam context would (its window is
+ * searched once it holds only its own samples).  Dynamic batches only; no
+ * gulp may be in flight.  dm_max above the batch's base.dm_max:
+ * HELLA_ERR_BUDGET. */
+hella_status hella_batch_set_beam(hella_batch *b, int beam, int member, float dm_max,
+                                  const int *killmask);
+/* Running bandpass of a slot: per channel, the exponentially weighted mean
+ * (weight bp_alpha for the newest gulp) of calc_bandpass_new over the gulps
+ * since the slot joined; fp32 [nchan]. */
+hella_status hella_batch_get_bandpass(hella_batch *b, int beam, float *out);
+/* Device bytes a batch with these parameters would hold (admission by HBM
+ * budget: size nbeam so that this stays within the budget). */
+hella_status hella_batch_bytes(const hella_batch_params *p, size_t *bytes);
+
 /* Inspection: beam's last dedispersed plane, fp32 [ndms_b][ntime_dd]. */
 hella_status hella_batch_copy_dedisp(hella_batch *b, int beam, float *out);
 hella_status hella_batch_get_tuning(const hella_batch *b, hella_tuning *t);

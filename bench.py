@@ -47,10 +47,11 @@ def args_():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batched"],
+    ap.add_argument("--workload", default="full", choices=["full", "batched", "stream"],
                     help="full: the single-beam headline workload; batched: all beams of the "
                          "multi-beam configuration per step")
     ap.add_argument("--beams", type=int, default=256, help="beams of the batched workload")
+    ap.add_argument("--seconds", type=float, default=600.0, help="sky seconds of the stream workload")
     return ap.parse_args()
 
 
@@ -166,6 +167,8 @@ def main():
     torch.cuda.set_device(local)
     if a.workload == "batched":
         return main_batched(a, rank, world, local, dist)
+    if a.workload == "stream":
+        return main_stream(a, rank, world, local, dist)
     import hella_gb300 as hg
 
     hg.lib()
@@ -436,6 +439,132 @@ def main_batched(a, rank, world, local, dist):
         per, cores, desc = cpu_sample(batched_sample_params(params, ceilings[0]), g0, dm_rows=64)
         line["cpu_baseline"] = {"value": round(gulp_s / per, 4), "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": "beam 0 of the batch: " + desc}
+    bt.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+STREAM_WORKLOAD = ("streaming serving loop: 64 beam requests x 1024 ch, tsamp 1.048576 ms, gulps of 8192 "
+                   "samples for {sec:.0f} s of sky, DM 0-2000, widths 1-32, slots admitted by an HBM budget, "
+                   "beams joining and leaving, RFI occupancy drifting 0-20%, two gulps in flight")
+
+
+def main_stream(a, rank, world, local, dist):
+    """The serving loop of the streaming configuration (submit/poll)."""
+    import torch
+    import hella_gb300 as hg
+    import synth
+
+    params, ngulps, skies_at = synth.config_stream(seconds=a.seconds, seed=4 + rank)
+    NB, G, nch = params["nbeam"], params["gulp"], params["nchan"]
+    gulp_s = G * params["tsamp"]
+    kw = dict(dynamic=True, inflight=2)
+    # admission: slots = the most that fit the HBM budget (here 3/4 of what all 64 requests need)
+    need = hg.batch_bytes(hg.default_params(**params), **kw)
+    budget = int(0.75 * need)
+    slots = NB
+    while slots > 1 and hg.batch_bytes(hg.default_params(**dict(params, nbeam=slots, hbm_budget=budget)),
+                                       **kw) > budget:
+        slots -= 1
+    rng = np.random.default_rng(7 + rank)
+    # requests: 48 beams from the start, 16 more at 25% of the run; 12 leave at 50%
+    join_at = {b: 0 if b < 48 else ngulps // 4 for b in range(NB)}
+    leave_at = {int(b): ngulps // 2 for b in rng.choice(48, 12, replace=False)}
+    kills = (rng.random((NB, nch)) >= rng.uniform(0, 0.1, (NB, 1))).astype(np.int32)
+
+    # all gulps of the run, drawn on the GPU into pinned host memory before timing
+    t_gen = time.perf_counter()
+    host = torch.empty((ngulps, NB, G, nch), dtype=torch.uint8, pin_memory=True)
+    buf = torch.empty((NB, G, nch), dtype=torch.uint8, device="cuda")
+    for g in range(ngulps):
+        sk = skies_at(g)
+        for b in range(NB):
+            synth.gulp_device(sk[b], g, G, out=buf[b])
+        host[g].copy_(buf)
+    del buf
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t_gen
+
+    member = np.zeros(slots, np.int32)
+    bt = hg.Batch(hg.default_params(**dict(params, nbeam=slots, device=local, hbm_budget=budget)),
+                  member=member, **kw)
+    slot_of, free, waiting = {}, list(range(slots)), []
+    admitted = refused_at_once = 0
+    lat, dev_ms, ncand, searched_beams = [], [], [], 0
+    pending = 0
+    lanes = [torch.empty((slots, G, nch), dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    for g in range(ngulps):
+        # membership changes need an idle batch: drain, then admit / release
+        changes = [b for b, t in leave_at.items() if t == g and b in slot_of]
+        arrivals = [b for b, t in join_at.items() if t == g]
+        if changes or arrivals or (waiting and free):
+            while pending:
+                got, counts, searched, l_ms, d_ms = bt.poll()
+                lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
+                searched_beams += int(searched.sum())
+                pending -= 1
+            for b in changes:
+                s = slot_of.pop(b)
+                bt.set_beam(s, False)
+                free.append(s)
+            for b in arrivals:
+                waiting.append(b)
+                if not free:
+                    refused_at_once += 1
+            while waiting and free:
+                b, s = waiting.pop(0), free.pop(0)
+                bt.set_beam(s, True, params["dm_max"], kills[b])
+                slot_of[b] = s
+                admitted += 1
+        # this gulp's data of the admitted beams, laid out by slot
+        lane = lanes[g % 2]
+        for b, s in slot_of.items():
+            lane[s].copy_(host[g, b])
+        bt.submit(lane.data_ptr())
+        pending += 1
+        if pending == 2:
+            got, counts, searched, l_ms, d_ms = bt.poll()
+            lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
+            searched_beams += int(searched.sum())
+            pending -= 1
+    while pending:
+        got, counts, searched, l_ms, d_ms = bt.poll()
+        lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
+        searched_beams += int(searched.sum())
+        pending -= 1
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    beam_gulps = searched_beams
+    value = beam_gulps * gulp_s / (float(np.sum(dev_ms)) / 1e3)
+    e2e = beam_gulps * gulp_s / wall
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": ngulps,
+        "warmup": 0, "ms_per_step": round(float(np.mean(dev_ms)), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded noise, drifting RFI, bursts 1 per beam per 30 s; drawn on the GPU)",
+        "config": {"workload": STREAM_WORKLOAD.format(sec=a.seconds), "beam_requests": NB,
+                   "slots_in_budget": slots, "hbm_budget_gb": round(budget / 1e9, 2), "admitted": admitted,
+                   "waited_for_a_slot": refused_at_once, "gulps": ngulps, "searched_beam_gulps": beam_gulps,
+                   "cadence": "gulps replayed back to back (no real-time wait); latency = submit to results",
+                   "gen_s": round(gen_s, 1), "parallelism": f"replicas{world}"},
+        "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": slots * G * nch,
+                "d2h_bytes_per_step": int(4 * slots + 20 * np.mean(ncand)),
+                "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                "p99_ms": round(float(np.percentile(lat, 99)), 2), "max_ms": round(float(np.max(lat)), 2),
+                "gulp_ms": round(gulp_s * 1e3, 1)},
+        "gpu_launches": None,
+        "clocks": clk,
+        "candidates_per_gulp": float(np.mean(ncand)),
+    }
+    try:
+        line["gpu_launches"] = int(ngulps * bt.graph_kernels())
+    except Exception:
+        pass
     bt.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -248,3 +248,40 @@ def config_batched(nbeam: int = 256, seed: int = 3, nchan: int = 1024, gulp: int
                   dm_min=0.0, dm_max=float(ceilings.max()), dm_tol=1.25, ti_us=40.0, width_min=1, width_max=64,
                   snr=7.0)
     return params, ceilings, kill, skies
+
+
+def config_stream(nbeam: int = 64, seconds: float = 600.0, seed: int = 4, nchan: int = 1024, gulp: int = 8192):
+    """Streaming serving loop: nbeam beams of 1024 ch, tsamp 1.048576 ms, gulps
+    of 8192 samples for `seconds` of sky.  RFI occupancy drifts between 0 and
+    20% of the channels over the run; each beam gets one burst per 30 s on
+    average (DM U[50, 2000], FWHM 2 ms, S/N 20).  Returns (params, ngulps,
+    skies_at) where skies_at(g) gives every beam's sky model for gulp g (its
+    RFI channels of that time)."""
+    rng = np.random.default_rng(seed)
+    tsamp = 1.048576e-3
+    df = -(F0 - FLO) / nchan
+    ngulps = int(math.ceil(seconds / (gulp * tsamp)))
+    per_gulp = gulp * tsamp / 30.0
+    skies = []
+    for b in range(nbeam):
+        sky = Sky(nchan, tsamp, F0, df, seed * 100000 + b, 128.0, 20.0, (), 80.0, 0.0, [], [])
+        for g in range(ngulps):
+            if rng.random() < per_gulp:
+                dm = float(rng.uniform(50.0, 2000.0))
+                sky.bursts.append(Burst(int(g * gulp + rng.integers(0, gulp)), dm, 2.0,
+                                        snr_amp(20.0, 20.0, nchan, 2.0, tsamp), 0.0))
+        skies.append(sky)
+    order = rng.permutation(nchan)
+    phase = rng.uniform(0, 2 * math.pi, nbeam)
+
+    def skies_at(g: int):
+        out = []
+        for b, sky in enumerate(skies):
+            occ = 0.10 + 0.10 * math.sin(2 * math.pi * g / max(1, ngulps) + phase[b])  # 0..20 %
+            k = int(round(occ * nchan))
+            out.append(dc.replace(sky, rfi_chans=tuple(int(c) for c in order[:k])))
+        return out
+
+    params = dict(nchan=nchan, nbeam=nbeam, gulp=gulp, tsamp=tsamp, plan_dt=tsamp, f0_mhz=F0, df_mhz=df,
+                  dm_min=0.0, dm_max=2000.0, dm_tol=1.25, ti_us=40.0, width_min=1, width_max=64, snr=7.0)
+    return params, ngulps, skies_at

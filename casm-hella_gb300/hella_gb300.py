@@ -58,6 +58,11 @@ class BatchParams(C.Structure):
                 ("member", C.c_void_p), ("inflight", C.c_int), ("bp_alpha", C.c_float)]
 
 
+class RefineParams(C.Structure):
+    _fields_ = [("ncut", C.c_int), ("nchan", C.c_int), ("nsamp", C.c_int), ("tsamp", C.c_double),
+                ("f0_mhz", C.c_double), ("df_mhz", C.c_double), ("device", C.c_int)]
+
+
 class HellaTuning(C.Structure):
     _fields_ = [("dm_per_block", C.c_int), ("samples_per_thread", C.c_int), ("chan_chunk", C.c_int),
                 ("stages", C.c_int), ("group", C.c_int), ("add_mode", C.c_int)]
@@ -165,6 +170,13 @@ def lib() -> C.CDLL:
     _sig(L, "hella_batch_set_beam", C.c_int, [_VP, C.c_int, C.c_int, C.c_float, _VP])
     _sig(L, "hella_batch_get_bandpass", C.c_int, [_VP, C.c_int, _VP])
     _sig(L, "hella_batch_bytes", C.c_int, [C.POINTER(BatchParams), C.POINTER(C.c_size_t)])
+    _sig(L, "hella_refine_create", C.c_int, [C.POINTER(_VP), C.POINTER(RefineParams)])
+    _sig(L, "hella_refine_destroy", None, [_VP])
+    _sig(L, "hella_refine_set_stream", C.c_int, [_VP, _VP])
+    _sig(L, "hella_refine_delay_table", C.c_int, [_VP, _VP])
+    _sig(L, "hella_refine_forward", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP])
+    _sig(L, "hella_refine_adjoint", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP])
+    _sig(L, "hella_refine_fit", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, C.c_int, _VP, _VP])
     _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
@@ -560,3 +572,48 @@ def batch_bytes(base: HellaParams, **kw) -> int:
     n = C.c_size_t()
     _chk(lib().hella_batch_bytes(C.byref(bp), C.byref(n)))
     return n.value
+
+
+# --------------------------------------------------------- candidate refinement
+
+class Refine:
+    """Differentiable candidate refinement (hella_refine_*).  Arguments are
+    CUDA tensors: cutouts f32 [n][nchan][nsamp], dm_ref f32 [n], theta f32
+    [n][5] = (dm, t0, width_ms, amp, index)."""
+
+    def __init__(self, ncut: int, nchan: int, nsamp: int, tsamp: float, f0_mhz: float, df_mhz: float,
+                 device: int = 0, stream: int | None = None):
+        self.L = lib()
+        p = RefineParams(ncut, nchan, nsamp, tsamp, f0_mhz, df_mhz, device)
+        h = _VP()
+        _chk(self.L.hella_refine_create(C.byref(h), C.byref(p)))
+        self.h, self.p = h, p
+        if stream is not None:
+            _chk(self.L.hella_refine_set_stream(self.h, stream))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_refine_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_stream(self, stream: int):
+        _chk(self.L.hella_refine_set_stream(self.h, stream))
+
+    def delay_table(self) -> np.ndarray:
+        out = np.zeros(self.p.nchan, np.float32)
+        _chk(self.L.hella_refine_delay_table(self.h, out.ctypes.data))
+        return out
+
+    def forward(self, cut, dm_ref, theta, chi2):
+        _chk(self.L.hella_refine_forward(self.h, theta.shape[0], _ptr(cut), _ptr(dm_ref), _ptr(theta), _ptr(chi2)))
+
+    def adjoint(self, cut, dm_ref, theta, gchi2, gtheta):
+        _chk(self.L.hella_refine_adjoint(self.h, theta.shape[0], _ptr(cut), _ptr(dm_ref), _ptr(theta), _ptr(gchi2),
+                                         _ptr(gtheta)))
+
+    def fit(self, cut, dm_ref, theta, steps: int, lr, chi2=None):
+        lr = np.ascontiguousarray(lr, dtype=np.float32)
+        _chk(self.L.hella_refine_fit(self.h, theta.shape[0], _ptr(cut), _ptr(dm_ref), _ptr(theta), steps,
+                                     lr.ctypes.data, _ptr(chi2)))

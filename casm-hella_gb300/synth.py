@@ -285,3 +285,66 @@ def config_stream(nbeam: int = 64, seconds: float = 600.0, seed: int = 4, nchan:
     params = dict(nchan=nchan, nbeam=nbeam, gulp=gulp, tsamp=tsamp, plan_dt=tsamp, f0_mhz=F0, df_mhz=df,
                   dm_min=0.0, dm_max=2000.0, dm_tol=1.25, ti_us=40.0, width_min=1, width_max=64, snr=7.0)
     return params, ngulps, skies_at
+
+
+def refine_truth(n: int, dm_grid: np.ndarray, nchan: int = 1024, nsamp: int = 2048, seed: int = 5,
+                 tsamp: float = 1.048576e-3):
+    """Candidate-refinement cutouts: n bursts with DM U[100,2000], FWHM
+    U[0.5,20] ms, band-integrated S/N U[6,40], spectral index U[-3,3], near
+    the cutout centre, in N(0,1) noise.  Each cutout is pre-dedispersed at
+    its detection DM (the nearest trial of dm_grid) and the fit starts from
+    the detection grid: that DM, the nearest boxcar width 2^k samples
+    (k = 0..5), the detection sample, amplitude within +-30% of the truth,
+    index 0.  Returns (theta_true [n,5], dm_ref [n], theta0 [n,5]) as f32,
+    theta = (dm, t0 samples, width ms, amp, index)."""
+    rng = np.random.default_rng(seed)
+    df = -(F0 - FLO) / nchan
+    fc = F0 - np.arange(nchan) * abs(df)
+    tab = (4.148808e3 / tsamp * (1.0 / fc**2 - 1.0 / F0**2)).astype(np.float32).astype(np.float64)
+    lnf = np.log(fc / F0)
+    dm = rng.uniform(100.0, 2000.0, n)
+    width = rng.uniform(0.5, 20.0, n)
+    snr = rng.uniform(6.0, 40.0, n)
+    idx = rng.uniform(-3.0, 3.0, n)
+    dm_ref = dm_grid[np.abs(dm_grid[None, :] - dm[:, None]).argmin(axis=1)].astype(np.float32)
+    sigma = width / (2.0 * math.sqrt(2.0 * math.log(2.0)) * tsamp * 1e3)
+    s2 = np.exp(2.0 * idx[:, None] * lnf[None, :]).sum(axis=1)
+    amp = snr / np.sqrt(s2 * sigma * math.sqrt(math.pi))
+    t0 = nsamp / 2 + rng.uniform(-8.0, 8.0, n)
+    resid = ((dm - dm_ref)[:, None] * tab[None, :]).mean(axis=1)
+    t_det = np.round(t0 + resid)
+    k = np.clip(np.round(np.log2(np.maximum(width / (tsamp * 1e3), 1.0))), 0, 5)
+    w_det = 2.0 ** k * tsamp * 1e3
+    truth = np.stack([dm, t0, width, amp, idx], axis=1).astype(np.float32)
+    theta0 = np.stack([dm_ref, t_det, w_det, amp * rng.uniform(0.7, 1.3, n), np.zeros(n)], axis=1)
+    return truth, dm_ref, theta0.astype(np.float32)
+
+
+def refine_cutouts_device(truth: np.ndarray, dm_ref: np.ndarray, nchan: int, nsamp: int, out, seed: int = 6,
+                          tsamp: float = 1.048576e-3, chunk: int = 32):
+    """Fills the CUDA tensor out [n][nchan][nsamp] with model(truth) +
+    N(0,1), evaluated with torch on the GPU in fp32 (the refinement model of
+    include/hella_refine.h, pre-dedispersed at dm_ref)."""
+    import torch
+
+    df = -(F0 - FLO) / nchan
+    fc = F0 - np.arange(nchan) * abs(df)
+    tab32 = (4.148808e3 / tsamp * (1.0 / fc**2 - 1.0 / F0**2)).astype(np.float32)
+    tab = torch.from_numpy(tab32).cuda()
+    lnf = torch.from_numpy(np.log(fc / F0).astype(np.float32)).cuda()
+    t = torch.arange(nsamp, device="cuda", dtype=torch.float32)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    c_w = 1.0 / (2.0 * math.sqrt(2.0 * math.log(2.0)) * tsamp * 1e3)
+    th = torch.from_numpy(truth).cuda()
+    dr = torch.from_numpy(dm_ref).cuda()
+    for a in range(0, truth.shape[0], chunk):
+        b = min(a + chunk, truth.shape[0])
+        dm, t0, w, amp, idx = (th[a:b, k] for k in range(5))
+        off = torch.floor(dr[a:b, None] * tab[None, :] + 0.5)
+        mu = t0[:, None] + dm[:, None] * tab[None, :] - off
+        sig = (w * c_w)[:, None, None]
+        u = (t[None, None, :] - mu[:, :, None]) / sig
+        m = (amp[:, None] * torch.exp(idx[:, None] * lnf[None, :]))[:, :, None] * torch.exp(-0.5 * u * u)
+        out[a:b] = m + torch.randn(m.shape, generator=gen, device="cuda")
+    return out

@@ -29,6 +29,7 @@ constexpr int kWarps = 8;
 constexpr int kChPerWarp = 2;
 constexpr int kChPerBlock = kWarps * kChPerWarp;
 constexpr int kNp = 6;  // chi2 + 5 gradient partials
+constexpr int kLoads = 4;  // float4 loads per lane per round
 
 struct RefineArgs {
   const float *cut;     // [n][nchan][nsamp]
@@ -71,20 +72,29 @@ __global__ void __launch_bounds__(kWarps * 32) k_refine(RefineArgs a) {
     const float b = __fmul_rn(-mu, inv);
     const float4 *row = reinterpret_cast<const float4 *>(a.cut + ((size_t)i * a.nchan + c) * a.nsamp);
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-    for (int q = lane; q < a.nsamp / 4; q += 32) {
-      const float4 d4 = __ldcs(row + q);  // streamed: read once per pass
-      const float dv[4] = {d4.x, d4.y, d4.z, d4.w};
+    const int nq = a.nsamp / 4;
+    for (int q0 = lane; q0 < nq; q0 += 32 * kLoads) {
+      float4 d4[kLoads];  // kLoads independent 16-byte loads in flight per lane
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float u = __fmaf_rn((float)(4 * q + k), inv, b);
-        const float e = exp2f(__fmul_rn(-0.72134752f, __fmul_rn(u, u)));  // exp(-u^2/2)
-        const float r = __fsub_rn(dv[k], __fmul_rn(sc, e));
-        s0 = __fmaf_rn(r, r, s0);
-        if (GRAD) {
-          const float re = __fmul_rn(r, e);
-          s1 = __fadd_rn(s1, re);
-          s2 = __fmaf_rn(re, u, s2);
-          s3 = __fmaf_rn(__fmul_rn(re, u), u, s3);
+      for (int l = 0; l < kLoads; ++l)
+        d4[l] = q0 + 32 * l < nq ? __ldcs(row + q0 + 32 * l) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int l = 0; l < kLoads; ++l) {
+        const int q = q0 + 32 * l;
+        if (q >= nq) break;
+        const float dv[4] = {d4[l].x, d4[l].y, d4[l].z, d4[l].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float u = __fmaf_rn((float)(4 * q + k), inv, b);
+          const float e = exp2f(__fmul_rn(-0.72134752f, __fmul_rn(u, u)));  // exp(-u^2/2)
+          const float r = __fsub_rn(dv[k], __fmul_rn(sc, e));
+          s0 = __fmaf_rn(r, r, s0);
+          if (GRAD) {
+            const float re = __fmul_rn(r, e);
+            s1 = __fadd_rn(s1, re);
+            s2 = __fmaf_rn(re, u, s2);
+            s3 = __fmaf_rn(__fmul_rn(re, u), u, s3);
+          }
         }
       }
     }

@@ -269,6 +269,7 @@ hella_status batch_sizes(const hella_batch_params *bp, hdd_plan *plan_out, Sizes
   const size_t lanes = bp->inflight == 2 ? 2 : 1;
   z->fixed = lanes * (size_t)nb * p.gulp * nch + (size_t)nb * nch * R * 5 + (size_t)nb * nch * 5 +
              (size_t)nb * nch * (256 * 6 + 16) + (size_t)nb * p.gulp * 6 + dd_floats * 4 + rows * z->nbox * 20 +
+             (p.nscrunch > 0 ? (size_t)nb * nch * ((size_t)p.gulp * 6 + 8) : 0) + (size_t)nch * 4 +
              (size_t)nb * cap * 20 + lanes * (size_t)nb * cap * sizeof(hella_cand) + (size_t)nb * 512;
   z->per_width = rows * z->ntime_out * 4;
   *plan_out = plan;
@@ -644,6 +645,15 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   DA(f.flag2, (size_t)nb * nch);
   DA(f.ts, (size_t)nb * p->gulp * 4);
   DA(f.hts, (size_t)nb * p->gulp * 2);
+  hg::flag_scrunch_params(*p, &f);
+  if (p->nscrunch > 0) {
+    DA(f.P, (size_t)nb * nch * p->gulp * 2);
+    DA(f.M, (size_t)nb * nch * p->gulp * 2);
+    DA(f.S, (size_t)nb * nch * p->gulp * 2);
+    DA(f.bpx, (size_t)nb * nch * 4);
+    DA(f.fsb, (size_t)nb * nch * 4);
+  }
+  DA(f.flagspec, (size_t)nch * 4);
   DA(b->d_dd, dd_floats * 4);
   DA(b->d_boxes, z.per_width * b->nwp);
   const size_t rw = rows * z.nbox;
@@ -688,6 +698,7 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
       cudaMemset(b->d_plain, 0, (size_t)nb * nch * R) != cudaSuccess ||
       cudaMemset(b->d_packed, 0, (size_t)nb * nch * R * 4) != cudaSuccess ||
       cudaMemset(b->d_ew, 0, (size_t)nb * nch * 4) != cudaSuccess ||
+      cudaMemset(f.flagspec, 0, (size_t)nch * 4) != cudaSuccess ||
       cudaMemset(b->d_err, 0, 16) != cudaSuccess || cudaMemset(b->d_total, 0, (size_t)nb * 4) != cudaSuccess ||
       cudaDeviceSynchronize() != cudaSuccess) {
     cudaGetLastError();
@@ -745,6 +756,13 @@ hella_status hella_batch_set_beam(hella_batch *b, int beam, int member, float dm
   }
   b->member[beam] = member != 0;
   return upload_layout(b);
+}
+
+hella_status hella_batch_get_flag_spec(hella_batch *b, float *out) {
+  if (!b || !out) return HELLA_ERR_INVALID_ARG;
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaMemcpy(out, b->fs.flagspec, (size_t)b->p.nchan * 4, cudaMemcpyDeviceToHost));
+  return HELLA_OK;
 }
 
 hella_status hella_batch_get_bandpass(hella_batch *b, int beam, float *out) {

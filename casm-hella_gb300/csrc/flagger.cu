@@ -23,6 +23,9 @@
 #include "hg_internal.h"
 #include "hella_search.h"
 
+#include <algorithm>
+#include <cmath>
+
 namespace hg {
 namespace {
 
@@ -107,6 +110,7 @@ __global__ void k_lane_finish(FlagState st, int mode) {
       st.flag2[gw] = (bp < st.spec_min || bp > st.spec_max) ? 1 : 0;
     }
     if (mode == 2) st.bp3[gw] = bp;
+    if (mode == 3) st.bpx[gw] = bp;
   }
 }
 
@@ -260,6 +264,256 @@ __global__ void k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
 }  // namespace
 
 namespace {
+// ------------------------------------------------ SCRUNCH entries (planes)
+// Kernels of the plane path, each the counterpart of a reference kernel run
+// on the fp16 copy of the gulp; index `i` runs over [nbeam][nchan][gulp].
+
+// The data after bandpass_flag (table stage 3) as a channel-major plane.
+__global__ void k_plane_init(const uint8_t *__restrict__ gulp, FlagState st) {
+  __shared__ uint8_t tile[32][33];
+  const int b = blockIdx.z, c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y, nchan = st.nchan, w = st.gulp;
+  const uint8_t *g = gulp + (size_t)b * w * nchan;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) tile[ty + j][tx] = g[(size_t)(t0 + ty + j) * nchan + c0 + tx];
+  __syncthreads();
+  const __half *lb = st.lut + (size_t)b * nchan * 256;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int c = c0 + ty + j;
+    st.P[((size_t)b * nchan + c) * w + t0 + tx] = lb[(size_t)c * 256 + tile[tx][ty + j]];
+  }
+}
+
+// calc_bandpass_new partials of the plane (lane l: samples l, l+32, ...).
+// One warp per (beam, channel).
+__global__ void k_plane_lanes(FlagState st) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (gw >= st.nbeam * st.nchan) return;
+  const __half *p = st.P + (size_t)gw * st.gulp + lane;
+  const int np = st.gulp / 32;
+  float s = 0.f;
+  for (int i = 0; i < np; ++i) s = __fadd_rn(s, __half2float(p[(size_t)i * 32]));
+  st.part[(size_t)gw * 32 + lane] = s;
+}
+
+// divide_by_bp (flagger.cu:180-194) with bandpass bp [nbeam][nchan].
+__global__ void k_plane_div(FlagState st, const float *bp) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = bp[i / st.gulp];
+    st.P[i] = v > 0.f ? __hdiv(st.P[i], __float2half_rn(v)) : hzero();
+  }
+}
+
+// computeRowMeans / computeRowVariances partials of the plane.
+template <bool VAR>
+__global__ void __launch_bounds__(256) k_plane_rows(FlagState st, int which) {
+  const int c = blockIdx.x, b = blockIdx.y, j = threadIdx.x, w = st.gulp;
+  const __half *p = st.P + ((size_t)b * st.nchan + c) * w + j;
+  const float mean = VAR ? st.scal[b * 8 + 2 * which] : 0.f;
+  float s = 0.f;
+  for (int k = 0; k < w / 256; ++k) {
+    const float f = __half2float(p[(size_t)k * 256]);
+    if (VAR) {
+      const float d = __fsub_rn(f, mean);
+      s = __fmaf_rn(d, d, s);
+    } else {
+      s = __fadd_rn(s, f);
+    }
+  }
+  st.part[((size_t)b * st.nchan + c) * 256 + j] = s;
+}
+
+// normalize_data (flagger.cu:198-214) with the constants of slot `which`.
+__global__ void k_plane_norm(FlagState st, int which) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp, per = (size_t)st.nchan * st.gulp;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(i / per);
+    st.P[i] = __hmul(__hadd(st.P[i], st.hsc[b * 8 + 2 * which]), st.hsc[b * 8 + 2 * which + 1]);
+  }
+}
+
+// npp_convolve_handler (convolution.cu:20-55): an xw (time) x yw (channel)
+// box of equal taps k, anchor (xw/2, yw/2), replicate border, fp32 sum of
+// fp16 input, fp16 output.  Tap (j, i) multiplies input (c + ay - j,
+// t + ax - i); the sum runs j outer, i inner, one fmaf per tap.  A block
+// computes 64 samples x 16 channels from a staged halo tile.
+constexpr int kBoxT = 64, kBoxC = 16;
+__global__ void __launch_bounds__(256) k_box(const __half *__restrict__ in, __half *__restrict__ out,
+                                             int nchan, int w, int xw, int yw, float k) {
+  extern __shared__ float tile[];
+  const int b = blockIdx.z, t0 = blockIdx.x * kBoxT, c0 = blockIdx.y * kBoxC, tid = threadIdx.x;
+  const int ax = xw / 2, ay = yw / 2;
+  const int tw = kBoxT + xw - 1, th = kBoxC + yw - 1;
+  const int cb = c0 + ay - (yw - 1), tb = t0 + ax - (xw - 1);  // tile origin (before clamping)
+  const __half *src = in + (size_t)b * nchan * w;
+  for (int q = tid; q < tw * th; q += 256) {
+    const int r = q / tw, col = q - r * tw;
+    const int cc = min(max(cb + r, 0), nchan - 1), tt = min(max(tb + col, 0), w - 1);
+    tile[q] = __half2float(src[(size_t)cc * w + tt]);
+  }
+  __syncthreads();
+  const int tl = tid & (kBoxT - 1);
+  for (int cl = tid >> 6; cl < kBoxC; cl += 256 / kBoxT) {
+    const int c = c0 + cl, t = t0 + tl;
+    float acc = 0.f;
+    for (int j = 0; j < yw; ++j) {
+      const float *row = tile + (size_t)(cl + yw - 1 - j) * tw + tl + xw - 1;
+      for (int i = 0; i < xw; ++i) acc = __fmaf_rn(k, row[-i], acc);
+    }
+    if (c < nchan && t < w) out[((size_t)b * nchan + c) * w + t] = __float2half_rn(acc);
+  }
+}
+
+// threshold_data (flagger.cu:162-176): mask 1 where the smoothed value
+// exceeds +-half(thr).
+__global__ void k_plane_thresh(FlagState st, __half hp, __half hn) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
+  const float p = __half2float(hp), m = __half2float(hn);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = __half2float(st.S[i]);
+    st.M[i] = (v > p || v < m) ? hone() : hzero();
+  }
+}
+
+// replace_data (flagger.cu:128-144) with FLAG1/FLAG2, then add_number 1.
+__global__ void k_plane_replace(FlagState st) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)((i / st.gulp) % st.nchan);
+    __half v = st.P[i];
+    if (__half2float(st.S[i]) > 0.f) v = hzero();
+    if (c >= st.flag_lo && c < st.flag_hi) v = hzero();
+    st.P[i] = __hadd(v, hone());
+  }
+}
+
+// calc_bandpass (flagger.cu:50-81) of the grown mask: thread t sums its
+// contiguous floor(w/256) samples in fp16, / half(256 floor(w/256)), then an
+// fp16 tree.  Block = (channel, beam).
+__global__ void __launch_bounds__(256) k_plane_bp16(FlagState st) {
+  __shared__ __half ps[256];
+  const int c = blockIdx.x, b = blockIdx.y, t = threadIdx.x, np = st.gulp / 256;
+  const __half *p = st.S + ((size_t)b * st.nchan + c) * st.gulp + (size_t)t * np;
+  __half s = hzero();
+  for (int i = 0; i < np; ++i) s = __hadd(s, p[i]);
+  ps[t] = __hdiv(s, __float2half_rn((float)(256 * np)));
+  __syncthreads();
+  for (int h = 128; h >= 1; h /= 2) {
+    if (t < h) ps[t] = __hadd(ps[t], ps[t + h]);
+    __syncthreads();
+  }
+  if (t == 0) st.fsb[(size_t)b * st.nchan + c] = __half2float(ps[0]);
+}
+
+// add_bandpass into d_flagSpec (flagger.cu:333-334), beams in order.
+__global__ void k_flagspec_add(FlagState st) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= st.nchan) return;
+  float f = st.flagspec[c];
+  for (int b = 0; b < st.nbeam; ++b) f = __fadd_rn(f, st.fsb[(size_t)b * st.nchan + c]);
+  st.flagspec[c] = f;
+}
+
+// measure_ts + divide_by_ts (timeseries.cu:19-55) on the plane.
+__global__ void k_plane_ts(FlagState st) {
+  const int b = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x, w = st.gulp;
+  if (t >= w) return;
+  const __half *p = st.P + (size_t)b * st.nchan * w + t;
+  __half s = hzero();
+  for (int c = 0; c < st.nchan; ++c) s = __hadd(s, p[(size_t)c * w]);
+  const float ts = __fdiv_rn(__half2float(s), (float)st.nchan);
+  st.ts[(size_t)b * w + t] = ts;
+  st.hts[(size_t)b * w + t] = __float2half_rn(ts);
+}
+
+__global__ void k_plane_tsdiv(FlagState st) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp, per = (size_t)st.nchan * st.gulp;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = i / per, t = i % st.gulp;
+    st.P[i] = __hdiv(st.P[i], st.hts[b * st.gulp + t]);
+  }
+}
+
+// transpose_output of the plane into the channel-major ring.
+__global__ void k_plane_out(FlagState st, uint8_t *__restrict__ plain, long R, long wpos, const GulpPos *dpos) {
+  if (dpos) wpos = dpos->wpos;
+  const int b = blockIdx.z, c = blockIdx.y, w = st.gulp;
+  const __half *p = st.P + ((size_t)b * st.nchan + c) * w;
+  uint8_t *row = plain + ((size_t)b * st.nchan + c) * R;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w; t += gridDim.x * blockDim.x) {
+    long pos = wpos + t;
+    if (pos >= R) pos -= R;
+    row[pos] = requant(p[t]);
+  }
+}
+
+}  // namespace
+
+namespace {
+
+// SCRUNCH entries and the final scrunch on fp16 planes (flagger.cu:365-401),
+// from the data after bandpass_flag.
+cudaError_t scrunch_planes(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+                           const GulpPos *dpos, cudaStream_t s) {
+  const dim3 lutg(st.nchan, st.nbeam);
+  const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
+  const int beam_blocks = (st.nbeam + 63) / 64;
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
+  const int eb = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  const dim3 chg(st.nchan, st.nbeam);
+  unsigned launches = 0;
+  auto normalize = [&](int which) {
+    k_plane_rows<false><<<chg, 256, 0, s>>>(st, which);
+    k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+    k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, which);
+    k_plane_rows<true><<<chg, 256, 0, s>>>(st, which);
+    k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
+    k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, which);
+    k_plane_norm<<<eb, 256, 0, s>>>(st, which);
+    launches += 7;
+  };
+  auto bandpass_correct = [&](int mode, const float *bp) {
+    k_plane_lanes<<<fin_blocks, 256, 0, s>>>(st);
+    k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, mode);
+    k_plane_div<<<eb, 256, 0, s>>>(st, bp);
+    launches += 3;
+  };
+  k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
+  k_plane_init<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(gulp, st);
+  launches += 2;
+  for (int e = 0; e < st.nscrunch; ++e) {
+    const int xw = st.sc_t[e], yw = st.sc_f[e];
+    bandpass_correct(3, st.bpx);
+    normalize(2);
+    const float k = (float)(1. / xw / yw);
+    const float thr = (float)(st.sc_thresh[e] / std::sqrt(1. * xw * yw));
+    const __half hp = __float2half_rn(thr), hn = __float2half_rn((float)(-1. * thr));
+    const dim3 bg((st.gulp + kBoxT - 1) / kBoxT, (st.nchan + kBoxC - 1) / kBoxC, st.nbeam);
+    const size_t smem = sizeof(float) * (size_t)(kBoxT + xw - 1) * (kBoxC + yw - 1);
+    k_box<<<bg, 256, smem, s>>>(st.P, st.S, st.nchan, st.gulp, xw, yw, k);
+    k_plane_thresh<<<eb, 256, 0, s>>>(st, hp, hn);
+    k_box<<<bg, 256, smem, s>>>(st.M, st.S, st.nchan, st.gulp, xw, yw, k);
+    k_plane_replace<<<eb, 256, 0, s>>>(st);
+    launches += 4;
+    if (st.flagspec) {
+      k_plane_bp16<<<chg, 256, 0, s>>>(st);
+      k_flagspec_add<<<(st.nchan + 255) / 256, 256, 0, s>>>(st);
+      launches += 2;
+    }
+  }
+  // apply_scrunch(8, 8, 100, flag=0, ts=1)
+  bandpass_correct(2, st.bp3);
+  k_plane_ts<<<dim3((st.gulp + 127) / 128, st.nbeam), 128, 0, s>>>(st);
+  k_plane_tsdiv<<<eb, 256, 0, s>>>(st);
+  normalize(1);
+  k_plane_out<<<dim3((st.gulp + 1023) / 1024, st.nchan, st.nbeam), 256, 0, s>>>(st, plain, R, wpos, dpos);
+  launches += 3;
+  count_launches(launches);
+  return cudaGetLastError();
+}
+
 cudaError_t flag_impl(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
                       const GulpPos *dpos, cudaStream_t s) {
   const dim3 lutg(st.nchan, st.nbeam);
@@ -284,6 +538,10 @@ cudaError_t flag_impl(const FlagState &st, const uint8_t *gulp, uint8_t *plain, 
   k_build_lut<<<lutg, 256, 0, s>>>(st, 2);
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
   k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 1);
+  if (st.nscrunch > 0) {
+    count_launches(11);
+    return scrunch_planes(st, gulp, plain, R, wpos, dpos, s);
+  }
   // apply_scrunch(8,8,100,flag=0,ts=1): bandpass_correct ...
   k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);

@@ -46,7 +46,20 @@ struct FlagState {
   uint8_t *flag2;           // [nbeam][nchan] spectral flag decision
   float *ts;                // [nbeam][gulp]
   __half *hts;              // [nbeam][gulp]
+  // SCRUNCH entries (apply_scrunch with flag = 1, flagger.cu:271-343): the
+  // data stop being a function of (channel, u8 level), so the flagger then
+  // keeps fp16 planes [nbeam][nchan][gulp] (channel-major) instead
+  int nscrunch;
+  int sc_t[16], sc_f[16];   // time and channel widths of each entry
+  float sc_thresh[16];
+  int flag_lo, flag_hi;     // FLAG1 / FLAG2: channels [lo, hi) zeroed by each entry
+  __half *P, *M, *S;        // data, threshold mask, box-filtered plane
+  float *bpx;               // [nbeam][nchan] bandpass of an entry
+  float *fsb;               // [nbeam][nchan] flag fractions of an entry
+  float *flagspec;          // [nchan] flag fractions accumulated over beams and gulps
 };
+// Largest SCRUNCH widths the box filter stages in shared memory.
+constexpr int kMaxScrunch = 64;
 
 // Runs the whole parity flagger for all beams of `gulp` (u8 [nbeam][gulp]
 // [nchan]) and writes the requantised output into the plain ring at ring

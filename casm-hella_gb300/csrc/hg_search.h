@@ -3,6 +3,7 @@
 #pragma once
 
 #include "hella_search.h"
+#include "hg_internal.h"
 
 #include <vector>
 
@@ -14,5 +15,7 @@ hella_status validate_params(const hella_params *p);
 // padded to a multiple of 16: concatenated taps, offsets and padded counts.
 void smoothing_taps(const hella_params &p, int nbox, std::vector<float> *taps, std::vector<int> *off,
                     std::vector<int> *n);
+// SCRUNCH entries and FLAG1/FLAG2 of the configuration into the flagger state.
+void flag_scrunch_params(const hella_params &p, FlagState *f);
 
 }  // namespace hg

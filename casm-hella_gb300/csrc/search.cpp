@@ -70,8 +70,25 @@ hella_status validate_params(const hella_params *p) {
     return HELLA_ERR_INVALID_ARG;
   if (p->max_giants < 1) return HELLA_ERR_INVALID_ARG;
   if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
-  if (p->nscrunch != 0) return HELLA_ERR_INVALID_ARG;  // scrunch flagging: not in this build
+  if (p->nscrunch < 0 || p->nscrunch > HELLA_MAX_SCRUNCH) return HELLA_ERR_INVALID_ARG;
+  for (int i = 0; i < p->nscrunch; ++i) {
+    const hella_scrunch &sc = p->scrunch[i];
+    if (sc.tscrunch < 1 || sc.tscrunch > kMaxScrunch || sc.fscrunch < 1 || sc.fscrunch > kMaxScrunch ||
+        !(sc.thresh > 0.f) || !(sc.thresh < 3.0e38f))
+      return HELLA_ERR_INVALID_ARG;
+  }
   return HELLA_OK;
+}
+
+void flag_scrunch_params(const hella_params &p, FlagState *f) {
+  f->nscrunch = p.nscrunch;
+  for (int i = 0; i < p.nscrunch; ++i) {
+    f->sc_t[i] = p.scrunch[i].tscrunch;
+    f->sc_f[i] = p.scrunch[i].fscrunch;
+    f->sc_thresh[i] = p.scrunch[i].thresh;
+  }
+  f->flag_lo = p.flag1;
+  f->flag_hi = p.flag2;
 }
 
 }  // namespace hg
@@ -313,6 +330,7 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
 
   const size_t nb = p->nbeam, nch = p->nchan, R = c->R, h = c->ndms - 2;
   const size_t need = nb * p->gulp * nch + nb * nch * R * 5 + nb * nch * (256 * 6 + 16) +
+                      (p->nscrunch > 0 ? nb * nch * (p->gulp * 6 + 8) : 0) +
                       nb * p->gulp * 6 + (size_t)c->ndms * c->ntime_dd * 4 +
                       (size_t)c->nbox * h * c->ntime_out * 4 + (size_t)c->nbox * h * 20 +
                       (size_t)p->max_giants * 20;
@@ -341,6 +359,14 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   DA(f.flag2, nb * nch);
   DA(f.ts, nb * p->gulp * 4);
   DA(f.hts, nb * p->gulp * 2);
+  hg::flag_scrunch_params(*p, &f);
+  if (p->nscrunch > 0) {
+    DA(f.P, nb * nch * p->gulp * 2);
+    DA(f.M, nb * nch * p->gulp * 2);
+    DA(f.S, nb * nch * p->gulp * 2);
+    DA(f.bpx, nb * nch * 4);
+    DA(f.fsb, nb * nch * 4);
+  }
   DA(c->d_dd, (size_t)c->ndms * c->ntime_dd * 4);
   DA(c->d_boxes, (size_t)c->nbox * h * c->ntime_out * 4);
   DA(c->d_rowmean, c->nbox * h * 4);
@@ -349,6 +375,7 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   DA(c->d_stats, c->nbox * 16);
   DA(c->d_gate, 16);
   DA(c->d_flagspec, nch * 4);
+  f.flagspec = c->d_flagspec;
   DA(c->d_counts, c->nbox * h * 4);
   DA(c->d_offsets, c->nbox * h * 4);
   DA(c->d_total, 16);

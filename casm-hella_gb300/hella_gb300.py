@@ -169,6 +169,7 @@ def lib() -> C.CDLL:
                                            C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "hella_batch_set_beam", C.c_int, [_VP, C.c_int, C.c_int, C.c_float, _VP])
     _sig(L, "hella_batch_get_bandpass", C.c_int, [_VP, C.c_int, _VP])
+    _sig(L, "hella_batch_get_flag_spec", C.c_int, [_VP, _VP])
     _sig(L, "hella_batch_bytes", C.c_int, [C.POINTER(BatchParams), C.POINTER(C.c_size_t)])
     _sig(L, "hella_refine_create", C.c_int, [C.POINTER(_VP), C.POINTER(RefineParams)])
     _sig(L, "hella_refine_destroy", None, [_VP])
@@ -486,6 +487,11 @@ class Batch:
     def set_beam(self, beam: int, member: bool, dm_max: float = 0.0, killmask=None):
         km = None if killmask is None else np.ascontiguousarray(killmask, dtype=np.int32)
         _chk(self.L.hella_batch_set_beam(self.h, beam, int(member), dm_max, None if km is None else km.ctypes.data))
+
+    def flag_spec(self) -> np.ndarray:
+        out = np.zeros(self.base.nchan, np.float32)
+        _chk(self.L.hella_batch_get_flag_spec(self.h, out.ctypes.data))
+        return out
 
     def bandpass(self, beam: int) -> np.ndarray:
         out = np.zeros(self.base.nchan, np.float32)

@@ -69,7 +69,8 @@ typedef struct {
   float snr;        /* SNR */
   float spec_min, spec_max;     /* SPEC_MIN / SPEC_MAX (-0.05 / 0.15) */
   int flag1, flag2;             /* FLAG1 / FLAG2 (-1 / -1) */
-  int nscrunch;                 /* SCRUNCH n */
+  int nscrunch;                 /* SCRUNCH entries (each: flag with a tscrunch x
+                                   fscrunch box at thresh; widths 1..64) */
   hella_scrunch scrunch[HELLA_MAX_SCRUNCH];
   int max_giants;   /* candidate cap per gulp (MAX_GIANTS) */
   int beam0;        /* BEAM0, added to reported beam indices */
@@ -244,6 +245,9 @@ hella_status hella_batch_set_beam(hella_batch *b, int beam, int member, float dm
  * (weight bp_alpha for the newest gulp) of calc_bandpass_new over the gulps
  * since the slot joined; fp32 [nchan]. */
 hella_status hella_batch_get_bandpass(hella_batch *b, int beam, float *out);
+/* Accumulated per-channel flag fractions of the SCRUNCH entries over all
+ * beams and gulps (d_flagSpec, flagger.cu:333-334), fp32 [nchan]. */
+hella_status hella_batch_get_flag_spec(hella_batch *b, float *out);
 /* Device bytes a batch with these parameters would hold (admission by HBM
  * budget: size nbeam so that this stays within the budget). */
 hella_status hella_batch_bytes(const hella_batch_params *p, size_t *bytes);

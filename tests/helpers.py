@@ -11,7 +11,8 @@ def oracle_pipeline(oracle, params: dict, **over):
         f0=p["f0_mhz"], df=p["df_mhz"], dm_min=p["dm_min"], dm_max=p["dm_max"], dm_tol=p["dm_tol"],
         ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
         max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
-        spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15))
+        spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15), flag1=p.get("flag1", -1),
+        flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()))
 
 
 def small_params(**over):

@@ -267,9 +267,10 @@ hella_status batch_sizes(const hella_batch_params *bp, hdd_plan *plan_out, Sizes
   }
   const size_t R = z->R, cap = p.max_giants;
   const size_t lanes = bp->inflight == 2 ? 2 : 1;
-  z->fixed = lanes * (size_t)nb * p.gulp * nch + (size_t)nb * nch * R * 5 + (size_t)nb * nch * 5 +
+  z->fixed = lanes * hg::gulp_bytes(p) + (size_t)nb * nch * R * 5 + (size_t)nb * nch * 5 +
              (size_t)nb * nch * (256 * 6 + 16) + (size_t)nb * p.gulp * 6 + dd_floats * 4 + rows * z->nbox * 20 +
-             (p.nscrunch > 0 ? (size_t)nb * nch * ((size_t)p.gulp * 6 + 8) : 0) + (size_t)nch * 4 +
+             (p.nscrunch > 0 || p.input_format ? (size_t)nb * nch * ((size_t)p.gulp * 6 + 8) : 0) +
+             (size_t)nch * 4 +
              (size_t)nb * cap * 20 + lanes * (size_t)nb * cap * sizeof(hella_cand) + (size_t)nb * 512;
   z->per_width = rows * z->ntime_out * 4;
   *plan_out = plan;
@@ -615,7 +616,7 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   if ((s = dalloc(b, (void **)&(ptr), (bytes))) != HELLA_OK) return fail(s);
   b->lanes.resize(bp->inflight);
   for (Lane &l : b->lanes) {
-    DA(l.d_gulp, (size_t)nb * p->gulp * nch);
+    DA(l.d_gulp, hg::gulp_bytes(*p));
     DA(l.d_out, (size_t)nb * cap * sizeof(hella_cand));
     if ((s = halloc(b, (void **)&l.h_total, (size_t)nb * 4)) != HELLA_OK) return fail(s);
     if (cudaEventCreate(&l.copied) != cudaSuccess || cudaEventCreate(&l.t0) != cudaSuccess ||
@@ -646,7 +647,7 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   DA(f.ts, (size_t)nb * p->gulp * 4);
   DA(f.hts, (size_t)nb * p->gulp * 2);
   hg::flag_scrunch_params(*p, &f);
-  if (p->nscrunch > 0) {
+  if (p->nscrunch > 0 || f.f16_input) {
     DA(f.P, (size_t)nb * nch * p->gulp * 2);
     DA(f.M, (size_t)nb * nch * p->gulp * 2);
     DA(f.S, (size_t)nb * nch * p->gulp * 2);
@@ -783,7 +784,7 @@ hella_status hella_batch_submit(hella_batch *b, const uint8_t *gulp, int on_devi
   l.submitted = now_ms();
   // the input copy waits for the last search that read this lane's buffers
   CK(cudaStreamWaitEvent(b->copy_stream, l.t1, 0));
-  const size_t bytes = (size_t)b->nbeam * b->p.gulp * b->p.nchan;
+  const size_t bytes = hg::gulp_bytes(b->p);
   CK(cudaMemcpyAsync(l.d_gulp, gulp, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                      b->copy_stream));
   CK(cudaEventRecord(l.copied, b->copy_stream));

@@ -407,6 +407,14 @@ __global__ void __launch_bounds__(256) k_plane_bp16(FlagState st) {
   if (t == 0) st.fsb[(size_t)b * st.nchan + c] = __half2float(ps[0]);
 }
 
+// replace_data_and_add_bandpass (flagger.cu:146-158): flagged channels 1,
+// the others x + 1.
+__global__ void k_plane_spec(FlagState st) {
+  const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    st.P[i] = st.flag2[i / st.gulp] ? hone() : __hadd(st.P[i], hone());
+}
+
 // add_bandpass into d_flagSpec (flagger.cu:333-334), beams in order.
 __global__ void k_flagspec_add(FlagState st) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -455,7 +463,7 @@ namespace {
 
 // SCRUNCH entries and the final scrunch on fp16 planes (flagger.cu:365-401),
 // from the data after bandpass_flag.
-cudaError_t scrunch_planes(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+cudaError_t scrunch_planes(const FlagState &st, const void *gulp, uint8_t *plain, long R, long wpos,
                            const GulpPos *dpos, cudaStream_t s) {
   const dim3 lutg(st.nchan, st.nbeam);
   const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
@@ -480,9 +488,22 @@ cudaError_t scrunch_planes(const FlagState &st, const uint8_t *gulp, uint8_t *pl
     k_plane_div<<<eb, 256, 0, s>>>(st, bp);
     launches += 3;
   };
-  k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
-  k_plane_init<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(gulp, st);
-  launches += 2;
+  if (st.f16_input) {
+    // the DADA path (transpose.cu:87-90): the gulp is the fp16 plane; bandpass_flag on it
+    cudaError_t e = cudaMemcpyAsync(st.P, gulp, n * sizeof(__half), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    bandpass_correct(0, st.bp1);
+    normalize(0);
+    k_plane_lanes<<<fin_blocks, 256, 0, s>>>(st);
+    k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 1);
+    k_plane_spec<<<eb, 256, 0, s>>>(st);
+    launches += 3;
+  } else {
+    k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
+    k_plane_init<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(
+        static_cast<const uint8_t *>(gulp), st);
+    launches += 2;
+  }
   for (int e = 0; e < st.nscrunch; ++e) {
     const int xw = st.sc_t[e], yw = st.sc_f[e];
     bandpass_correct(3, st.bpx);
@@ -514,8 +535,10 @@ cudaError_t scrunch_planes(const FlagState &st, const uint8_t *gulp, uint8_t *pl
   return cudaGetLastError();
 }
 
-cudaError_t flag_impl(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, long R, long wpos,
                       const GulpPos *dpos, cudaStream_t s) {
+  if (st.f16_input) return scrunch_planes(st, gulp_in, plain, R, wpos, dpos, s);
+  const uint8_t *gulp = static_cast<const uint8_t *>(gulp_in);
   const dim3 lutg(st.nchan, st.nbeam);
   const dim3 laneg(st.nchan / kCT, 32 / 8, st.nbeam);
   const dim3 rowg(st.nchan / kCT, 256 / 8, st.nbeam);
@@ -564,12 +587,12 @@ cudaError_t flag_impl(const FlagState &st, const uint8_t *gulp, uint8_t *plain, 
 }
 }  // namespace
 
-cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R, long wpos,
+cudaError_t flag_gulp(const FlagState &st, const void *gulp, uint8_t *plain, long R, long wpos,
                       cudaStream_t s) {
   return flag_impl(st, gulp, plain, R, wpos, nullptr, s);
 }
 
-cudaError_t flag_gulp_dev(const FlagState &st, const uint8_t *gulp, uint8_t *plain, long R,
+cudaError_t flag_gulp_dev(const FlagState &st, const void *gulp, uint8_t *plain, long R,
                           const GulpPos *pos, cudaStream_t s) {
   return flag_impl(st, gulp, plain, R, 0, pos, s);
 }

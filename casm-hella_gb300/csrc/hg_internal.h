@@ -57,6 +57,8 @@ struct FlagState {
   float *bpx;               // [nbeam][nchan] bandpass of an entry
   float *fsb;               // [nbeam][nchan] flag fractions of an entry
   float *flagspec;          // [nchan] flag fractions accumulated over beams and gulps
+  int f16_input;            // gulps arrive as fp16 [nbeam][nchan][gulp] (DADA input):
+                            // every stage then runs on the planes
 };
 // Largest SCRUNCH widths the box filter stages in shared memory.
 constexpr int kMaxScrunch = 64;
@@ -64,10 +66,12 @@ constexpr int kMaxScrunch = 64;
 // Runs the whole parity flagger for all beams of `gulp` (u8 [nbeam][gulp]
 // [nchan]) and writes the requantised output into the plain ring at ring
 // position `wpos` (mod R) of every beam.
-cudaError_t flag_gulp(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
+// `gulp` is u8 [nbeam][gulp][nchan], or fp16 [nbeam][nchan][gulp] when
+// st.f16_input is set.
+cudaError_t flag_gulp(const FlagState &st, const void *gulp, uint8_t *plain,
                       long R, long wpos, cudaStream_t s);
 // As above with the ring position read on the device from pos->wpos.
-cudaError_t flag_gulp_dev(const FlagState &st, const uint8_t *gulp, uint8_t *plain,
+cudaError_t flag_gulp_dev(const FlagState &st, const void *gulp, uint8_t *plain,
                           long R, const struct GulpPos *pos, cudaStream_t s);
 
 // ---------------------------------------------------------- packing

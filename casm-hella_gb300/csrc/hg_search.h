@@ -17,5 +17,7 @@ void smoothing_taps(const hella_params &p, int nbox, std::vector<float> *taps, s
                     std::vector<int> *n);
 // SCRUNCH entries and FLAG1/FLAG2 of the configuration into the flagger state.
 void flag_scrunch_params(const hella_params &p, FlagState *f);
+// Bytes of one gulp of all beams in the configured input format.
+size_t gulp_bytes(const hella_params &p);
 
 }  // namespace hg

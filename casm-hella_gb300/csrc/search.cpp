@@ -71,6 +71,7 @@ hella_status validate_params(const hella_params *p) {
   if (p->max_giants < 1) return HELLA_ERR_INVALID_ARG;
   if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
   if (p->nscrunch < 0 || p->nscrunch > HELLA_MAX_SCRUNCH) return HELLA_ERR_INVALID_ARG;
+  if (p->input_format != HELLA_INPUT_U8_TF && p->input_format != HELLA_INPUT_F16_FT) return HELLA_ERR_INVALID_ARG;
   for (int i = 0; i < p->nscrunch; ++i) {
     const hella_scrunch &sc = p->scrunch[i];
     if (sc.tscrunch < 1 || sc.tscrunch > kMaxScrunch || sc.fscrunch < 1 || sc.fscrunch > kMaxScrunch ||
@@ -89,6 +90,11 @@ void flag_scrunch_params(const hella_params &p, FlagState *f) {
   }
   f->flag_lo = p.flag1;
   f->flag_hi = p.flag2;
+  f->f16_input = p.input_format == HELLA_INPUT_F16_FT;
+}
+
+size_t gulp_bytes(const hella_params &p) {
+  return (size_t)p.nbeam * p.gulp * p.nchan * (p.input_format == HELLA_INPUT_F16_FT ? 2 : 1);
 }
 
 }  // namespace hg
@@ -330,7 +336,8 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
 
   const size_t nb = p->nbeam, nch = p->nchan, R = c->R, h = c->ndms - 2;
   const size_t need = nb * p->gulp * nch + nb * nch * R * 5 + nb * nch * (256 * 6 + 16) +
-                      (p->nscrunch > 0 ? nb * nch * (p->gulp * 6 + 8) : 0) +
+                      (p->nscrunch > 0 || p->input_format ? nb * nch * (p->gulp * 6 + 8) : 0) +
+                      (p->input_format ? nb * p->gulp * nch : 0) +
                       nb * p->gulp * 6 + (size_t)c->ndms * c->ntime_dd * 4 +
                       (size_t)c->nbox * h * c->ntime_out * 4 + (size_t)c->nbox * h * 20 +
                       (size_t)p->max_giants * 20;
@@ -339,7 +346,7 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   hella_status s;
 #define DA(ptr, bytes)                                                  \
   if ((s = dalloc(c, (void **)&(ptr), (bytes))) != HELLA_OK) return fail(s);
-  DA(c->d_gulp, nb * p->gulp * nch);
+  DA(c->d_gulp, hg::gulp_bytes(*p));
   DA(c->d_plain, nb * nch * R);
   DA(c->d_packed, nb * nch * R * 4);
   hg::FlagState &f = c->fs;
@@ -360,7 +367,7 @@ hella_status hella_create(hella_ctx **out, const hella_params *p) {
   DA(f.ts, nb * p->gulp * 4);
   DA(f.hts, nb * p->gulp * 2);
   hg::flag_scrunch_params(*p, &f);
-  if (p->nscrunch > 0) {
+  if (p->nscrunch > 0 || f.f16_input) {
     DA(f.P, nb * nch * p->gulp * 2);
     DA(f.M, nb * nch * p->gulp * 2);
     DA(f.S, nb * nch * p->gulp * 2);
@@ -449,7 +456,7 @@ hella_status hella_set_killmask(hella_ctx *c, const int *killmask) {
 
 hella_status hella_load_gulp(hella_ctx *c, const uint8_t *gulp, int on_device) {
   if (!c || !gulp) return HELLA_ERR_INVALID_ARG;
-  const size_t n = (size_t)c->p.nbeam * c->p.gulp * c->p.nchan;
+  const size_t n = hg::gulp_bytes(c->p);
   CK(cudaMemcpyAsync(c->d_gulp, gulp, n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                      c->stream));
   c->loaded = true;

@@ -83,7 +83,14 @@ typedef struct {
                        HELLA_ERR_BUDGET if the context would need more */
   int autotune;     /* 1: hella_create times dedispersion tile shapes on the
                        context's own buffers and keeps the fastest */
+  int input_format; /* HELLA_INPUT_U8_TF (0, default): u8 [nbeam][gulp][nchan]
+                       filterbank gulps; HELLA_INPUT_F16_FT (1): fp16
+                       [nbeam][nchan][gulp], the DADA input (INPUT DADA,
+                       casm_hella_refactored.cu:78, transpose.cu:87-90) */
 } hella_params;
+
+#define HELLA_INPUT_U8_TF 0
+#define HELLA_INPUT_F16_FT 1
 
 /* Dedispersion tile shape (no counterpart in the reference, whose dedisp
  * library fixes its own).  Every shape computes the same exact sums. */
@@ -132,7 +139,8 @@ const float *hella_get_dm_list(const hella_ctx *ctx);
 /* Killmask shared by all beams (0 = channel dropped from dedispersion). */
 hella_status hella_set_killmask(hella_ctx *ctx, const int *killmask);
 
-/* Gulp input: u8 [nbeam][gulp][nchan] (time-major, as a SIGPROC gulp);
+/* Gulp input: u8 [nbeam][gulp][nchan] (time-major, as a SIGPROC gulp), or
+ * fp16 [nbeam][nchan][gulp] with input_format HELLA_INPUT_F16_FT;
  * on_device != 0 means `gulp` is a device pointer. */
 hella_status hella_load_gulp(hella_ctx *ctx, const uint8_t *gulp,
                              int on_device);

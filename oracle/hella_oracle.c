@@ -424,18 +424,41 @@ static uint8_t requant(uint16_t h) {
   return (uint8_t)v;
 }
 
+/* fast_flagger (flagger.cu:345-411) from the fp16 channel-major copy d of
+ * one beam's gulp, which it consumes. */
+static void flag_plane(uint16_t *d, int w, int nchan, const ho_flag_params *fp, uint8_t *out,
+                       float *ts_out, float *flagspec, ho_flag_trace *tr);
+
 void ho_flag_beam(const uint8_t *gulp, int w, int nchan,
                   const ho_flag_params *fp, uint8_t *out, float *ts_out,
                   float *flagspec, ho_flag_trace *tr) {
   size_t n = (size_t)nchan * w;
   uint16_t *d = (uint16_t *)malloc(n * sizeof(uint16_t));
+  /* transpose_input  transpose.cu:23-42 (u8 -> fp16, exact) */
+  for (int t = 0; t < w; ++t)
+    for (int c = 0; c < nchan; ++c) d[(size_t)c * w + t] = ho_f2h((float)gulp[(size_t)t * nchan + c]);
+  flag_plane(d, w, nchan, fp, out, ts_out, flagspec, tr);
+  free(d);
+}
+
+/* The DADA input path (transpose_input_handler, transpose.cu:87-90): the
+ * gulp arrives as fp16 in channel-major (FT) order and is flagged as is. */
+void ho_flag_beam_f16(const uint16_t *ft, int w, int nchan, const ho_flag_params *fp,
+                      uint8_t *out, float *ts_out, float *flagspec, ho_flag_trace *tr) {
+  size_t n = (size_t)nchan * w;
+  uint16_t *d = (uint16_t *)malloc(n * sizeof(uint16_t));
+  memcpy(d, ft, n * sizeof(uint16_t));
+  flag_plane(d, w, nchan, fp, out, ts_out, flagspec, tr);
+  free(d);
+}
+
+static void flag_plane(uint16_t *d, int w, int nchan, const ho_flag_params *fp, uint8_t *out,
+                       float *ts_out, float *flagspec, ho_flag_trace *tr) {
+  size_t n = (size_t)nchan * w;
   uint16_t *mask = (uint16_t *)malloc(n * sizeof(uint16_t));
   uint16_t *sm = (uint16_t *)malloc(n * sizeof(uint16_t));
   float *bp = (float *)malloc(sizeof(float) * (size_t)nchan);
   float m1, s1, m2, s2;
-  /* transpose_input  transpose.cu:23-42 (u8 -> fp16, exact) */
-  for (int t = 0; t < w; ++t)
-    for (int c = 0; c < nchan; ++c) d[(size_t)c * w + t] = ho_f2h((float)gulp[(size_t)t * nchan + c]);
   /* bandpass_flag  flagger.cu:216-242 */
   bandpass_correct(d, nchan, w, tr ? tr->bp1 : NULL);
   normalize_data(d, nchan, w, &m1, &s1);
@@ -467,7 +490,6 @@ void ho_flag_beam(const uint8_t *gulp, int w, int nchan,
   }
   for (int t = 0; t < w; ++t)
     for (int c = 0; c < nchan; ++c) out[(size_t)t * nchan + c] = requant(d[(size_t)c * w + t]);
-  free(d);
   free(mask);
   free(sm);
   free(bp);
@@ -668,16 +690,35 @@ int ho_search_window(const ho_pipeline *pl, const uint8_t *window, int beam,
   return n;
 }
 
+static int pipeline_step(ho_pipeline *pl, const void *gulp, int f16, ho_cand *cands, int max_cands,
+                         int *searched);
+
 int ho_pipeline_gulp(ho_pipeline *pl, const uint8_t *gulp, ho_cand *cands,
                      int max_cands, int *searched) {
+  return pipeline_step(pl, gulp, 0, cands, max_cands, searched);
+}
+
+/* The gulp loop fed fp16 FT gulps [nbeam][nchan][gulp] (DADA input). */
+int ho_pipeline_gulp_f16(ho_pipeline *pl, const uint16_t *gulp, ho_cand *cands,
+                         int max_cands, int *searched) {
+  return pipeline_step(pl, gulp, 1, cands, max_cands, searched);
+}
+
+static int pipeline_step(ho_pipeline *pl, const void *gulp, int f16, ho_cand *cands, int max_cands,
+                         int *searched) {
   const ho_params *p = &pl->p;
   size_t beam_ring = (size_t)pl->ntime * p->nchan;
   size_t beam_gulp = (size_t)p->gulp * p->nchan;
   int nout = 0;
-  for (int b = 0; b < p->nbeam; ++b)
-    ho_flag_beam(gulp + b * beam_gulp, p->gulp, p->nchan, &p->flag,
-                 pl->ring + b * beam_ring + (size_t)(pl->ntime - p->gulp) * p->nchan,
-                 NULL, pl->flagspec, NULL);
+  for (int b = 0; b < p->nbeam; ++b) {
+    uint8_t *dst = pl->ring + b * beam_ring + (size_t)(pl->ntime - p->gulp) * p->nchan;
+    if (f16)
+      ho_flag_beam_f16((const uint16_t *)gulp + b * beam_gulp, p->gulp, p->nchan, &p->flag, dst, NULL,
+                       pl->flagspec, NULL);
+    else
+      ho_flag_beam((const uint8_t *)gulp + b * beam_gulp, p->gulp, p->nchan, &p->flag, dst, NULL,
+                   pl->flagspec, NULL);
+  }
   int cap = p->max_giants < max_cands ? p->max_giants : max_cands;
   int do_search = pl->gulp_idx >= pl->min_gulp; /* :705 */
   if (do_search)

@@ -113,6 +113,10 @@ typedef struct {
  * out: u8 [w][nchan] (the tail of the beam's ring); ts_out: [w] or NULL;
  * flagspec: [nchan] accumulated flag fractions (scrunch path) or NULL;
  * trace may be NULL.  nchan <= 8192, w % 32 == 0, nchan % 32 == 0. */
+/* As ho_flag_beam from an fp16 channel-major gulp [nchan][w] (the DADA
+ * input path, transpose.cu:87-90). */
+void ho_flag_beam_f16(const uint16_t *ft, int w, int nchan, const ho_flag_params *fp,
+                      uint8_t *out, float *ts_out, float *flagspec, ho_flag_trace *tr);
 void ho_flag_beam(const uint8_t *gulp, int w, int nchan,
                   const ho_flag_params *fp, uint8_t *out, float *ts_out,
                   float *flagspec, ho_flag_trace *trace);
@@ -192,6 +196,8 @@ const int32_t *ho_pipeline_delays(const ho_pipeline *pl);
  * candidates exist (once the ring is full), then rewind.  gulp: u8
  * [nbeam][gulp][nchan].  Returns the candidate count; *searched is 1 when
  * the search ran. */
+int ho_pipeline_gulp_f16(ho_pipeline *pl, const uint16_t *gulp, ho_cand *cands,
+                         int max_cands, int *searched);
 int ho_pipeline_gulp(ho_pipeline *pl, const uint8_t *gulp, ho_cand *cands,
                      int max_cands, int *searched);
 /* Access to the last gulp's state for stage-level checks. */

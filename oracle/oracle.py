@@ -99,6 +99,9 @@ def lib() -> C.CDLL:
         L.ho_pipeline_delays.argtypes = [_VP]
         L.ho_pipeline_gulp.restype = C.c_int
         L.ho_pipeline_gulp.argtypes = [_VP, _VP, _VP, C.c_int, C.POINTER(C.c_int)]
+        L.ho_pipeline_gulp_f16.restype = C.c_int
+        L.ho_pipeline_gulp_f16.argtypes = [_VP, _VP, _VP, C.c_int, C.POINTER(C.c_int)]
+        L.ho_flag_beam_f16.argtypes = [_VP, C.c_int, C.c_int, C.POINTER(FlagParams), _VP, _VP, _VP, _VP]
         L.ho_pipeline_ring.restype = C.POINTER(C.c_uint8)
         L.ho_pipeline_ring.argtypes = [_VP, C.c_int]
         L.ho_pipeline_flagspec.restype = C.POINTER(C.c_float)
@@ -185,6 +188,22 @@ def flag_beam(gulp: np.ndarray, fp: FlagParams | None = None, flagspec=None):
     return out, ts, trace
 
 
+def flag_beam_f16(ft: np.ndarray, fp: FlagParams | None = None, flagspec=None):
+    """fp16 channel-major [nchan][w] (the DADA input) -> (u8 [w][nchan], ts [w], trace dict)."""
+    ft = np.ascontiguousarray(ft, np.float16)
+    nchan, w = ft.shape
+    fp = fp or flag_params()
+    out = np.zeros((w, nchan), np.uint8)
+    ts = np.zeros(w, np.float32)
+    tr = FlagTrace()
+    lib().ho_flag_beam_f16(ft.ctypes.data, w, nchan, C.byref(fp), out.ctypes.data, ts.ctypes.data,
+                           None if flagspec is None else flagspec.ctypes.data, C.byref(tr))
+    trace = dict(bp1=np.array(tr.bp1[:nchan], np.float32), bp2=np.array(tr.bp2[:nchan], np.float32),
+                 bp3=np.array(tr.bp3[:nchan], np.float32), mean1=np.float32(tr.mean1),
+                 std1=np.float32(tr.std1), mean2=np.float32(tr.mean2), std2=np.float32(tr.std2))
+    return out, ts, trace
+
+
 def smooth_taps(sm: int) -> np.ndarray:
     k = np.zeros(3 * (2 * sm + 1), np.float32)
     lib().ho_smooth_taps(sm, k.ctypes.data)
@@ -233,6 +252,14 @@ class Pipeline:
         out = np.zeros(self.max_giants, CAND_DTYPE)
         s = C.c_int()
         n = self.L.ho_pipeline_gulp(self.h, gulp.ctypes.data, out.ctypes.data, self.max_giants, C.byref(s))
+        return out[:n], bool(s.value)
+
+    def gulp_step_f16(self, gulp: np.ndarray):
+        """One gulp of fp16 FT data [nbeam][nchan][gulp] (DADA input)."""
+        gulp = np.ascontiguousarray(gulp, np.float16)
+        out = np.zeros(self.max_giants, CAND_DTYPE)
+        s = C.c_int()
+        n = self.L.ho_pipeline_gulp_f16(self.h, gulp.ctypes.data, out.ctypes.data, self.max_giants, C.byref(s))
         return out[:n], bool(s.value)
 
     def search_window(self, window: np.ndarray, beam=0, cap=None, want_planes=True):

@@ -1,0 +1,63 @@
+"""The DADA input path (INPUT DADA: fp16 gulps in channel-major order,
+casm_hella_refactored.cu:78,245-248,688-691; transpose.cu:87-90): flagger
+output and candidates bit-exact against the oracle fed the same fp16 gulps,
+for the single-beam context (with and without SCRUNCH entries) and the batch."""
+import numpy as np
+import pytest
+
+import synth
+from helpers import cands_equal, oracle_pipeline, small_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _f16_ft(x_u8: np.ndarray, seed: int) -> np.ndarray:
+    """u8 [..., w, nchan] -> fp16 [..., nchan, w] with sub-integer detail, as a
+    voltage beamformer's fp16 output would carry."""
+    rng = np.random.default_rng(seed)
+    f = x_u8.astype(np.float32) + rng.uniform(-0.45, 0.45, x_u8.shape).astype(np.float32)
+    return np.ascontiguousarray(np.swapaxes(f.astype(np.float16), -1, -2))
+
+
+@pytest.mark.parametrize("entries", [(), ((4, 2, 3.0, 1),)])
+def test_dada_flagger_bit_exact(hella, oracle, entries):
+    p = small_params(nchan=128, gulp=4096)
+    sky = synth.Sky(p["nchan"], p["tsamp"], p["f0_mhz"], p["df_mhz"], seed=41, rfi_chans=(5, 90), slope=0.3)
+    s = hella.Search(hella.default_params(**p, scrunches=list(entries), input_format=1))
+    fspec = np.zeros(p["nchan"], np.float32)
+    fp = oracle.flag_params(scrunches=list(entries))
+    for g in range(2):
+        x = sky.gulp(g, p["gulp"])
+        x[:, 77] = 0
+        ft = _f16_ft(x, g)
+        s.load_gulp(ft[None])
+        s.fast_flagger()
+        out, ts, tr = oracle.flag_beam_f16(ft, fp, fspec)
+        st = s.flag_stats(0)
+        for k in ("bp1", "bp2", "bp3"):
+            assert np.array_equal(st[k].view(np.uint32), tr[k].view(np.uint32)), (g, k)
+        for k in ("mean1", "std1", "mean2", "std2"):
+            assert np.float32(st[k]).view(np.uint32) == np.float32(tr[k]).view(np.uint32), (g, k)
+        assert np.array_equal(st["ts"].view(np.uint32), ts.view(np.uint32))
+        assert np.array_equal(s.copy_window(0)[-p["gulp"]:], out), g
+        s.rewind()
+
+
+def test_dada_gulp_loop_and_batch(hella, oracle):
+    params, _ = synth.config_plain(seed=43, nchan=128, gulp=2048, dm_max=400.0)
+    skies = [synth.config_plain(seed=44 + b, nchan=128, gulp=2048, dm_max=400.0)[1] for b in range(2)]
+    for sk in skies:
+        sk.bursts[0].amp *= 3
+    s = hella.Search(hella.default_params(**dict(params, nbeam=2), input_format=1))
+    bt = hella.Batch(hella.default_params(**dict(params, nbeam=2), input_format=1))
+    pl = oracle_pipeline(oracle, params, nbeam=2)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        ft = _f16_ft(synth.multibeam_gulp(skies, g, params["gulp"]), 100 + g)
+        got, _ = s.process_gulp(ft)
+        want, _ = pl.gulp_step_f16(ft)
+        assert cands_equal(got, want), g
+        bgot, _, _ = bt.process_gulp(ft)
+        assert cands_equal(bgot, want), g
+        total += len(got)
+    assert total > 0

@@ -58,6 +58,15 @@ class BatchParams(C.Structure):
                 ("member", C.c_void_p), ("inflight", C.c_int), ("bp_alpha", C.c_float)]
 
 
+class FilHeader(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("machine_id", "telescope_id", "data_type", "nchans", "nbits", "nifs",
+                                        "barycentric", "pulsarcentric", "ibeam", "nbeams")] + \
+               [(k, C.c_double) for k in ("tstart", "tsamp", "fch1", "foff", "refdm", "az_start", "za_start",
+                                          "src_raj", "src_dej", "period")] + \
+               [("isign", C.c_char), ("npuls", C.c_long), ("source_name", C.c_char * 81),
+                ("rawdatafile", C.c_char * 81), ("nfreq", C.c_int), ("header_bytes", C.c_long)]
+
+
 class RefineParams(C.Structure):
     _fields_ = [("ncut", C.c_int), ("nchan", C.c_int), ("nsamp", C.c_int), ("tsamp", C.c_double),
                 ("f0_mhz", C.c_double), ("df_mhz", C.c_double), ("device", C.c_int)]
@@ -178,6 +187,33 @@ def lib() -> C.CDLL:
     _sig(L, "hella_refine_forward", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP])
     _sig(L, "hella_refine_adjoint", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP])
     _sig(L, "hella_refine_fit", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, C.c_int, _VP, _VP])
+    # I/O around the search
+    _sig(L, "hella_fil_open", C.c_int, [C.POINTER(_VP), C.c_char_p, C.c_int, C.POINTER(FilHeader)])
+    _sig(L, "hella_fil_read", C.c_int, [_VP, _VP, C.c_int, C.POINTER(C.c_int)])
+    _sig(L, "hella_fil_close", None, [_VP])
+    _sig(L, "hella_cands_format", C.c_int, [_VP, C.c_int, C.c_long, _VP, C.c_int, C.c_double, _VP, C.c_size_t,
+                                            C.POINTER(C.c_size_t)])
+    _sig(L, "hella_cands_append", C.c_int, [C.c_char_p, _VP, C.c_int, C.c_long, _VP, C.c_int, C.c_double])
+    _sig(L, "hella_cands_coincidencer", C.c_int, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, _VP, C.c_int,
+                                                  C.c_long, _VP, C.c_int, C.c_double, _VP, C.c_size_t,
+                                                  C.POINTER(C.c_size_t)])
+    _sig(L, "hella_cluster", C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, C.POINTER(C.c_int), _VP])
+    _sig(L, "hella_flagstats_create", C.c_int, [C.POINTER(_VP), C.c_int, C.c_int])
+    _sig(L, "hella_flagstats_destroy", None, [_VP])
+    _sig(L, "hella_flagstats_update", C.c_int, [_VP, _VP])
+    _sig(L, "hella_flagstats_counts", C.c_int, [_VP, _VP])
+    _sig(L, "hella_flagstats_append", C.c_int, [_VP, C.c_char_p])
+    _sig(L, "hella_ring_create", C.c_int, [C.POINTER(_VP), C.c_size_t, C.c_int, C.c_int])
+    _sig(L, "hella_ring_destroy", None, [_VP])
+    _sig(L, "hella_ring_block_bytes", C.c_size_t, [_VP])
+    _sig(L, "hella_ring_write_header", C.c_int, [_VP, C.c_char_p, C.c_size_t])
+    _sig(L, "hella_ring_read_header", C.c_int, [_VP, _VP, C.c_size_t, C.POINTER(C.c_size_t), C.c_int])
+    _sig(L, "hella_ring_open_write", C.c_int, [_VP, C.POINTER(_VP), C.c_int])
+    _sig(L, "hella_ring_mark_filled", C.c_int, [_VP, C.c_size_t])
+    _sig(L, "hella_ring_end", C.c_int, [_VP])
+    _sig(L, "hella_ring_open_read", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(C.c_size_t), C.c_int])
+    _sig(L, "hella_ring_mark_cleared", C.c_int, [_VP])
+    _sig(L, "hella_header_get", C.c_int, [C.c_char_p, C.c_size_t, C.c_char_p, _VP, C.c_size_t])
     _sig(L, "hella_get_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_set_tuning", C.c_int, [_VP, C.POINTER(HellaTuning)])
     _sig(L, "hella_time_dedisp", C.c_int, [_VP, C.POINTER(HellaTuning), C.c_int, C.POINTER(C.c_float)])
@@ -623,3 +659,153 @@ class Refine:
         lr = np.ascontiguousarray(lr, dtype=np.float32)
         _chk(self.L.hella_refine_fit(self.h, theta.shape[0], _ptr(cut), _ptr(dm_ref), _ptr(theta), steps,
                                      lr.ctypes.data, _ptr(chi2)))
+
+
+# ------------------------------------------------------------------- I/O
+
+class Filterbank:
+    """SIGPROC filterbank reader (hella_fil_*)."""
+
+    def __init__(self, path: str, expect_nchan: int = 0):
+        self.L = lib()
+        h, hdr = _VP(), FilHeader()
+        _chk(self.L.hella_fil_open(C.byref(h), str(path).encode(), expect_nchan, C.byref(hdr)))
+        self.h, self.header = h, hdr
+
+    def read(self, nsamp: int) -> np.ndarray:
+        out = np.empty((nsamp, self.header.nchans), np.uint8)
+        got = C.c_int()
+        _chk(self.L.hella_fil_read(self.h, out.ctypes.data, nsamp, C.byref(got)))
+        return out[: got.value]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_fil_close(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+def _cands_arg(c):
+    c = np.ascontiguousarray(c, CAND_DTYPE)
+    return c, (c.ctypes.data if len(c) else None)
+
+
+def cands_format(cands, samp0: int, dms, time_resolution: float = 1.0e-3) -> str:
+    c, cp = _cands_arg(cands)
+    d = np.ascontiguousarray(dms, np.float32)
+    buf = C.create_string_buffer(96 * len(c) + 64)
+    n = C.c_size_t()
+    _chk(lib().hella_cands_format(cp, len(c), samp0, d.ctypes.data, len(d), time_resolution, buf, len(buf),
+                                  C.byref(n)))
+    return buf.raw[: n.value].decode()
+
+
+def cands_append(path: str, cands, samp0: int, dms, time_resolution: float = 1.0e-3):
+    c, cp = _cands_arg(cands)
+    d = np.ascontiguousarray(dms, np.float32)
+    _chk(lib().hella_cands_append(str(path).encode(), cp, len(c), samp0, d.ctypes.data, len(d), time_resolution))
+
+
+def cands_coincidencer(gulp_number: int, cands, samp0: int, dms, time_resolution: float = 1.0e-3,
+                       utc_start=None, picoseconds=None, tsamp=None) -> str:
+    c, cp = _cands_arg(cands)
+    d = np.ascontiguousarray(dms, np.float32)
+    buf = C.create_string_buffer(96 * len(c) + 256)
+    n = C.c_size_t()
+    enc = lambda v: None if v is None else str(v).encode()
+    _chk(lib().hella_cands_coincidencer(gulp_number, enc(utc_start), enc(picoseconds), enc(tsamp), cp, len(c),
+                                        samp0, d.ctypes.data, len(d), time_resolution, buf, len(buf), C.byref(n)))
+    return buf.raw[: n.value].decode()
+
+
+def cluster(cands, dsamp: int, ddm: int, dwidth: int):
+    """(representatives, labels) of friends-of-friends clusters (hella_cluster)."""
+    c, cp = _cands_arg(cands)
+    out = np.zeros(max(1, len(c)), CAND_DTYPE)
+    labels = np.zeros(max(1, len(c)), np.int32)
+    n = C.c_int()
+    _chk(lib().hella_cluster(cp, len(c), dsamp, ddm, dwidth, out.ctypes.data, C.byref(n), labels.ctypes.data))
+    return out[: n.value], labels[: len(c)]
+
+
+class FlagStats:
+    """Per-channel flag counts over searched gulps (hella_flagstats_*)."""
+
+    def __init__(self, nchan: int, ntime: int):
+        self.L = lib()
+        h = _VP()
+        _chk(self.L.hella_flagstats_create(C.byref(h), nchan, ntime))
+        self.h, self.nchan = h, nchan
+
+    def update(self, cumulative):
+        a = np.ascontiguousarray(cumulative, np.float32)
+        _chk(self.L.hella_flagstats_update(self.h, a.ctypes.data))
+
+    def counts(self) -> np.ndarray:
+        out = np.zeros(self.nchan, np.int64)
+        _chk(self.L.hella_flagstats_counts(self.h, out.ctypes.data))
+        return out
+
+    def append(self, path: str):
+        _chk(self.L.hella_flagstats_append(self.h, str(path).encode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_flagstats_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class Ring:
+    """In-process header + data-block ring (hella_ring_*)."""
+
+    def __init__(self, block_bytes: int, nblocks: int, pinned: bool = False):
+        self.L = lib()
+        h = _VP()
+        _chk(self.L.hella_ring_create(C.byref(h), block_bytes, nblocks, int(pinned)))
+        self.h, self.block_bytes = h, block_bytes
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hella_ring_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def write_header(self, text: str):
+        b = text.encode()
+        _chk(self.L.hella_ring_write_header(self.h, b, len(b)))
+
+    def read_header(self, timeout_ms: int = 1000) -> str:
+        buf = C.create_string_buffer(65536)
+        n = C.c_size_t()
+        _chk(self.L.hella_ring_read_header(self.h, buf, len(buf), C.byref(n), timeout_ms))
+        return buf.raw[: n.value].decode()
+
+    def write(self, data: bytes, timeout_ms: int = 1000):
+        p = _VP()
+        _chk(self.L.hella_ring_open_write(self.h, C.byref(p), timeout_ms))
+        C.memmove(p, data, len(data))
+        _chk(self.L.hella_ring_mark_filled(self.h, len(data)))
+
+    def end(self):
+        _chk(self.L.hella_ring_end(self.h))
+
+    def read(self, timeout_ms: int = 1000):
+        """bytes of the next block, or None at the end of the data."""
+        p, n = _VP(), C.c_size_t()
+        _chk(self.L.hella_ring_open_read(self.h, C.byref(p), C.byref(n), timeout_ms))
+        if n.value == 0:
+            return None
+        data = C.string_at(p, n.value)
+        _chk(self.L.hella_ring_mark_cleared(self.h))
+        return data
+
+
+def header_get(header: str, key: str):
+    b = header.encode()
+    out = C.create_string_buffer(4096)
+    rc = lib().hella_header_get(b, len(b), key.encode(), out, len(out))
+    return out.value.decode() if rc == 0 else None

@@ -38,6 +38,9 @@ WORKLOAD = ("full single beam: 2048 ch 375-468.75 MHz, tsamp 0.524288 ms, gulp 6
             "DM 0-2000 tol 1.25, widths 1-256, 7 sigma")
 METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp latency"
 UNIT = "beam·s/s"
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_dedisp launch of this workload, from one
+# ncu --set full capture of `bench.py --steps 1 --warmup 3` (8.09 GB read + 0.686 GB written)
+DEDISP_TRAFFIC_BYTES = 8.777e9
 
 
 def args_():
@@ -275,7 +278,8 @@ def main():
     achieved = adds / dd_t / 1e12
     peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
     roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
+            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES,
+            "traffic_unit": "bytes per launch (ncu)",
             "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
             "ms_per_launch": round(dd_t * 1e3, 3)}

@@ -406,6 +406,39 @@ __global__ void k_pack(const uint8_t *__restrict__ plain, uint32_t *__restrict__
   packed[row + q] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
 }
 
+// k_pack for 4-word-aligned ranges: thread i builds words q..q+3
+// (q = q0 + 4i) from one 32-bit load at each of q, q+S, q+2S, q+3S and a
+// 4x4 byte transpose, and stores them as one 16-byte word.  R % 4 == 0 and
+// q0 % 4 == 0 keep every load and store aligned and no group straddles the
+// ring's end.
+__global__ void k_pack4(const uint8_t *__restrict__ plain, uint32_t *__restrict__ packed,
+                        int nchan, long R, long q0, long ngroups, const uint8_t *__restrict__ keep,
+                        const GulpPos *dpos) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ngroups) return;
+  if (dpos) q0 = ((dpos->wpos - 3L * S) % R + R) % R;
+  const size_t bc = (size_t)blockIdx.z * nchan + blockIdx.y;
+  const size_t row = bc * (size_t)R;
+  long q = q0 + 4 * i;
+  while (q >= R) q -= R;
+  uint4 *dst = reinterpret_cast<uint4 *>(packed + row + q);
+  if (keep && !keep[bc]) {
+    *dst = make_uint4(0u, 0u, 0u, 0u);
+    return;
+  }
+  uint32_t a[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    long pos = q + (long)k * S;
+    while (pos >= R) pos -= R;
+    a[k] = *reinterpret_cast<const uint32_t *>(plain + row + pos);  // byte j = sample pos + j
+  }
+  const uint32_t t0 = __byte_perm(a[0], a[1], 0x5140), t1 = __byte_perm(a[2], a[3], 0x5140);
+  const uint32_t t2 = __byte_perm(a[0], a[1], 0x7362), t3 = __byte_perm(a[2], a[3], 0x7362);
+  *dst = make_uint4(__byte_perm(t0, t1, 0x5410), __byte_perm(t0, t1, 0x7632), __byte_perm(t2, t3, 0x5410),
+                    __byte_perm(t2, t3, 0x7632));
+}
+
 // [nsamps][in_stride] -> [nchan][R], 32x32 tiles through shared memory.
 __global__ void k_transpose_tf(const uint8_t *__restrict__ in, size_t in_stride,
                                int nsamps, int nchan, uint8_t *__restrict__ out, long R) {
@@ -546,6 +579,12 @@ cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam, int nch
   if (nq <= 0) return cudaSuccess;
   q0 = ((q0 % R) + R) % R;
   nq = std::min(nq, R);  // each ring position once
+  if (R % 4 == 0 && q0 % 4 == 0 && nq % 4 == 0) {
+    const dim3 grid((unsigned)((nq / 4 + 255) / 256), nchan, nbeam);
+    k_pack4<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq / 4, keep, nullptr);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   const dim3 grid((unsigned)((nq + 255) / 256), nchan, nbeam);
   k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, q0, nq, keep, nullptr);
   count_launches(1);
@@ -555,6 +594,12 @@ cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam, int nch
 cudaError_t pack_gulp_dev(const uint8_t *plain, uint32_t *packed, int nbeam, int nchan, long R,
                           int gulp, const GulpPos *pos, cudaStream_t s, const uint8_t *keep) {
   const long nq = std::min((long)gulp + 3L * S, R);  // each ring position once
+  if (R % 4 == 0 && gulp % 4 == 0 && nq % 4 == 0) {  // wpos is then a multiple of 4 as well
+    const dim3 grid((unsigned)((nq / 4 + 255) / 256), nchan, nbeam);
+    k_pack4<<<grid, 256, 0, s>>>(plain, packed, nchan, R, 0, nq / 4, keep, pos);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   const dim3 grid((unsigned)((nq + 255) / 256), nchan, nbeam);
   k_pack<<<grid, 256, 0, s>>>(plain, packed, nchan, R, 0, nq, keep, pos);
   count_launches(1);

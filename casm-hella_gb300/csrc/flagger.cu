@@ -189,11 +189,13 @@ __global__ void k_beam_sum(FlagState st, int which) {
 // measure_ts: per sample, fp16 running sum over channels in channel order,
 // then ts = float(sum) / nchan.  Block = 128 consecutive samples; rows and
 // table slices are staged through shared memory 64 channels at a time.
+// The gulp rows and table slices are staged with 4- and 16-byte loads
+// (nchan % 32 == 0 keeps every 64-channel chunk whole and aligned).
 constexpr int kTsT = 128, kTsC = 64;
 __global__ void __launch_bounds__(kTsT) k_ts(const uint8_t *__restrict__ gulp,
                                              FlagState st) {
-  __shared__ uint8_t rows_s[kTsT][kTsC + 4];
-  __shared__ __half lut_s[kTsC][256];
+  __shared__ __align__(16) uint8_t rows_s[kTsT][kTsC + 4];
+  __shared__ __align__(16) __half lut_s[kTsC][256];
   const int b = blockIdx.y, t0 = blockIdx.x * kTsT, nchan = st.nchan, w = st.gulp;
   const int tid = threadIdx.x;
   const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)t0 * nchan;
@@ -202,14 +204,15 @@ __global__ void __launch_bounds__(kTsT) k_ts(const uint8_t *__restrict__ gulp,
   for (int c0 = 0; c0 < nchan; c0 += kTsC) {
     const int nc = min(kTsC, nchan - c0);
     __syncthreads();
-    for (int i = tid; i < kTsT * kTsC; i += kTsT) {
-      int r = i / kTsC, cc = i % kTsC;
-      if (cc < nc && t0 + r < w) rows_s[r][cc] = g[(size_t)r * nchan + c0 + cc];
+    for (int i = tid; i < kTsT * (kTsC / 4); i += kTsT) {
+      const int r = i / (kTsC / 4), c4 = 4 * (i % (kTsC / 4));
+      if (c4 < nc && t0 + r < w)
+        *reinterpret_cast<uint32_t *>(&rows_s[r][c4]) =
+            *reinterpret_cast<const uint32_t *>(g + (size_t)r * nchan + c0 + c4);
     }
-    for (int i = tid; i < kTsC * 256; i += kTsT) {
-      int cc = i >> 8, v = i & 255;
-      if (cc < nc) lut_s[cc][v] = lb[(size_t)(c0 + cc) * 256 + v];
-    }
+    const uint4 *lsrc = reinterpret_cast<const uint4 *>(lb + (size_t)c0 * 256);
+    uint4 *ldst = reinterpret_cast<uint4 *>(&lut_s[0][0]);
+    for (int i = tid; i < nc * 256 / 8; i += kTsT) ldst[i] = lsrc[i];
     __syncthreads();
     if (t0 + tid < w)
       for (int cc = 0; cc < nc; ++cc) s = __hadd(s, lut_s[cc][rows_s[tid][cc]]);

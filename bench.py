@@ -50,7 +50,7 @@ def args_():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batched", "stream", "refine"],
+    ap.add_argument("--workload", default="full", choices=["full", "plain", "batched", "stream", "refine"],
                     help="full: the single-beam headline workload; batched: all beams of the "
                          "multi-beam configuration per step")
     ap.add_argument("--beams", type=int, default=256, help="beams of the batched workload")
@@ -101,10 +101,17 @@ class Clocks:
 
 # ------------------------------------------------------------- workload
 
-def workload(rank: int, ngulps: int = 3):
+PLAIN_WORKLOAD = ("plain single beam: 512 ch 375-468.75 MHz, tsamp 1.048576 ms, gulp 16384, DM 0-500 tol 1.25 "
+                  "(0.5 ms pulse), widths 1-32, 7 sigma, one DM-300 burst")
+
+
+def workload(rank: int, ngulps: int = 3, which: str = "full"):
     import synth
 
-    params, sky = synth.config_full(seed=2 + rank)
+    if which == "plain":
+        params, sky = synth.config_plain(seed=1 + rank)
+    else:
+        params, sky = synth.config_full(seed=2 + rank)
     gulps = [sky.gulp(g, params["gulp"]) for g in range(ngulps)]
     return params, sky, gulps
 
@@ -178,7 +185,7 @@ def main():
     import hella_gb300 as hg
 
     hg.lib()
-    params, sky, gulps = workload(rank)
+    params, sky, gulps = workload(rank, which=a.workload)
     G, nch = params["gulp"], params["nchan"]
     gulp_s = G * params["tsamp"]
     s = hg.Search(hg.default_params(**params, device=local))
@@ -278,7 +285,7 @@ def main():
     achieved = adds / dd_t / 1e12
     peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
     roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES,
+            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES if a.workload == "full" else None,
             "traffic_unit": "bytes per launch (ncu)",
             "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
@@ -303,11 +310,17 @@ def main():
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)",
-        "config": {"workload": WORKLOAD, "nchan": nch, "gulp": G, "tsamp": params["tsamp"],
+        "vs_baseline": None, "dtype": "u8",
+        "data": ("synthetic (seeded noise, 4 RFI channels, 3 broadband impulses, one DM-300 burst)"
+                 if a.workload == "plain" else "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)"),
+        "config": {"workload": PLAIN_WORKLOAD if a.workload == "plain" else WORKLOAD, "nchan": nch, "gulp": G,
+                   "tsamp": params["tsamp"],
                    "ndms": info.ndms, "max_delay": info.max_delay, "ntime": info.ntime,
                    "widths": info.nboxcar, "beams_per_gpu": 1, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2: 134 MB gulp, 1.1 GB ring, 0.66 GB plane, 5.9 GB smoothed planes"},
+                   "l2": (f"inputs {'larger' if info.ndms * info.ntime_dd * 4 > 129e6 else 'smaller'} than L2: "
+                          f"{G * nch / 1e6:.0f} MB gulp, {nch * info.ntime * 5 / 1e9:.2f} GB ring, "
+                          f"{info.ndms * info.ntime_dd * 4 / 1e9:.2f} GB plane, "
+                          f"{info.nboxcar * (info.ndms - 2) * G * 4 / 1e9:.2f} GB smoothed planes")},
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": G * nch,
                 "d2h_bytes_per_step": int(4 + 20 * np.mean(ncand)),
                 "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
@@ -672,7 +685,8 @@ def run_reference(a, rank, world):
     """The reference path's CPU implementation on the host cores."""
     if rank != 0:
         return
-    params, sky, gulps = workload(0, ngulps=1)
+    which = a.workload if a.workload in ("full", "plain") else "full"
+    params, sky, gulps = workload(0, ngulps=1, which=which)
     gulp_s = params["gulp"] * params["tsamp"]
     for _ in range(a.warmup):
         cpu_sample(params, gulps[0], dm_rows=32)
@@ -685,7 +699,7 @@ def run_reference(a, rank, world):
     line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)",
-            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "config": {"workload": PLAIN_WORKLOAD if which == "plain" else WORKLOAD}, "impl": "reference",
             "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -280,7 +280,7 @@ class Plan:
         self.h = h
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             self.L.hdd_destroy_plan(self.h)
             self.h = None
 

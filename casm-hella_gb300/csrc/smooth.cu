@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
       const int smw = a.wmin << b;
       const int off = a.anchor ? span - 2 * smw : 0;
       const float *tp = taps + a.tap_off[b] - tap0;
-      const int n = a.tap_n[b];
+      const int ntap = 2 * smw + 1, nblk = ntap / kR, tail = ntap - nblk * kR;
       const int base = kR * tid + off;
       // win[] slides over y; pre[kk] is where the slot refilled at tap kk of
       // the first block of kR taps lives in Y (later blocks add one column)
@@ -115,14 +115,34 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
         win[i] = Y[(x % kR) * M + x / kR];
         pre[i] = (xr % kR) * M + xr / kR;
       }
-      for (int kb = 0, kq = 0; kb < n; kb += kR, ++kq) {
+      int kq = 0;
+      for (; kq < nblk; ++kq) {
 #pragma unroll
         for (int k4 = 0; k4 < kR; k4 += 4) {
-          const float4 c4 = *reinterpret_cast<const float4 *>(tp + kb + k4);
+          const float4 c4 = *reinterpret_cast<const float4 *>(tp + kq * kR + k4);
           const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
           for (int jj = 0; jj < 4; ++jj) {
             const int kk = k4 + jj;
+#pragma unroll
+            for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cfs[jj], win[(i + kk) % kR], acc[i]);
+            win[kk] = Y[pre[kk] + kq];
+          }
+        }
+      }
+      // the last partial block: the same steps, stopping after `tail` taps
+      // (no zero taps are issued; every width of 17 taps or more has a
+      // 1-tap tail)
+      if (tail) {
+#pragma unroll
+        for (int k4 = 0; k4 < kR; k4 += 4) {
+          if (k4 >= tail) break;
+          const float4 c4 = *reinterpret_cast<const float4 *>(tp + kq * kR + k4);
+          const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int kk = k4 + jj;
+            if (kk >= tail) break;
 #pragma unroll
             for (int i = 0; i < kR; ++i) acc[i] = __fmaf_rn(cfs[jj], win[(i + kk) % kR], acc[i]);
             win[kk] = Y[pre[kk] + kq];

@@ -179,6 +179,8 @@ struct SmoothArgs {
   const int *tap_off;       // [nbox] offset into taps
   const int *tap_n;         // [nbox] padded tap count (multiple of 16)
   float snr;
+  int split;                // FIR: first width of the second width group
+                            // (w0 + nw: one group); set by smooth_planes
 };
 // Shared memory of the FIR launch.
 size_t fir_smem_bytes(const SmoothArgs &a);

@@ -27,6 +27,8 @@
 // that cannot hold a candidate.
 #include "hg_internal.h"
 
+#include <algorithm>
+
 namespace hg {
 namespace {
 
@@ -179,6 +181,190 @@ __global__ void __launch_bounds__(kT) k_fir(SmoothArgs a) {
     if ((tid & 31) == 0) {
       B.rowmean[(size_t)(w0 + j) * h + r] = __fdiv_rn(tot, (float)nwcol);
       B.rowmax[(size_t)(w0 + j) * h + r] = mx;
+    }
+  }
+}
+
+// k_firR: the arithmetic of k_fir with R outputs per thread (R = 16 or
+// 32) and 128 threads per (row, width group); widths [w0, split) form
+// group 0 and [split, w0 + nw) group 1 (blockIdx.y), so that a short list
+// of long rows still fills the GPU.  The chunk's y values are staged in an
+// R-phase layout with a compile-time phase stride M and 2R phase rows,
+//   Y[p * M + c] = y(R c + p)   (p < 2R, c < M),
+// so that for every width (off = R O + o) window element n of thread t is
+// Y[(o + n % R) * M + t + O + n / R]: one base address per width, and
+// every load of the tap loop sits at a constant offset from it.  Outputs
+// go to global memory straight from registers; the row-mean partials of
+// the reference's order (owner j sums columns j, j + 256, ...) read them
+// back through a swizzled shared transpose (conflict-free both ways).
+constexpr int kTF = 128;  // threads per block
+
+// float4 slot q of thread t's R outputs sits at slot q ^ fir_swz_key(t).
+template <int R>
+__device__ __forceinline__ int fir_swz_key(int t) {
+  return R == 32 ? (t & 7) : ((t >> 1) & 3);
+}
+// Transposed position of chunk column c.
+template <int R>
+__device__ __forceinline__ int fir_swz(int c) {
+  const int t = c / R, q = (c % R) >> 2;
+  return R * t + 4 * (q ^ fir_swz_key<R>(t)) + (c & 3);
+}
+
+template <int R, int M>
+__global__ void __launch_bounds__(kTF, R == 32 ? 3 : 5) k_firR(SmoothArgs a) {
+  constexpr int kC = R * kTF;  // outputs per chunk
+  extern __shared__ __align__(16) float sm[];
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  if (!*B.active) return;
+  const int wb = blockIdx.y == 0 ? a.w0 : a.split, we = blockIdx.y == 0 ? a.split : a.w0 + a.nw;
+  const int nw = we - wb;
+  if (nw <= 0) return;
+  const int h = B.h, tid = threadIdx.x;
+  const int span = 2 * (a.wmin << (a.w0 + a.nw - 1));
+  const int tap0 = a.tap_off[wb];
+  int ntaps_total = 0;
+  for (int b = wb; b < we; ++b) ntaps_total += a.tap_n[b];
+  float *taps = sm;
+  float *Y = taps + ((ntaps_total + 3) / 4) * 4;
+  float *out_s = Y + 2 * R * M;
+  float *part_s = out_s + kC;        // [nw][256] row-mean partials
+  float *max_s = part_s + nw * 256;  // [nw][kTF] row maxima
+  for (int i = tid; i < ntaps_total; i += kTF) taps[i] = a.taps[tap0 + i];
+  for (int j = 0; j < nw; ++j) {
+    part_s[j * 256 + tid] = 0.f;
+    part_s[j * 256 + kTF + tid] = 0.f;
+    max_s[j * kTF + tid] = -INFINITY;
+  }
+  const float *ra = B.dd + (size_t)r * B.dd_stride;
+  const float *rb = ra + B.dd_stride;
+  const float *rc = rb + B.dd_stride;
+  const int nwcol = 256 * (a.ntime_out / 256);
+  const int org = a.wmax / 2 - (a.anchor ? span : 0);
+
+  constexpr int NY = R * (M + 1);                // staged y values
+  constexpr int NX = (NY + kTF - 1) / kTF;       // per thread
+  constexpr int XB = 6;                          // loads in flight per thread
+  for (int cs = 0; cs < a.ntime_out; cs += kC) {
+    __syncthreads();
+    for (int i0 = 0; i0 < NX; i0 += XB) {
+      float va[XB], vb[XB], vc[XB];
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        int col = cs + org + tid + (i0 + u) * kTF;
+        col = col < 0 ? 0 : (col >= a.ntime_dd ? a.ntime_dd - 1 : col);
+        va[u] = ra[col];
+        vb[u] = rb[col];
+        vc[u] = rc[col];
+      }
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        const int x = tid + (i0 + u) * kTF;
+        const int c = x / R, p = x % R;
+        if (x < NY) {
+          const float y = __fmaf_rn(0.3f, __fadd_rn(va[u], vc[u]), vb[u]);
+          if (c < M) Y[p * M + c] = y;
+          if (c >= 1) Y[(p + R) * M + c - 1] = y;
+        }
+      }
+    }
+    __syncthreads();
+    const bool valid = cs + R * tid < a.ntime_out;  // ntime_out % R == 0
+    for (int j = 0; j < nw; ++j) {
+      const int b = wb + j;
+      const int smw = a.wmin << b;
+      const int off = a.anchor ? span - 2 * smw : 0;
+      const float *tp = taps + a.tap_off[b] - tap0;
+      const int ntap = 2 * smw + 1, nblk = ntap / R, tail = ntap % R;
+      const float *Yp = Y + (off % R) * M + tid + off / R;
+      // win[(i + kk) % R] holds y at window element R kq + kk + i of output
+      // i; slot kk is refilled after step kk of block kq
+      float acc[R], win[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        acc[i] = 0.f;
+        win[i] = Yp[i * M];
+      }
+      // taps are read one group of four ahead (cn); ntap is odd, so the
+      // group after the last full block is the tail's first
+      float4 cn = *reinterpret_cast<const float4 *>(tp);
+      int kq = 0;
+      for (; kq < nblk; ++kq) {
+        const float *Yq = Yp + kq + 1;
+        const float *tq = tp + kq * R;
+#pragma unroll
+        for (int k4 = 0; k4 < R; k4 += 4) {
+          const float4 c4 = cn;
+          cn = *reinterpret_cast<const float4 *>(tq + k4 + 4);
+          const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int kk = k4 + jj;
+#pragma unroll
+            for (int i = 0; i < R; ++i) acc[i] = __fmaf_rn(cfs[jj], win[(i + kk) % R], acc[i]);
+            win[kk] = Yq[kk * M];
+          }
+        }
+      }
+      if (tail) {  // the last `tail` taps (no zero taps are issued)
+        const float *Yq = Yp + kq + 1;
+        const float *tq = tp + kq * R;
+#pragma unroll
+        for (int k4 = 0; k4 < R; k4 += 4) {
+          if (k4 >= tail) break;
+          const float4 c4 = cn;
+          if (k4 + 4 < tail) cn = *reinterpret_cast<const float4 *>(tq + k4 + 4);
+          const float cfs[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int kk = k4 + jj;
+            if (kk >= tail) break;
+#pragma unroll
+            for (int i = 0; i < R; ++i) acc[i] = __fmaf_rn(cfs[jj], win[(i + kk) % R], acc[i]);
+            win[kk] = Yq[kk * M];
+          }
+        }
+      }
+      if (valid) {
+        float4 *dst = reinterpret_cast<float4 *>(B.boxes + ((size_t)(b - a.w0) * h + r) * a.ntime_out + cs +
+                                                 R * tid);
+        float mx = max_s[j * kTF + tid];
+#pragma unroll
+        for (int q = 0; q < R / 4; ++q) {
+          dst[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+          mx = fmaxf(fmaxf(fmaxf(mx, acc[4 * q]), fmaxf(acc[4 * q + 1], acc[4 * q + 2])), acc[4 * q + 3]);
+        }
+        max_s[j * kTF + tid] = mx;
+      }
+      const int key = fir_swz_key<R>(tid);
+#pragma unroll
+      for (int q = 0; q < R / 4; ++q)
+        *reinterpret_cast<float4 *>(out_s + R * tid + 4 * (q ^ key)) =
+            make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+      __syncthreads();
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int jo = tid + kTF * hh, c0 = cs + jo;
+        const int nm = c0 < nwcol ? min(kC / 256, (nwcol - c0 + 255) >> 8) : 0;
+        const float *src = out_s + fir_swz<R>(jo);  // column jo + 256 m at src[256 m]
+        float ps = part_s[j * 256 + jo];
+#pragma unroll
+        for (int m = 0; m < kC / 256; ++m)
+          if (m < nm) ps = __fadd_rn(ps, src[256 * m]);
+        part_s[j * 256 + jo] = ps;
+      }
+      __syncthreads();
+    }
+  }
+  for (int j = tid >> 5; j < nw; j += kTF / 32) {
+    const float tot = block256_tree(part_s + j * 256);
+    float mx = -INFINITY;
+    for (int i = threadIdx.x & 31; i < kTF; i += 32) mx = fmaxf(mx, max_s[j * kTF + i]);
+    for (int o = 16; o > 0; o /= 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) {
+      B.rowmean[(size_t)(wb + j) * h + r] = __fdiv_rn(tot, (float)nwcol);
+      B.rowmax[(size_t)(wb + j) * h + r] = mx;
     }
   }
 }
@@ -384,8 +570,83 @@ size_t fir_smem_bytes(const SmoothArgs &a) {
   return sizeof(float) * ((size_t)(ntot + 3) / 4 * 4 + (size_t)kR * M + kCH + (size_t)2 * a.nw * kT);
 }
 
-cudaError_t smooth_planes(const SmoothArgs &a, cudaStream_t s) {
-  if (a.nrows <= 0 || a.nw <= 0) return cudaSuccess;
+namespace {
+
+// Outputs per thread of k_firR.
+constexpr int kFirR = 16;
+
+// Instantiated phase strides of k_firR (odd, so that staging stores of a
+// warp spread over the banks): spans up to 64, 512 and 2048.
+template <int R>
+struct FirStrides {
+  static constexpr int m0 = (129 + 65 / R) | 1, m1 = (129 + 513 / R) | 1, m2 = (129 + 2049 / R) | 1;
+};
+// Phase stride for the launch's span: the smallest instantiated M >= 129 +
+// (span + 1) / R (the last column the tap loop reads), or 0.
+template <int R>
+int fir_stride(int span) {
+  const int need = 129 + (span + 1) / R;
+  for (int m : {FirStrides<R>::m0, FirStrides<R>::m1, FirStrides<R>::m2})
+    if (need <= m) return m;
+  return 0;
+}
+
+template <int R>
+size_t firR_smem(const SmoothArgs &a, int M) {
+  size_t best = 0;
+  for (int g = 0; g < 2; ++g) {
+    const int wb = g == 0 ? a.w0 : a.split, we = g == 0 ? a.split : a.w0 + a.nw;
+    if (we <= wb) continue;
+    int ntot = 0;
+    for (int b = wb; b < we; ++b) ntot += ((2 * (a.wmin << b) + 1 + 15) / 16) * 16;
+    const size_t f =
+        (size_t)(ntot + 3) / 4 * 4 + (size_t)2 * R * M + (size_t)R * kTF + (size_t)(we - wb) * (256 + kTF);
+    best = std::max(best, f * sizeof(float));
+  }
+  return best;
+}
+
+template <int R, int M>
+cudaError_t launch_firR(const SmoothArgs &a, cudaStream_t s) {
+  const size_t smem = firR_smem<R>(a, M);
+  cudaError_t e = cudaFuncSetAttribute(k_firR<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_firR<R, M><<<dim3(a.nrows, a.split < a.w0 + a.nw ? 2 : 1), kTF, smem, s>>>(a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t smooth_planes(const SmoothArgs &a0, cudaStream_t s) {
+  if (a0.nrows <= 0 || a0.nw <= 0) return cudaSuccess;
+  SmoothArgs a = a0;
+  a.split = a.w0 + a.nw;
+  const int M = a.ntime_out % kFirR == 0 ? fir_stride<kFirR>(2 * (a.wmin << (a.w0 + a.nw - 1))) : 0;
+  if (M) {
+    // two width groups of about equal taps when the rows alone would leave
+    // the GPU in few waves (fewer than 16 of three blocks per SM)
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return cudaErrorInvalidDevice;
+    if (a.nw > 1 && a.nrows < 16 * 3 * nsm) {
+      long tot = 0, run = 0, best = -1;
+      for (int b = a.w0; b < a.w0 + a.nw; ++b) tot += 2 * (a.wmin << b) + 1;
+      for (int b = a.w0; b < a.w0 + a.nw - 1; ++b) {
+        run += 2 * (a.wmin << b) + 1;
+        const long worst = std::max(run, tot - run);
+        if (best < 0 || worst < best) {
+          best = worst;
+          a.split = b + 1;
+        }
+      }
+    }
+    using F = FirStrides<kFirR>;
+    if (M == F::m0) return launch_firR<kFirR, F::m0>(a, s);
+    if (M == F::m1) return launch_firR<kFirR, F::m1>(a, s);
+    return launch_firR<kFirR, F::m2>(a, s);
+  }
   const size_t smem = fir_smem_bytes(a);
   cudaError_t e = cudaFuncSetAttribute(k_fir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

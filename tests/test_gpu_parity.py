@@ -158,6 +158,39 @@ def test_search_stages_bit_exact(hella, oracle):
     assert len(got) > 0
 
 
+@pytest.mark.parametrize("wmin,wmax,anchor", [
+    (1, 16, 1),     # span 16: 32-output kernel, stride 131
+    (3, 400, 1),    # odd widths 3..384, span 768: stride 193, odd window offsets
+    (1, 2048, 0),   # widths up to 1024, span 2048: the largest 32-output stride
+    (1, 4096, 1),   # span 4096: the 16-output fallback kernel
+    (5, 11, 0),     # a single width
+])
+def test_smoothing_width_sets_bit_exact(hella, oracle, wmin, wmax, anchor):
+    """Smoothed planes, per-width statistics and candidates for width sets
+    that take each FIR kernel and shared-memory stride."""
+    p = small_params(nchan=128, gulp=4096, dm_max=60.0, width_min=wmin, width_max=wmax, smooth_anchor=anchor,
+                     snr=5.0)
+    sky = synth.Sky(p["nchan"], p["tsamp"], p["f0_mhz"], p["df_mhz"], seed=31 + wmin, rfi_chans=(9,), slope=0.2)
+    s, pl = _run_to_search(hella, oracle, p, sky)
+    x = sky.gulp(pl.min_gulp, p["gulp"])[None]
+    s.clear_peaks()
+    s.load_gulp(x)
+    s.fast_flagger()
+    win = s.copy_window(0)
+    pl.gulp_step(x)
+    ref = pl.search_window(win, 0)
+    s.dedisperse(0)
+    s.smooth(1)
+    mean, std, s0 = s.smooth_stats()
+    boxes = s.copy_boxes()
+    assert boxes.shape == ref["boxes"].shape
+    assert np.array_equal(boxes.view(np.uint32), ref["boxes"].view(np.uint32))
+    assert np.array_equal(mean.view(np.uint32), ref["mean"].view(np.uint32))
+    assert np.array_equal(std.view(np.uint32), ref["std"].view(np.uint32))
+    s.find_peaks(0)
+    assert cands_equal(s.get_peaks(), ref["cands"])
+
+
 @pytest.mark.parametrize("anchor", [0, 1])
 def test_gulp_loop_multibeam(hella, oracle, anchor):
     params, _ = synth.config_plain(seed=7, nchan=128, gulp=2048, dm_max=400.0)

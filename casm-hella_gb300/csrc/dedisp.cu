@@ -172,7 +172,11 @@ __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
 // MODE picks how the integer adds are spread over the SM's pipes (the
 // sums are identical): 0 = three-input adds throughout; 1 = load addresses
 // as multiply-adds by a runtime 1 (FMA pipe); 2 = as 1, and the odd-sample
-// lanes accumulated by multiply-adds as well.
+// lanes accumulated by multiply-adds as well; 3 = two-input address adds
+// (which issue on the full-rate FMA pipes), odd lanes by multiply-adds.
+// Byte permutes and three-input adds share the half-rate ALU pipe, and
+// multiply-adds the half-rate heavy FMA pipe, so MODE 3 leaves 2.5 ALU
+// and 2 multiply-add instructions per word.
 template <int DPT, int CC, int MODE>
 __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int rowstride, int nbuf) {
   extern __shared__ __align__(128) uint32_t smem[];
@@ -313,10 +317,11 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
           for (int j = 0; j < 4; ++j) {
             const int m = 4 * q + j;
             if (m < DPT) {
-              const uint32_t w1 = lds32(MODE ? (uint32_t)o1[j] * unit + r1 : r1 + (uint32_t)o1[j]);
-              const uint32_t w2 = lds32(MODE ? (uint32_t)o2[j] * unit + r2 : r2 + (uint32_t)o2[j]);
+              constexpr bool kMadAddr = MODE == 1 || MODE == 2;
+              const uint32_t w1 = lds32(kMadAddr ? (uint32_t)o1[j] * unit + r1 : r1 + (uint32_t)o1[j]);
+              const uint32_t w2 = lds32(kMadAddr ? (uint32_t)o2[j] * unit + r2 : r2 + (uint32_t)o2[j]);
               acc_e[m] += __byte_perm(w1, 0u, 0x4240) + __byte_perm(w2, 0u, 0x4240);
-              if (MODE == 2) {
+              if (MODE >= 2) {
                 acc_o[m] = __byte_perm(w1, 0u, 0x4341) * unit + acc_o[m];
                 acc_o[m] = __byte_perm(w2, 0u, 0x4341) * unit + acc_o[m];
               } else {
@@ -547,7 +552,7 @@ cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
 
 template <int DPT>
 cudaError_t launch_cc(const DedispArgs &a, cudaStream_t s) {
-  if (DPT < 8 && a.mode != 0) return cudaErrorInvalidValue;  // modes 1-2: 8 and 16-trial tiles
+  if (DPT < 8 && a.mode != 0) return cudaErrorInvalidValue;  // modes 1-3: 8 and 16-trial tiles
   switch (a.cc * 4 + (DPT < 8 ? 0 : a.mode)) {
     case 32: return launch<DPT, 8, 0>(a, s);
     case 64: return launch<DPT, 16, 0>(a, s);
@@ -555,6 +560,8 @@ cudaError_t launch_cc(const DedispArgs &a, cudaStream_t s) {
     case 65: return launch<DPT, 16, DPT < 8 ? 0 : 1>(a, s);
     case 34: return launch<DPT, 8, DPT < 8 ? 0 : 2>(a, s);
     case 66: return launch<DPT, 16, DPT < 8 ? 0 : 2>(a, s);
+    case 35: return launch<DPT, 8, DPT < 8 ? 0 : 3>(a, s);
+    case 67: return launch<DPT, 16, DPT < 8 ? 0 : 3>(a, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -369,16 +369,33 @@ __global__ void __launch_bounds__(kTF, R == 32 ? 3 : 5) k_firR(SmoothArgs a) {
   }
 }
 
-// Host loop of calculate_stddev (normalization.cu:138-142): sequential over
-// rows, / height.  Block = beam, thread = width of the launch.
-__global__ void k_mean_finish(SmoothArgs a) {
-  const SmoothBeam &B = a.beams[blockIdx.x];
-  const int j = threadIdx.x;
-  if (j >= a.nw || !*B.active) return;
-  const int b = a.w0 + j, h = B.h;
+// Sequential sum of v[0..n) in index order (the reference's host loop),
+// in thread 0 of a kFin-thread block: the block stages kFinChunk values at
+// a time in shared memory with coalesced loads, thread 0 adds them.
+constexpr int kFin = 256, kFinChunk = 4096;
+__device__ float block_seq_sum(const float *v, int n, float *chunk_s) {
   float s = 0.f;
-  for (int r = 0; r < h; ++r) s = __fadd_rn(s, B.rowmean[(size_t)b * h + r]);
-  B.stats[b * 4 + 0] = __fdiv_rn(s, (float)h);
+  for (int c0 = 0; c0 < n; c0 += kFinChunk) {
+    const int m = min(kFinChunk, n - c0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += kFin) chunk_s[i] = v[c0 + i];
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int i = 0; i < m; ++i) s = __fadd_rn(s, chunk_s[i]);
+  }
+  return s;
+}
+
+// Host loop of calculate_stddev (normalization.cu:138-142): sequential over
+// rows, / height.  Block = (beam, width of the launch).
+__global__ void __launch_bounds__(kFin) k_mean_finish(SmoothArgs a) {
+  __shared__ float chunk_s[kFinChunk];
+  const SmoothBeam &B = a.beams[blockIdx.x];
+  const int j = blockIdx.y;
+  if (!*B.active) return;
+  const int b = a.w0 + j, h = B.h;
+  const float s = block_seq_sum(B.rowmean + (size_t)b * h, h, chunk_s);
+  if (threadIdx.x == 0) B.stats[b * 4 + 0] = __fdiv_rn(s, (float)h);
 }
 
 // computeRowVariances over one row of one width plane.  NORM0: the
@@ -416,13 +433,14 @@ __global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
 // Per (beam, width): variance -> std and the normalisation constants.
 // NORM0: the gate statistics of the normalised width-0 plane.
 template <bool NORM0, bool VAR>
-__global__ void k_stat_finish(SmoothArgs a) {
+__global__ void __launch_bounds__(kFin) k_stat_finish(SmoothArgs a) {
+  __shared__ float chunk_s[kFinChunk];
   const SmoothBeam &B = a.beams[blockIdx.x];
-  const int j = threadIdx.x;
-  if (j >= (NORM0 ? 1 : a.nw) || !*B.active) return;
+  const int j = NORM0 ? 0 : blockIdx.y;
+  if (!*B.active) return;
   const int b = NORM0 ? 0 : a.w0 + j, h = B.h;
-  float s = 0.f;
-  for (int r = 0; r < h; ++r) s = __fadd_rn(s, B.rowvar[(size_t)b * h + r]);
+  float s = block_seq_sum(B.rowvar + (size_t)b * h, h, chunk_s);
+  if (threadIdx.x != 0) return;
   s = __fdiv_rn(s, (float)h);
   if (NORM0) {
     if (!VAR) {
@@ -659,9 +677,9 @@ cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale) {
   if (a.nrows <= 0 || a.nw <= 0) return cudaSuccess;
   unsigned n = 0;
   if (scale) {
-    k_mean_finish<<<a.nbeam, 32, 0, s>>>(a);
+    k_mean_finish<<<dim3(a.nbeam, a.nw), kFin, 0, s>>>(a);
     k_row_stat<false, true><<<dim3(a.nrows, a.nw), kT, 0, s>>>(a);
-    k_stat_finish<false, true><<<a.nbeam, 32, 0, s>>>(a);
+    k_stat_finish<false, true><<<dim3(a.nbeam, a.nw), kFin, 0, s>>>(a);
     n += 3;
   } else {
     k_stat_zero<<<a.nbeam, 32, 0, s>>>(a);
@@ -669,9 +687,9 @@ cudaError_t smooth_stats(const SmoothArgs &a, cudaStream_t s, int scale) {
   }
   if (a.w0 == 0) {  // the gate statistics of the normalised width-0 plane
     k_row_stat<true, false><<<dim3(a.nrows, 1), kT, 0, s>>>(a);
-    k_stat_finish<true, false><<<a.nbeam, 32, 0, s>>>(a);
+    k_stat_finish<true, false><<<a.nbeam, kFin, 0, s>>>(a);
     k_row_stat<true, true><<<dim3(a.nrows, 1), kT, 0, s>>>(a);
-    k_stat_finish<true, true><<<a.nbeam, 32, 0, s>>>(a);
+    k_stat_finish<true, true><<<a.nbeam, kFin, 0, s>>>(a);
     n += 4;
   }
   count_launches(n);

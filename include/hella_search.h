@@ -103,8 +103,9 @@ typedef struct {
                              that fits two blocks per SM */
   int group;              /* DM tiles walked together per time tile (L2) */
   int add_mode;           /* 0: three-input adds; 1: load addresses as
-                             multiply-adds (FMA pipe); 2: 1 + odd lanes too
-                             (1 and 2 need dm_per_block >= 8) */
+                             multiply-adds (FMA pipe); 2: 1 + odd lanes too;
+                             3: odd lanes as multiply-adds, addresses as
+                             two-input adds (1-3 need dm_per_block >= 8) */
 } hella_tuning;
 
 /* Derived sizes (casm_hella_refactored.cu:184-224). */

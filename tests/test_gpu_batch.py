@@ -64,7 +64,7 @@ def test_batch_tile_shapes_agree(hella):
     params, ceilings, kill, skies = _setup(seed=50)
     base = hella.default_params(**dict(params, nbeam=NB))
     outs = []
-    for t in [(0, 4, 8, 0, 8, 0), (8, 4, 16, 2, 1, 1), (16, 4, 8, 3, 4, 2)]:
+    for t in [(0, 4, 8, 0, 8, 0), (8, 4, 16, 2, 1, 1), (16, 4, 8, 3, 4, 2), (16, 4, 16, 2, 8, 3)]:
         bt = hella.Batch(base, dm_max=ceilings, killmask=kill)
         bt.set_tuning(hella.HellaTuning(*t))
         res = []

@@ -29,7 +29,6 @@
 namespace hg {
 namespace {
 
-constexpr int kCT = 32;  // channels per block (a warp spans channels)
 
 __device__ __forceinline__ __half hzero() { return __float2half_rn(0.f); }
 __device__ __forceinline__ __half hone() { return __float2half_rn(1.f); }
@@ -61,27 +60,52 @@ __global__ void k_build_lut(FlagState st, int stage) {
   st.lut[((size_t)b * st.nchan + c) * 256 + v] = chain_value(stage, v, st, b, c);
 }
 
-// Stage a block's 32-channel slice of the table as lut_s[level][channel]:
-// lanes (consecutive channels) then hit at most two-way bank conflicts.
-__device__ __forceinline__ void load_lut_slice(__half (*lut_s)[kCT],
-                                               const __half *lut, int nchan,
-                                               int b, int c0) {
+// The row-statistics pass in a four-channel form: lane t of a warp holds
+// channels c0 + 4t .. c0 + 4t + 3 (one 32-bit load per row feeds four
+// chains, each summed in the reference's order), warps hold columns.  The
+// block's 128-channel slice of the table is staged as
+// lut_s[level * kQC + channel] through 16-byte loads of eight levels.
+constexpr int kQC = 128;
+constexpr int kRowT = 512;  // threads per block
+constexpr size_t kLutSlice = (size_t)256 * kQC * sizeof(__half);
+
+__device__ __forceinline__ void load_lut_slice4(__half *lut_s, const __half *lut, int nchan, int b,
+                                                int c0) {
+  const int ncl = min(kQC, nchan - c0);
   const __half *lb = lut + ((size_t)b * nchan + c0) * 256;
-  for (int i = threadIdx.x; i < kCT * 256; i += blockDim.x) {
-    int cc = i >> 8, v = i & 255;
-    lut_s[v][cc] = lb[(size_t)cc * 256 + v];
+  for (int i = threadIdx.x; i < kQC * 32; i += blockDim.x) {
+    const int cc = i % kQC, vb = i / kQC;  // levels 8vb .. 8vb+7 of channel cc
+    if (cc < ncl) {
+      const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
+      const __half *h = reinterpret_cast<const __half *>(&q);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) lut_s[(8 * vb + k) * kQC + cc] = h[k];
+    }
   }
 }
 
 // calc_bandpass_new partials: lane l of channel c sums samples l, l+32, ...
-// (below 32*floor(w/32)) in time order.  Block = 32 channels x 8 lanes.
+// (below 32*floor(w/32)) in time order.  Block = 32 channels x 8 lanes, one
+// chain a thread (65536 chains for 2048 channels: too few for the
+// four-channel form to hide the memory latency); the row bytes are loaded
+// kLaneB at a time so that as many loads are in flight.  The table slice
+// is staged as lut_s[level][channel] through 16-byte loads of eight levels.
+constexpr int kLaneC = 32, kLaneB = 16;
 __global__ void __launch_bounds__(256) k_lane_partials(const uint8_t *__restrict__ gulp,
                                                        const __half *__restrict__ lut,
-                                                       float *__restrict__ part,
-                                                       int nchan, int w) {
-  __shared__ __half lut_s[256][kCT];
-  const int b = blockIdx.z, c0 = blockIdx.x * kCT;
-  load_lut_slice(lut_s, lut, nchan, b, c0);
+                                                       float *__restrict__ part, int nchan, int w) {
+  __shared__ __half lut_s[256][kLaneC];
+  const int b = blockIdx.z, c0 = blockIdx.x * kLaneC;
+  {
+    const __half *lb = lut + ((size_t)b * nchan + c0) * 256;
+    for (int i = threadIdx.x; i < kLaneC * 32; i += blockDim.x) {
+      const int cc = i % kLaneC, vb = i / kLaneC;  // levels 8vb .. 8vb+7 of channel cc
+      const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
+      const __half *h = reinterpret_cast<const __half *>(&q);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) lut_s[8 * vb + k][cc] = h[k];
+    }
+  }
   __syncthreads();
   const int cl = threadIdx.x & 31, l = blockIdx.y * 8 + (threadIdx.x >> 5);
   const int c = c0 + cl;
@@ -89,9 +113,60 @@ __global__ void __launch_bounds__(256) k_lane_partials(const uint8_t *__restrict
   const size_t step = (size_t)32 * nchan;
   const int np = w / 32;
   float s = 0.f;
-#pragma unroll 8
-  for (int i = 0; i < np; ++i) s = __fadd_rn(s, __half2float(lut_s[g[i * step]][cl]));
+  int i = 0;
+  for (; i + kLaneB <= np; i += kLaneB) {
+    uint32_t v[kLaneB];
+#pragma unroll
+    for (int u = 0; u < kLaneB; ++u) v[u] = g[(size_t)(i + u) * step];
+#pragma unroll
+    for (int u = 0; u < kLaneB; ++u) s = __fadd_rn(s, __half2float(lut_s[v[u]][cl]));
+  }
+  for (; i < np; ++i) s = __fadd_rn(s, __half2float(lut_s[g[(size_t)i * step]][cl]));
   part[((size_t)b * nchan + c) * 32 + l] = s;
+}
+
+// computeRowMeans / computeRowVariances partials: column j of channel c
+// sums columns j, j+256, ... below nw = 256*floor(w/256).  TS: values
+// divided by half(ts[t]) (divide_by_ts, timeseries.cu:38-55).  VAR:
+// (x - mean)^2 with the fused multiply-add the reference's compiler emits.
+template <bool VAR, bool TS>
+__global__ void __launch_bounds__(kRowT) k_row_partials(const uint8_t *__restrict__ gulp, FlagState st,
+                                                         int which) {
+  extern __shared__ __align__(16) __half lut4_s[];
+  const int b = blockIdx.z, c0 = blockIdx.x * kQC, nchan = st.nchan, w = st.gulp;
+  load_lut_slice4(lut4_s, st.lut, nchan, b, c0);
+  __syncthreads();
+  const int cq = 4 * (threadIdx.x & 31), c = c0 + cq;
+  const int j = blockIdx.y * (kRowT / 32) + (threadIdx.x >> 5);
+  if (c >= nchan) return;
+  const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)j * nchan + c;
+  const __half *hts = st.hts + (size_t)b * w + j;
+  const size_t step = (size_t)256 * nchan;
+  const int nk = w / 256;
+  const float mean = VAR ? st.scal[b * 8 + 2 * which] : 0.f;
+  const __half *ls = lut4_s + cq;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+  for (int k = 0; k < nk; ++k) {
+    const uint32_t x = *reinterpret_cast<const uint32_t *>(g + k * step);
+    __half th;
+    if (TS) th = hts[k * 256];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      __half hv = ls[((x >> (8 * q)) & 255u) * kQC + q];
+      if (TS) hv = __hdiv(hv, th);
+      const float f = __half2float(hv);
+      if (VAR) {
+        const float d = __fsub_rn(f, mean);
+        acc[q] = __fmaf_rn(d, d, acc[q]);
+      } else {
+        acc[q] = __fadd_rn(acc[q], f);
+      }
+    }
+  }
+  float *pp = st.part + ((size_t)b * nchan + c) * 256 + j;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) pp[q * 256] = acc[q];
 }
 
 // Warp tree over the 32 lane partials, / w (flagger.cu:103-111).  One warp
@@ -112,40 +187,6 @@ __global__ void k_lane_finish(FlagState st, int mode) {
     if (mode == 2) st.bp3[gw] = bp;
     if (mode == 3) st.bpx[gw] = bp;
   }
-}
-
-// computeRowMeans / computeRowVariances partials: thread j of channel c sums
-// columns j, j+256, ... below nw = 256*floor(w/256).  TS: values divided by
-// half(ts[t]) (divide_by_ts, timeseries.cu:38-55).  VAR: (x - mean)^2 with
-// the fused multiply-add the reference's compiler emits.
-template <bool VAR, bool TS>
-__global__ void __launch_bounds__(256) k_row_partials(const uint8_t *__restrict__ gulp,
-                                                      FlagState st, int which) {
-  __shared__ __half lut_s[256][kCT];
-  const int b = blockIdx.z, c0 = blockIdx.x * kCT, nchan = st.nchan, w = st.gulp;
-  load_lut_slice(lut_s, st.lut, nchan, b, c0);
-  __syncthreads();
-  const int cl = threadIdx.x & 31, j = blockIdx.y * 8 + (threadIdx.x >> 5);
-  const int c = c0 + cl;
-  const uint8_t *g = gulp + (size_t)b * w * nchan + (size_t)j * nchan + c;
-  const __half *hts = st.hts + (size_t)b * w + j;
-  const size_t step = (size_t)256 * nchan;
-  const int nk = w / 256;
-  const float mean = VAR ? st.scal[b * 8 + 2 * which] : 0.f;
-  float s = 0.f;
-#pragma unroll 4
-  for (int k = 0; k < nk; ++k) {
-    __half hv = lut_s[g[k * step]][cl];
-    if (TS) hv = __hdiv(hv, hts[k * 256]);
-    float f = __half2float(hv);
-    if (VAR) {
-      float d = __fsub_rn(f, mean);
-      s = __fmaf_rn(d, d, s);
-    } else {
-      s = __fadd_rn(s, f);
-    }
-  }
-  st.part[((size_t)b * nchan + c) * 256 + j] = s;
 }
 
 // Thread 0 of the reference's 256-thread block: each warp's shuffle tree,
@@ -543,8 +584,19 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   if (st.f16_input) return scrunch_planes(st, gulp_in, plain, R, wpos, dpos, s);
   const uint8_t *gulp = static_cast<const uint8_t *>(gulp_in);
   const dim3 lutg(st.nchan, st.nbeam);
-  const dim3 laneg(st.nchan / kCT, 32 / 8, st.nbeam);
-  const dim3 rowg(st.nchan / kCT, 256 / 8, st.nbeam);
+  const dim3 laneg(st.nchan / kLaneC, 32 / 8, st.nbeam);
+  const dim3 rowg((st.nchan + kQC - 1) / kQC, 256 / (kRowT / 32), st.nbeam);
+  {  // the table slice is above the default 48 KB of dynamic shared memory
+    const int lb = (int)kLutSlice;
+    cudaError_t e = cudaFuncSetAttribute(k_row_partials<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lb);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_row_partials<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lb);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_row_partials<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lb);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_row_partials<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lb);
+    if (e != cudaSuccess) return e;
+  }
   const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
   const int beam_blocks = (st.nbeam + 63) / 64;
 
@@ -554,10 +606,10 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 0);
   k_build_lut<<<lutg, 256, 0, s>>>(st, 1);
   // normalize_data: calculate_stddev (mean pass, variance pass)
-  k_row_partials<false, false><<<rowg, 256, 0, s>>>(gulp, st, 0);
+  k_row_partials<false, false><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 0);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
   k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 0);
-  k_row_partials<true, false><<<rowg, 256, 0, s>>>(gulp, st, 0);
+  k_row_partials<true, false><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 0);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
   k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 0);
   // calc_bandpass_new of the normalised data -> spectral flag
@@ -576,10 +628,10 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   // ... ts_correct ...
   k_ts<<<dim3((st.gulp + kTsT - 1) / kTsT, st.nbeam), kTsT, 0, s>>>(gulp, st);
   // ... normalize_data
-  k_row_partials<false, true><<<rowg, 256, 0, s>>>(gulp, st, 1);
+  k_row_partials<false, true><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 1);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
   k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 1);
-  k_row_partials<true, true><<<rowg, 256, 0, s>>>(gulp, st, 1);
+  k_row_partials<true, true><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 1);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
   k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 1);
   // transpose_output into the ring

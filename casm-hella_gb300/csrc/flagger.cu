@@ -207,14 +207,20 @@ __global__ void k_row_finish(FlagState st) {
 
 // calculate_stddev's host loops (normalization.cu:138-153): sequential sum
 // over channels, / nchan; the variance pass also forms the half-precision
-// normalisation constants of normalize_data (flagger.cu:205-206).
+// normalisation constants of normalize_data (flagger.cu:205-206).  Block =
+// beam: the row values are staged in shared memory with coalesced loads,
+// thread 0 adds them in channel order.
+constexpr int kBeamT = 256, kMaxChan = 8192;  // the largest nchan accepted
 template <bool VAR>
-__global__ void k_beam_sum(FlagState st, int which) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= st.nbeam) return;
+__global__ void __launch_bounds__(kBeamT) k_beam_sum(FlagState st, int which) {
+  __shared__ float rv_s[kMaxChan];
+  const int b = blockIdx.x;
   const float *rv = st.rowval + (size_t)b * st.nchan;
+  for (int c = threadIdx.x; c < st.nchan; c += kBeamT) rv_s[c] = rv[c];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   float s = 0.f;
-  for (int c = 0; c < st.nchan; ++c) s = __fadd_rn(s, rv[c]);
+  for (int c = 0; c < st.nchan; ++c) s = __fadd_rn(s, rv_s[c]);
   s = __fdiv_rn(s, (float)st.nchan);
   if (!VAR) {
     st.scal[b * 8 + 2 * which] = s;
@@ -276,32 +282,52 @@ __device__ __forceinline__ uint8_t requant(__half h) {
 }
 
 // Final stage: divide_by_ts, normalize_data, requantise, and write the
-// channel-major ring (32 x 32 tiles transposed through shared memory).
-__global__ void k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
-                           uint8_t *__restrict__ plain, long R, long wpos, const GulpPos *dpos) {
+// channel-major ring.  Block = 32 channels x kOutT samples: the channels'
+// table slice is staged in shared memory (as in k_lane_partials), each
+// thread maps samples of one channel into a channel-major byte tile
+// (row stride kOutT + 4: conflict-free both ways), and the tile leaves as
+// 4-byte words, 128 bytes of one channel per warp.  The ring position of a
+// gulp (and R) are multiples of 32, so no word straddles the ring's end.
+constexpr int kOutT = 512, kOutC = 32;
+__global__ void __launch_bounds__(256) k_flag_out(const uint8_t *__restrict__ gulp, FlagState st,
+                                                  uint8_t *__restrict__ plain, long R, long wpos,
+                                                  const GulpPos *dpos) {
   if (dpos) wpos = dpos->wpos;
-  __shared__ uint8_t tile[32][33];
-  const int b = blockIdx.z, c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y, nchan = st.nchan, w = st.gulp;
-  const __half a2 = st.hsc[b * 8 + 2], m2 = st.hsc[b * 8 + 3];
-  const uint8_t *g = gulp + (size_t)b * w * nchan;
-  const __half *lb = st.lut + (size_t)b * nchan * 256;
+  __shared__ __half lut_s[256][kOutC];
+  __shared__ __align__(16) uint8_t tile[kOutC][kOutT + 4];
+  const int b = blockIdx.z, c0 = blockIdx.x * kOutC, t0 = blockIdx.y * kOutT;
+  const int nchan = st.nchan, w = st.gulp, tid = threadIdx.x;
+  {
+    const __half *lb = st.lut + ((size_t)b * nchan + c0) * 256;
+    for (int i = tid; i < kOutC * 32; i += 256) {
+      const int cc = i % kOutC, vb = i / kOutC;  // levels 8vb .. 8vb+7 of channel cc
+      const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
+      const __half *h = reinterpret_cast<const __half *>(&q);
 #pragma unroll
-  for (int j = 0; j < 32; j += 8) {
-    const int t = t0 + ty + j, c = c0 + tx;
-    const uint8_t x0 = g[(size_t)t * nchan + c];
-    __half x = __hdiv(lb[(size_t)c * 256 + x0], st.hts[(size_t)b * w + t]);
-    x = __hmul(__hadd(x, a2), m2);
-    tile[ty + j][tx] = requant(x);
+      for (int k = 0; k < 8; ++k) lut_s[8 * vb + k][cc] = h[k];
+    }
   }
   __syncthreads();
-  uint8_t *pb = plain + (size_t)b * nchan * R;
-#pragma unroll
-  for (int j = 0; j < 32; j += 8) {
-    const int c = c0 + ty + j, t = t0 + tx;
-    long pos = wpos + t;
+  const __half a2 = st.hsc[b * 8 + 2], m2 = st.hsc[b * 8 + 3];
+  const uint8_t *g = gulp + (size_t)b * w * nchan + c0;
+  const __half *hts = st.hts + (size_t)b * w;
+  const int cl = tid & 31, tr = tid >> 5;
+  const int nt = min(kOutT, w - t0);
+#pragma unroll 4
+  for (int tt = tr; tt < nt; tt += 8) {
+    const int t = t0 + tt;
+    __half x = __hdiv(lut_s[g[(size_t)t * nchan + cl]][cl], hts[t]);
+    x = __hmul(__hadd(x, a2), m2);
+    tile[cl][tt] = requant(x);
+  }
+  __syncthreads();
+  uint8_t *pb = plain + ((size_t)b * nchan + c0) * R;
+  const int nq = nt / 4;  // w % 32 == 0
+  for (int i = tid; i < kOutC * nq; i += 256) {
+    const int c = i / nq, q = i - c * nq;
+    long pos = wpos + t0 + 4 * q;
     if (pos >= R) pos -= R;
-    pb[(size_t)c * R + pos] = tile[tx][ty + j];
+    *reinterpret_cast<uint32_t *>(pb + (size_t)c * R + pos) = *reinterpret_cast<const uint32_t *>(&tile[c][4 * q]);
   }
 }
 
@@ -511,7 +537,6 @@ cudaError_t scrunch_planes(const FlagState &st, const void *gulp, uint8_t *plain
                            const GulpPos *dpos, cudaStream_t s) {
   const dim3 lutg(st.nchan, st.nbeam);
   const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
-  const int beam_blocks = (st.nbeam + 63) / 64;
   const size_t n = (size_t)st.nbeam * st.nchan * st.gulp;
   const int eb = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
   const dim3 chg(st.nchan, st.nbeam);
@@ -519,10 +544,10 @@ cudaError_t scrunch_planes(const FlagState &st, const void *gulp, uint8_t *plain
   auto normalize = [&](int which) {
     k_plane_rows<false><<<chg, 256, 0, s>>>(st, which);
     k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-    k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, which);
+    k_beam_sum<false><<<st.nbeam, kBeamT, 0, s>>>(st, which);
     k_plane_rows<true><<<chg, 256, 0, s>>>(st, which);
     k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-    k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, which);
+    k_beam_sum<true><<<st.nbeam, kBeamT, 0, s>>>(st, which);
     k_plane_norm<<<eb, 256, 0, s>>>(st, which);
     launches += 7;
   };
@@ -598,7 +623,6 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
     if (e != cudaSuccess) return e;
   }
   const int fin_blocks = (st.nbeam * st.nchan * 32 + 255) / 256;
-  const int beam_blocks = (st.nbeam + 63) / 64;
 
   // bandpass_flag: bandpass_correct (calc_bandpass_new, divide_by_bp)
   k_build_lut<<<lutg, 256, 0, s>>>(st, 0);
@@ -608,10 +632,10 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   // normalize_data: calculate_stddev (mean pass, variance pass)
   k_row_partials<false, false><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 0);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-  k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 0);
+  k_beam_sum<false><<<st.nbeam, kBeamT, 0, s>>>(st, 0);
   k_row_partials<true, false><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 0);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-  k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 0);
+  k_beam_sum<true><<<st.nbeam, kBeamT, 0, s>>>(st, 0);
   // calc_bandpass_new of the normalised data -> spectral flag
   k_build_lut<<<lutg, 256, 0, s>>>(st, 2);
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
@@ -630,25 +654,29 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   // ... normalize_data
   k_row_partials<false, true><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 1);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-  k_beam_sum<false><<<beam_blocks, 64, 0, s>>>(st, 1);
+  k_beam_sum<false><<<st.nbeam, kBeamT, 0, s>>>(st, 1);
   k_row_partials<true, true><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 1);
   k_row_finish<<<fin_blocks, 256, 0, s>>>(st);
-  k_beam_sum<true><<<beam_blocks, 64, 0, s>>>(st, 1);
+  k_beam_sum<true><<<st.nbeam, kBeamT, 0, s>>>(st, 1);
   // transpose_output into the ring
-  k_flag_out<<<dim3(st.nchan / 32, st.gulp / 32, st.nbeam), dim3(32, 8), 0, s>>>(gulp, st, plain,
-                                                                                 R, wpos, dpos);
+  k_flag_out<<<dim3(st.nchan / kOutC, (st.gulp + kOutT - 1) / kOutT, st.nbeam), 256, 0, s>>>(gulp, st, plain,
+                                                                                         R, wpos, dpos);
   count_launches(24);
   return cudaGetLastError();
 }
 }  // namespace
 
+// The ring writers store 4-byte words: the ring length and every write
+// position (gulp starts) are multiples of 32 samples.
 cudaError_t flag_gulp(const FlagState &st, const void *gulp, uint8_t *plain, long R, long wpos,
                       cudaStream_t s) {
+  if (R % 32 != 0 || wpos % 32 != 0 || st.gulp % 32 != 0) return cudaErrorInvalidValue;
   return flag_impl(st, gulp, plain, R, wpos, nullptr, s);
 }
 
 cudaError_t flag_gulp_dev(const FlagState &st, const void *gulp, uint8_t *plain, long R,
                           const GulpPos *pos, cudaStream_t s) {
+  if (R % 32 != 0 || st.gulp % 32 != 0) return cudaErrorInvalidValue;
   return flag_impl(st, gulp, plain, R, 0, pos, s);
 }
 

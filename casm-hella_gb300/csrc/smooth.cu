@@ -413,15 +413,26 @@ __global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
   const float *st = B.stats + b * 4;
   const float mean = NORM0 ? B.gate[0] : st[0];
   float s = 0.f;
-  for (int col = tid; col < nwcol; col += kT) {
-    float v = NORM0 ? normv(x[col], st) : x[col];
+  auto add = [&](float v) {
+    if (NORM0) v = normv(v, st);
     if (VAR) {
       const float d = __fsub_rn(v, mean);
       s = __fmaf_rn(d, d, s);
     } else {
       s = __fadd_rn(s, v);
     }
+  };
+  // eight loads in flight per thread, then the sums in column order
+  constexpr int kB = 8;
+  int col = tid;
+  for (; col + (kB - 1) * kT < nwcol; col += kB * kT) {
+    float v[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) v[u] = x[col + u * kT];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) add(v[u]);
   }
+  for (; col < nwcol; col += kT) add(x[col]);
   p_s[tid] = s;
   __syncthreads();
   if (tid < 32) {

@@ -56,6 +56,11 @@ def args_():
     ap.add_argument("--beams", type=int, default=256, help="beams of the batched workload")
     ap.add_argument("--seconds", type=float, default=600.0, help="sky seconds of the stream workload")
     ap.add_argument("--cutouts", type=int, default=4096, help="cutouts of the refine workload")
+    ap.add_argument("--nchan", type=int, default=0,
+                    help="channels of the full workload (0: 2048); smaller values give the small "
+                         "cases that profiling captures use")
+    ap.add_argument("--dm-max", type=float, default=0.0,
+                    help="DM ceiling of the full workload (0: 2000); a small profiling case")
     return ap.parse_args()
 
 
@@ -105,11 +110,13 @@ PLAIN_WORKLOAD = ("plain single beam: 512 ch 375-468.75 MHz, tsamp 1.048576 ms, 
                   "(0.5 ms pulse), widths 1-32, 7 sigma, one DM-300 burst")
 
 
-def workload(rank: int, ngulps: int = 3, which: str = "full"):
+def workload(rank: int, ngulps: int = 3, which: str = "full", nchan: int = 0, dm_max: float = 0.0):
     import synth
 
     if which == "plain":
         params, sky = synth.config_plain(seed=1 + rank)
+    elif nchan or dm_max:
+        params, sky = synth.config_full(seed=2 + rank, nchan=nchan or 2048, dm_max=dm_max or 2000.0)
     else:
         params, sky = synth.config_full(seed=2 + rank)
     gulps = [sky.gulp(g, params["gulp"]) for g in range(ngulps)]
@@ -185,7 +192,9 @@ def main():
     import hella_gb300 as hg
 
     hg.lib()
-    params, sky, gulps = workload(rank, which=a.workload)
+    if (a.nchan or a.dm_max) and a.workload != "full":
+        raise SystemExit("--nchan and --dm-max apply to the full workload only")
+    params, sky, gulps = workload(rank, which=a.workload, nchan=a.nchan, dm_max=a.dm_max)
     G, nch = params["gulp"], params["nchan"]
     gulp_s = G * params["tsamp"]
     s = hg.Search(hg.default_params(**params, device=local))
@@ -285,7 +294,7 @@ def main():
     achieved = adds / dd_t / 1e12
     peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
     roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES if a.workload == "full" else None,
+            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES if a.workload == "full" and not (a.nchan or a.dm_max) else None,
             "traffic_unit": "bytes per launch (ncu)",
             "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
@@ -313,7 +322,9 @@ def main():
         "vs_baseline": None, "dtype": "u8",
         "data": ("synthetic (seeded noise, 4 RFI channels, 3 broadband impulses, one DM-300 burst)"
                  if a.workload == "plain" else "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)"),
-        "config": {"workload": PLAIN_WORKLOAD if a.workload == "plain" else WORKLOAD, "nchan": nch, "gulp": G,
+        "config": {"workload": PLAIN_WORKLOAD if a.workload == "plain" else
+                   WORKLOAD.replace("2048 ch", f"{nch} ch").replace("DM 0-2000", f"DM 0-{params['dm_max']:g}"),
+                   "nchan": nch, "gulp": G,
                    "tsamp": params["tsamp"],
                    "ndms": info.ndms, "max_delay": info.max_delay, "ntime": info.ntime,
                    "widths": info.nboxcar, "beams_per_gpu": 1, "parallelism": f"replicas{world}",

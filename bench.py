@@ -110,6 +110,21 @@ PLAIN_WORKLOAD = ("plain single beam: 512 ch 375-468.75 MHz, tsamp 1.048576 ms, 
                   "(0.5 ms pulse), widths 1-32, 7 sigma, one DM-300 burst")
 
 
+def job_rate(dist, units: float, seconds: float, device: str = "cuda"):
+    """Whole-job throughput of independent replicas: the units every rank
+    processed over the slowest rank's time.  Returns (rate, slowest seconds).
+    The ranks exchange no data; these two reductions are the only collectives."""
+    if dist is None:
+        return units / seconds, seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
 def workload(rank: int, ngulps: int = 3, which: str = "full", nchan: int = 0, dm_max: float = 0.0):
     import synth
 
@@ -256,12 +271,9 @@ def main():
         fl_ms.append(e[0].elapsed_time(e[1]))
         dd_ms.append(e[1].elapsed_time(e[2]))
         sm_ms.append(e[2].elapsed_time(e[3]))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    value, slowest = job_rate(dist, a.steps * gulp_s, ms / 1e3)
+    ms = slowest * 1e3
     ms_step = ms / a.steps
-    value = world * a.steps * gulp_s / (ms / 1e3)
 
     # ---------------- end to end through the C ABI from pinned host memory
     lat = []
@@ -278,11 +290,7 @@ def main():
         gi += 1
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * a.steps * gulp_s / e2e_s
+    e2e, e2e_s = job_rate(dist, a.steps * gulp_s, e2e_s)
 
     clk = clocks.stop()
 
@@ -409,12 +417,8 @@ def main_batched(a, rank, world, local, dist):
         dev_ms.append(bt.last_gulp_ms())
         ncand.append(len(got))
         gi += 1
-    ms = float(np.sum(dev_ms))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * a.steps * NB * gulp_s / (ms / 1e3)
+    value, slowest = job_rate(dist, a.steps * NB * gulp_s, float(np.sum(dev_ms)) / 1e3)
+    ms = slowest * 1e3
 
     # ---------------- end to end from pinned host memory: two gulps in flight, the upload of
     # gulp k+1 overlapping the search of gulp k (hella_batch_submit / hella_batch_poll)
@@ -431,11 +435,7 @@ def main_batched(a, rank, world, local, dist):
         got, counts, _, l_ms, _ = bt.poll()
         lat.append(l_ms / 1e3)
     e2e_s = time.perf_counter() - w0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * a.steps * NB * gulp_s / e2e_s
+    e2e, e2e_s = job_rate(dist, a.steps * NB * gulp_s, e2e_s)
     clk = clocks.stop()
 
     # ---------------- dedispersion roofline: the all-beam launch alone
@@ -533,6 +533,8 @@ def main_stream(a, rank, world, local, dist):
     lanes = [torch.empty((slots, G, nch), dtype=torch.uint8, pin_memory=True) for _ in range(2)]
     clocks = Clocks(local)
     clocks.start()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for g in range(ngulps):
         # membership changes need an idle batch: drain, then admit / release
@@ -576,8 +578,8 @@ def main_stream(a, rank, world, local, dist):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     beam_gulps = searched_beams
-    value = beam_gulps * gulp_s / (float(np.sum(dev_ms)) / 1e3)
-    e2e = beam_gulps * gulp_s / wall
+    value, _ = job_rate(dist, beam_gulps * gulp_s, float(np.sum(dev_ms)) / 1e3)
+    e2e, _ = job_rate(dist, beam_gulps * gulp_s, wall)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": ngulps,
         "warmup": 0, "ms_per_step": round(float(np.mean(dev_ms)), 3), "higher_is_better": True,
@@ -637,6 +639,9 @@ def main_refine(a, rank, world, local, dist):
     theta = torch.from_numpy(theta0).cuda()
     chi = torch.empty(n, device="cuda")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     e0.record(stream)
     r.fit(cut, ddm, theta, steps, lr, chi)
     e1.record(stream)
@@ -656,6 +661,9 @@ def main_refine(a, rank, world, local, dist):
     # end to end: cutouts from pinned host memory, fit, parameters back
     host = torch.empty(cut.shape, dtype=torch.float32, pin_memory=True)
     host.copy_(cut)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     w0 = time.perf_counter()
     dcut = torch.empty_like(cut)
     dcut.copy_(host, non_blocking=True)
@@ -664,6 +672,8 @@ def main_refine(a, rank, world, local, dist):
     out = th2.cpu()
     e2e_s = time.perf_counter() - w0
     fit = theta.cpu().numpy()
+    rate, _ = job_rate(dist, n, ms / 1e3)
+    rate_e2e, _ = job_rate(dist, n, e2e_s)
     bytes_pass = float(n) * nch * ns * 4
     hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") if (
         ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
@@ -672,7 +682,7 @@ def main_refine(a, rank, world, local, dist):
     derr1 = np.abs(fit[:, 0] - truth[:, 0])
     line = {
         "metric": "candidate cutouts refined per second (50 Adam steps each)",
-        "value": round(n / (ms / 1e3), 1), "unit": "cutouts/s", "n_gpus": world, "steps": steps,
+        "value": round(rate, 1), "unit": "cutouts/s", "n_gpus": world, "steps": steps,
         "warmup": a.warmup, "ms_per_step": round(ms / steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (dispersed Gaussian bursts in N(0,1) noise, drawn on the GPU)",
@@ -682,7 +692,7 @@ def main_refine(a, rank, world, local, dist):
                    "cutout_gb": round(bytes_pass / 1e9, 1),
                    "dm_abs_err_median": [round(float(np.median(derr0)), 3), round(float(np.median(derr1)), 3)],
                    "chi2_ratio_median": round(float(np.median((chi.cpu() / chi0.cpu()).numpy())), 4)},
-        "e2e": {"value": round(n / e2e_s, 1), "unit": "cutouts/s", "h2d_bytes_per_step": int(bytes_pass),
+        "e2e": {"value": round(rate_e2e, 1), "unit": "cutouts/s", "h2d_bytes_per_step": int(bytes_pass),
                 "d2h_bytes_per_step": int(out.numel() * 4)},
         "gpu_launches": 2 * steps,
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",

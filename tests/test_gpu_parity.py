@@ -111,9 +111,10 @@ def _run_to_search(hella, oracle, params, sky, beams=1):
     return s, pl
 
 
-def test_flagger_bit_exact(hella, oracle):
-    p = small_params(nchan=256, gulp=4096)
-    sky = synth.Sky(p["nchan"], p["tsamp"], p["f0_mhz"], p["df_mhz"], seed=21, rfi_chans=(3, 100), slope=0.4)
+@pytest.mark.parametrize("nchan", [256, 96, 160])  # 96, 160: partial 128-channel slices
+def test_flagger_bit_exact(hella, oracle, nchan):
+    p = small_params(nchan=nchan, gulp=4096)
+    sky = synth.Sky(p["nchan"], p["tsamp"], p["f0_mhz"], p["df_mhz"], seed=21, rfi_chans=(3, 50), slope=0.4)
     s = _search(hella, p)
     x = sky.gulp(0, p["gulp"])
     x[:, 77] = 0  # a dead channel (spectral flag)
@@ -159,10 +160,10 @@ def test_search_stages_bit_exact(hella, oracle):
 
 
 @pytest.mark.parametrize("wmin,wmax,anchor", [
-    (1, 16, 1),     # span 16: 32-output kernel, stride 131
-    (3, 400, 1),    # odd widths 3..384, span 768: stride 193, odd window offsets
-    (1, 2048, 0),   # widths up to 1024, span 2048: the largest 32-output stride
-    (1, 4096, 1),   # span 4096: the 16-output fallback kernel
+    (1, 16, 1),     # span 16: k_firR, stride 133
+    (3, 400, 1),    # odd widths 3..384, span 768: stride 257, odd window offsets
+    (1, 2048, 0),   # widths up to 1024, span 2048: the largest k_firR stride
+    (1, 4096, 1),   # span 4096: the k_fir fallback
     (5, 11, 0),     # a single width
 ])
 def test_smoothing_width_sets_bit_exact(hella, oracle, wmin, wmax, anchor):
@@ -189,6 +190,25 @@ def test_smoothing_width_sets_bit_exact(hella, oracle, wmin, wmax, anchor):
     assert np.array_equal(std.view(np.uint32), ref["std"].view(np.uint32))
     s.find_peaks(0)
     assert cands_equal(s.get_peaks(), ref["cands"])
+
+
+@pytest.mark.parametrize("nchan", [96, 160])
+def test_gulp_loop_partial_channel_slices(hella, oracle, nchan):
+    """Channel counts that are not multiples of the flagger's 128-channel
+    slices: candidates of a whole gulp loop identical to the oracle's."""
+    params, sky = synth.config_plain(seed=11, nchan=nchan, gulp=2048, dm_max=300.0)
+    sky.bursts[0].amp *= 4
+    s = _search(hella, params)
+    pl = oracle_pipeline(oracle, params)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        x = sky.gulp(g, params["gulp"])[None]
+        got, sg = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert sg == so
+        assert cands_equal(got, want), (g, len(got), len(want))
+        total += len(got)
+    assert total > 0
 
 
 @pytest.mark.parametrize("anchor", [0, 1])

@@ -1,7 +1,14 @@
 // io.cpp -- host-side data paths around the search (include/hella_io.h).
 #include "hella_io.h"
 
+#include <arpa/inet.h>
 #include <cuda_runtime.h>
+#include <errno.h>
+#include <fcntl.h>
+#include <netinet/in.h>
+#include <poll.h>
+#include <sys/socket.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -207,6 +214,62 @@ hella_status hella_cands_coincidencer(int gulp_number, const char *utc_start, co
   if (k < 0 || (size_t)k >= cap) return HELLA_ERR_BUDGET;
   *len = (size_t)k;
   return format_lines(c, n, samp0, dms, ndms, time_resolution, buf, cap, len);
+}
+
+namespace {
+
+// Waits until fd is ready for `events` (POLLOUT); false on timeout or error.
+bool wait_fd(int fd, short events, int timeout_ms) {
+  pollfd pf{fd, events, 0};
+  for (;;) {
+    const int r = poll(&pf, 1, timeout_ms);
+    if (r > 0) return (pf.revents & (POLLERR | POLLHUP | POLLNVAL)) == 0 || (pf.revents & events);
+    if (r == 0) return false;
+    if (errno != EINTR) return false;
+  }
+}
+
+hella_status send_on(int fd, const sockaddr_in &addr, const char *msg, size_t len, int timeout_ms) {
+  if (timeout_ms > 0) {
+    const int fl = fcntl(fd, F_GETFL, 0);
+    if (fl < 0 || fcntl(fd, F_SETFL, fl | O_NONBLOCK) != 0) return HELLA_ERR_IO;
+  }
+  if (connect(fd, reinterpret_cast<const sockaddr *>(&addr), sizeof addr) != 0) {
+    if (timeout_ms <= 0 || errno != EINPROGRESS || !wait_fd(fd, POLLOUT, timeout_ms)) return HELLA_ERR_IO;
+    int err = 0;
+    socklen_t el = sizeof err;
+    if (getsockopt(fd, SOL_SOCKET, SO_ERROR, &err, &el) != 0 || err != 0) return HELLA_ERR_IO;
+  }
+  size_t at = 0;
+  while (at < len) {
+    const ssize_t k = send(fd, msg + at, len - at, MSG_NOSIGNAL);
+    if (k > 0) {
+      at += (size_t)k;
+    } else if (k < 0 && errno == EINTR) {
+      continue;
+    } else if (k < 0 && (errno == EAGAIN || errno == EWOULDBLOCK) && timeout_ms > 0) {
+      if (!wait_fd(fd, POLLOUT, timeout_ms)) return HELLA_ERR_IO;
+    } else {
+      return HELLA_ERR_IO;
+    }
+  }
+  return HELLA_OK;
+}
+
+}  // namespace
+
+hella_status hella_cands_send(const char *host, int port, const char *msg, size_t len, int timeout_ms) {
+  if (!host || (!msg && len) || port < 1 || port > 65535) return HELLA_ERR_INVALID_ARG;
+  sockaddr_in addr;
+  std::memset(&addr, 0, sizeof addr);
+  addr.sin_family = AF_INET;
+  addr.sin_port = htons((uint16_t)port);
+  if (inet_pton(AF_INET, host, &addr.sin_addr) != 1) return HELLA_ERR_INVALID_ARG;
+  const int fd = socket(AF_INET, SOCK_STREAM, 0);
+  if (fd < 0) return HELLA_ERR_IO;
+  const hella_status st = send_on(fd, addr, msg, len, timeout_ms);
+  const int cr = close(fd);
+  return st != HELLA_OK ? st : (cr == 0 ? HELLA_OK : HELLA_ERR_IO);
 }
 
 // ---------------------------------------------------------- clustering

@@ -695,6 +695,7 @@ const char *hella_status_string(hella_status s) {
     case HELLA_ERR_DEDISP: return "dedispersion plan error";
     case HELLA_ERR_BUDGET: return "hbm budget exceeded";
     case HELLA_ERR_TIMEOUT: return "device wait timed out";
+    case HELLA_ERR_IO: return "socket error";
   }
   return "unknown status";
 }

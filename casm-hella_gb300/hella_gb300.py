@@ -197,6 +197,7 @@ def lib() -> C.CDLL:
     _sig(L, "hella_cands_coincidencer", C.c_int, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, _VP, C.c_int,
                                                   C.c_long, _VP, C.c_int, C.c_double, _VP, C.c_size_t,
                                                   C.POINTER(C.c_size_t)])
+    _sig(L, "hella_cands_send", C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.c_int])
     _sig(L, "hella_cluster", C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, _VP, C.POINTER(C.c_int), _VP])
     _sig(L, "hella_flagstats_create", C.c_int, [C.POINTER(_VP), C.c_int, C.c_int])
     _sig(L, "hella_flagstats_destroy", None, [_VP])
@@ -717,6 +718,12 @@ def cands_coincidencer(gulp_number: int, cands, samp0: int, dms, time_resolution
     _chk(lib().hella_cands_coincidencer(gulp_number, enc(utc_start), enc(picoseconds), enc(tsamp), cp, len(c),
                                         samp0, d.ctypes.data, len(d), time_resolution, buf, len(buf), C.byref(n)))
     return buf.raw[: n.value].decode()
+
+
+def cands_send(host: str, port: int, message, timeout_ms: int = 2000):
+    """Sends one message (str or bytes) to host:port over TCP (hella_cands_send)."""
+    data = message.encode() if isinstance(message, str) else bytes(message)
+    _chk(lib().hella_cands_send(host.encode(), port, data, len(data), timeout_ms))
 
 
 def cluster(cands, dsamp: int, ddm: int, dwidth: int):

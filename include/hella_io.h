@@ -65,6 +65,15 @@ hella_status hella_cands_coincidencer(int gulp_number, const char *utc_start, co
                                       const float *dms, int ndms, double time_resolution, char *buf,
                                       size_t cap, size_t *len);
 
+/* Sends len bytes of msg (e.g. a hella_cands_coincidencer message) over one
+ * TCP connection to host (dotted IPv4) : port, then closes it (output_peaks'
+ * socket branch, peaks.cu:179-258: connect, one message, close).  Partial
+ * writes are continued until every byte is sent; the socket is closed on
+ * every path.  timeout_ms > 0 bounds the connect and each write (0: the
+ * system's blocking behaviour).  HELLA_ERR_INVALID_ARG for a bad host or
+ * port, HELLA_ERR_IO when the connection or a write fails or times out. */
+hella_status hella_cands_send(const char *host, int port, const char *msg, size_t len, int timeout_ms);
+
 /* ---- candidate clustering (no counterpart in the reference) */
 /* Friends-of-friends: two candidates of the same beam are friends when
  * |samp difference| <= dsamp, |dm_idx difference| <= ddm and |width

@@ -41,7 +41,8 @@ typedef enum {
   HELLA_ERR_STATE = 4,        /* stage called out of order */
   HELLA_ERR_DEDISP = 5,       /* the dedispersion plan rejected the call */
   HELLA_ERR_BUDGET = 6,       /* HBM budget would be exceeded */
-  HELLA_ERR_TIMEOUT = 7       /* a bounded device wait expired */
+  HELLA_ERR_TIMEOUT = 7,      /* a bounded device wait expired */
+  HELLA_ERR_IO = 8            /* a socket could not be opened, connected or written */
 } hella_status;
 
 #define HELLA_MAX_SCRUNCH 16

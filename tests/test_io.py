@@ -105,6 +105,56 @@ def test_candidate_formats(hella, tmp_path):
     assert hella.cands_coincidencer(2, c[:0], 0, dms) == "2\n"
 
 
+def _listen():
+    import socket
+
+    srv = socket.socket(socket.AF_INET, socket.SOCK_STREAM)
+    srv.bind(("127.0.0.1", 0))
+    srv.listen(1)
+    return srv
+
+
+def test_coincidencer_message_over_tcp(hella):
+    """The message arrives whole on one connection, which is then closed
+    (output_peaks' socket branch)."""
+    c = _cands(600)
+    dms = np.linspace(0, 500, 50).astype(np.float32)
+    msg = hella.cands_coincidencer(9, c, 1000, dms)
+    srv = _listen()
+    got = []
+
+    def serve():
+        conn, _ = srv.accept()
+        with conn:
+            buf = b""
+            while True:
+                part = conn.recv(65536)
+                if not part:
+                    break
+                buf += part
+        got.append(buf)
+
+    th = threading.Thread(target=serve)
+    th.start()
+    hella.cands_send("127.0.0.1", srv.getsockname()[1], msg, timeout_ms=5000)
+    th.join(timeout=10)
+    srv.close()
+    assert got == [msg.encode()]
+    assert len(msg) > 16384  # more than one small write's worth
+
+
+def test_coincidencer_send_errors(hella):
+    srv = _listen()
+    port = srv.getsockname()[1]
+    srv.close()  # nothing listens there now: connection refused
+    with pytest.raises(hella.HellaError, match="socket"):
+        hella.cands_send("127.0.0.1", port, "1\n", timeout_ms=2000)
+    with pytest.raises(hella.HellaError, match="invalid"):
+        hella.cands_send("not-an-address", 5000, "1\n")
+    with pytest.raises(hella.HellaError, match="invalid"):
+        hella.cands_send("127.0.0.1", 0, "1\n")
+
+
 def _fof(c, dsamp, ddm, dw):
     n = len(c)
     parent = list(range(n))

@@ -21,11 +21,13 @@
 // spread across the tile and the per-trial byte offsets, so every stage is
 // one contiguous bulk copy per channel (the packed words [t0 + delay,
 // + S + spread), two copies where the ring wraps) plus one for the offsets.
-// The copies are issued by the lanes of warp 0 with cp.async.bulk (TMA)
-// onto an mbarrier per buffer; two buffers alternate so that stage k+1
-// lands while stage k is summed.  Every wait is bounded: a wait that runs
-// out sets bit 0 of the status word, drains the copies in flight (bounded
-// again) and ends the block.
+// Stage g of a block is issued by warp g mod 8 (lane i copies channel i)
+// with cp.async.bulk (TMA) onto the full mbarrier of buffer g mod nbuf
+// (2-4 buffers); every warp arrives on the buffer's empty mbarrier once it
+// has summed the stage, which frees the buffer for stage g + nbuf.  No
+// block-wide barrier sits in the loop.  Every wait is bounded: a wait that
+// runs out sets bit 0 of the status word, drains the copies in flight
+// (bounded again) and ends the block.
 //
 // Persistence.  The grid is sized to the resident blocks of the GPU and
 // strides over the work items of every beam of the launch; items of one

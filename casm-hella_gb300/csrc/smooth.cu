@@ -37,8 +37,9 @@ constexpr int kT = 256;           // threads per row block
 constexpr int kCH = kR * kT;      // outputs per chunk
 
 __device__ __forceinline__ float block256_tree(const float *p) {
-  // p: 256 partials in shared memory; returns thread 0's total
-  // (normalization.cu:41-68) in every thread of warp 0.
+  // p: 256 partials in shared memory; called by one whole warp, returns in
+  // its lane 0 the total the reference's thread 0 forms (normalization.cu:
+  // 41-68: each warp's shuffle tree, then the warp totals in order).
   const int lane = threadIdx.x & 31;
   float tot = 0.f;
   for (int wi = 0; wi < 8; ++wi) {

@@ -318,11 +318,18 @@ def main():
     extra = {
         "smooth": {"bound": "hbm", "achieved": round(smooth_bytes / sm_t / 1e9, 1), "peak": hbm, "unit": "GB/s",
                    "frac": round(smooth_bytes / sm_t / 1e9 / hbm, 4), "ms_per_launch": round(sm_t * 1e3, 3),
-                   "note": "FIR + per-width statistics; bytes = dd plane read x3 + planes write/read"},
+                   "note": "FIR + per-width statistics; bytes = dd plane read x3 + planes write/read; the FIR "
+                           "itself is FP32-FMA issue bound (profiles/)"},
         "flagger": {"bound": "hbm", "achieved": round(flag_bytes / fl_t / 1e9, 1), "peak": hbm, "unit": "GB/s",
                     "frac": round(flag_bytes / fl_t / 1e9 / hbm, 4), "ms_per_launch": round(fl_t * 1e3, 3),
                     "note": "9 u8 passes + 1 u8 write per sample"},
     }
+    if roof["traffic"]:
+        # the dominant kernel against HBM: its measured DRAM traffic over the launch time
+        gbs = roof["traffic"] / dd_t / 1e9
+        extra["dedisp_hbm"] = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                               "frac": round(gbs / hbm, 4), "ms_per_launch": round(dd_t * 1e3, 3),
+                               "note": "k_dedisp's ncu DRAM bytes per launch over its time: not HBM bound"}
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,

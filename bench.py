@@ -38,8 +38,9 @@ WORKLOAD = ("full single beam: 2048 ch 375-468.75 MHz, tsamp 0.524288 ms, gulp 6
             "DM 0-2000 tol 1.25, widths 1-256, 7 sigma")
 METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp latency"
 UNIT = "beam·s/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_dedisp launch of this workload, from one
-# ncu --set full capture of `bench.py --steps 1 --warmup 3` (8.09 GB read + 0.686 GB written)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_dedisp launch of this workload, from a
+# single-pass ncu capture of those two metrics on `bench.py --steps 1 --warmup 3 --no-cpu-baseline`
+# (8.09 GB read + 0.686 GB written)
 DEDISP_TRAFFIC_BYTES = 8.777e9
 
 

@@ -430,7 +430,13 @@ def main_batched(a, rank, world, local, dist):
 
     # ---------------- end to end from pinned host memory: two gulps in flight, the upload of
     # gulp k+1 overlapping the search of gulp k (hella_batch_submit / hella_batch_poll)
-    lat = []
+    lat, e2e_dev = [], []
+    # untimed warm-up of both lanes (each lane's graph is built on its first use)
+    for _ in range(2):
+        bt.submit(host[gi % ngen].data_ptr())
+        gi += 1
+    for _ in range(2):
+        bt.poll()
     if dist:
         dist.barrier()
     w0 = time.perf_counter()
@@ -440,8 +446,9 @@ def main_batched(a, rank, world, local, dist):
         if k + 1 < a.steps:
             bt.submit(host[gi % ngen].data_ptr())
             gi += 1
-        got, counts, _, l_ms, _ = bt.poll()
+        got, counts, _, l_ms, d_ms = bt.poll()
         lat.append(l_ms / 1e3)
+        e2e_dev.append(d_ms)
     e2e_s = time.perf_counter() - w0
     e2e, e2e_s = job_rate(dist, a.steps * NB * gulp_s, e2e_s)
     clk = clocks.stop()
@@ -472,7 +479,9 @@ def main_batched(a, rank, world, local, dist):
                 "d2h_bytes_per_step": int(4 * NB + 20 * np.mean(ncand)), "inflight": 2,
                 "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
-                "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1)},
+                "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1),
+                "device_ms_p50": round(float(np.percentile(e2e_dev, 50)), 2),
+                "period_ms": round(1e3 * e2e_s / a.steps, 2)},
         "gpu_launches": int(a.steps * 2 * bt.graph_kernels()),
         "roofline": roof,
         "clocks": clk,

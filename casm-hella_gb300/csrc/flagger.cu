@@ -69,17 +69,21 @@ constexpr int kQC = 128;
 constexpr int kRowT = 512;  // threads per block
 constexpr size_t kLutSlice = (size_t)256 * kQC * sizeof(__half);
 
-__device__ __forceinline__ void load_lut_slice4(__half *lut_s, const __half *lut, int nchan, int b,
-                                                int c0) {
-  const int ncl = min(kQC, nchan - c0);
+// Stages the table slice of channels c0 .. c0 + NC - 1 of beam b as
+// lut_s[level * NC + channel] (channels past nchan are left alone): each
+// thread loads eight levels of one channel with a 16-byte load, and the
+// lanes of a warp, holding consecutive channels, store without conflicts.
+template <int NC>
+__device__ __forceinline__ void load_lut_slice(__half *lut_s, const __half *lut, int nchan, int b, int c0) {
+  const int ncl = min(NC, nchan - c0);
   const __half *lb = lut + ((size_t)b * nchan + c0) * 256;
-  for (int i = threadIdx.x; i < kQC * 32; i += blockDim.x) {
-    const int cc = i % kQC, vb = i / kQC;  // levels 8vb .. 8vb+7 of channel cc
+  for (int i = threadIdx.x; i < NC * 32; i += blockDim.x) {
+    const int cc = i % NC, vb = i / NC;  // levels 8vb .. 8vb+7 of channel cc
     if (cc < ncl) {
       const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
       const __half *h = reinterpret_cast<const __half *>(&q);
 #pragma unroll
-      for (int k = 0; k < 8; ++k) lut_s[(8 * vb + k) * kQC + cc] = h[k];
+      for (int k = 0; k < 8; ++k) lut_s[(8 * vb + k) * NC + cc] = h[k];
     }
   }
 }
@@ -96,16 +100,7 @@ __global__ void __launch_bounds__(256) k_lane_partials(const uint8_t *__restrict
                                                        float *__restrict__ part, int nchan, int w) {
   __shared__ __half lut_s[256][kLaneC];
   const int b = blockIdx.z, c0 = blockIdx.x * kLaneC;
-  {
-    const __half *lb = lut + ((size_t)b * nchan + c0) * 256;
-    for (int i = threadIdx.x; i < kLaneC * 32; i += blockDim.x) {
-      const int cc = i % kLaneC, vb = i / kLaneC;  // levels 8vb .. 8vb+7 of channel cc
-      const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
-      const __half *h = reinterpret_cast<const __half *>(&q);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) lut_s[8 * vb + k][cc] = h[k];
-    }
-  }
+  load_lut_slice<kLaneC>(&lut_s[0][0], lut, nchan, b, c0);
   __syncthreads();
   const int cl = threadIdx.x & 31, l = blockIdx.y * 8 + (threadIdx.x >> 5);
   const int c = c0 + cl;
@@ -134,7 +129,7 @@ __global__ void __launch_bounds__(kRowT) k_row_partials(const uint8_t *__restric
                                                          int which) {
   extern __shared__ __align__(16) __half lut4_s[];
   const int b = blockIdx.z, c0 = blockIdx.x * kQC, nchan = st.nchan, w = st.gulp;
-  load_lut_slice4(lut4_s, st.lut, nchan, b, c0);
+  load_lut_slice<kQC>(lut4_s, st.lut, nchan, b, c0);
   __syncthreads();
   const int cq = 4 * (threadIdx.x & 31), c = c0 + cq;
   const int j = blockIdx.y * (kRowT / 32) + (threadIdx.x >> 5);
@@ -297,16 +292,7 @@ __global__ void __launch_bounds__(256) k_flag_out(const uint8_t *__restrict__ gu
   __shared__ __align__(16) uint8_t tile[kOutC][kOutT + 4];
   const int b = blockIdx.z, c0 = blockIdx.x * kOutC, t0 = blockIdx.y * kOutT;
   const int nchan = st.nchan, w = st.gulp, tid = threadIdx.x;
-  {
-    const __half *lb = st.lut + ((size_t)b * nchan + c0) * 256;
-    for (int i = tid; i < kOutC * 32; i += 256) {
-      const int cc = i % kOutC, vb = i / kOutC;  // levels 8vb .. 8vb+7 of channel cc
-      const uint4 q = *reinterpret_cast<const uint4 *>(lb + (size_t)cc * 256 + 8 * vb);
-      const __half *h = reinterpret_cast<const __half *>(&q);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) lut_s[8 * vb + k][cc] = h[k];
-    }
-  }
+  load_lut_slice<kOutC>(&lut_s[0][0], st.lut, nchan, b, c0);
   __syncthreads();
   const __half a2 = st.hsc[b * 8 + 2], m2 = st.hsc[b * 8 + 3];
   const uint8_t *g = gulp + (size_t)b * w * nchan + c0;

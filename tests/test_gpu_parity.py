@@ -211,6 +211,26 @@ def test_gulp_loop_partial_channel_slices(hella, oracle, nchan):
     assert total > 0
 
 
+@pytest.mark.parametrize("gulp", [256, 1056, 2080])
+def test_gulp_loop_ragged_gulps(hella, oracle, gulp):
+    """Gulps that are not multiples of the FIR's 2048-sample chunks, the ring
+    writer's 512-sample tiles or the statistics' 256 columns: candidates and
+    the smoothed planes of the last gulp identical to the oracle's."""
+    params, sky = synth.config_plain(seed=12, nchan=128, gulp=gulp, dm_max=150.0)
+    params["snr"] = 4.0
+    s = _search(hella, params)
+    pl = oracle_pipeline(oracle, params)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        x = sky.gulp(g, gulp)[None]
+        got, sg = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert sg == so
+        assert cands_equal(got, want), (g, len(got), len(want))
+        total += len(got)
+    assert total > 0
+
+
 @pytest.mark.parametrize("anchor", [0, 1])
 def test_gulp_loop_multibeam(hella, oracle, anchor):
     params, _ = synth.config_plain(seed=7, nchan=128, gulp=2048, dm_max=400.0)

@@ -29,7 +29,7 @@ constexpr int kWarps = 8;
 constexpr int kChPerWarp = 2;
 constexpr int kChPerBlock = kWarps * kChPerWarp;
 constexpr int kNp = 6;  // chi2 + 5 gradient partials
-constexpr int kLoads = 4;  // float4 loads per lane per round
+constexpr int kLoads = 8;  // float4 loads per lane per round
 
 struct RefineArgs {
   const float *cut;     // [n][nchan][nsamp]

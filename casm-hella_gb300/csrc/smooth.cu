@@ -423,8 +423,8 @@ __global__ void __launch_bounds__(kT) k_row_stat(SmoothArgs a) {
       s = __fadd_rn(s, v);
     }
   };
-  // eight loads in flight per thread, then the sums in column order
-  constexpr int kB = 8;
+  // sixteen loads in flight per thread, then the sums in column order
+  constexpr int kB = 16;
   int col = tid;
   for (; col + (kB - 1) * kT < nwcol; col += kB * kT) {
     float v[kB];

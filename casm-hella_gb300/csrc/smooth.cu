@@ -494,7 +494,16 @@ __global__ void __launch_bounds__(kT) k_count(SmoothArgs a) {
   }
   const float *x = B.boxes + ((size_t)j * h + r) * a.ntime_out;
   int n = 0;
-  for (int col = tid; col < a.ntime_out; col += kT) n += normv(x[col], st) > thr;
+  constexpr int kB = 16;  // loads in flight per thread
+  int col = tid;
+  for (; col + (kB - 1) * kT < a.ntime_out; col += kB * kT) {
+    float v[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) v[u] = x[col + u * kT];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) n += normv(v[u], st) > thr;
+  }
+  for (; col < a.ntime_out; col += kT) n += normv(x[col], st) > thr;
   for (int off = 16; off > 0; off /= 2) n += __shfl_xor_sync(0xffffffffu, n, off);
   if ((tid & 31) == 0) c_s[tid >> 5] = n;
   __syncthreads();
@@ -537,10 +546,14 @@ __global__ void __launch_bounds__(1024) k_scan(SmoothArgs a) {
   if (tid == 1023) B.total[0] = min(base + s_s[1023], B.cap);
 }
 
-// Ordered compaction of one row's candidates.
+// Ordered compaction of one row's candidates, kWR chunks of 256 columns a
+// round: every thread reads one column of each chunk, the warps' hit
+// counts of the round are published once, and each hit is written at the
+// row's offset + the hits of earlier chunks + earlier warps of its chunk +
+// earlier lanes (column order).
+constexpr int kWR = 4;
 __global__ void __launch_bounds__(kT) k_write(SmoothArgs a) {
-  __shared__ int w_s[kT / 32];
-  __shared__ int base_s;
+  __shared__ int w_s[kWR][kT / 32];
   int r;
   const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
   const int j = blockIdx.y, b = a.w0 + j, h = B.h, tid = threadIdx.x;
@@ -550,32 +563,41 @@ __global__ void __launch_bounds__(kT) k_write(SmoothArgs a) {
   const float *st = B.stats + b * 4;
   const float thr = B.gate[2];
   const float *x = B.boxes + ((size_t)j * h + r) * a.ntime_out;
-  if (tid == 0) base_s = B.offsets[row];
-  for (int cs = 0; cs < a.ntime_out; cs += kT) {
-    const int col = cs + tid;
-    float v = 0.f;
-    bool hit = false;
-    if (col < a.ntime_out) {
-      v = normv(x[col], st);
-      hit = v > thr;
+  int base = B.offsets[row];  // the same in every thread
+  for (int cs = 0; cs < a.ntime_out && base < B.cap; cs += kWR * kT) {
+    float v[kWR];
+    unsigned bal[kWR];
+#pragma unroll
+    for (int m = 0; m < kWR; ++m) {
+      const int col = cs + m * kT + tid;
+      v[m] = col < a.ntime_out ? normv(x[col], st) : 0.f;
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, hit);
-    __syncthreads();
-    if (lane == 0) w_s[warp] = __popc(bal);
-    __syncthreads();
-    int before = base_s;
-    for (int i = 0; i < warp; ++i) before += w_s[i];
-    before += __popc(bal & ((1u << lane) - 1u));
-    if (hit && before < B.cap) {
-      B.cand_i[before] = make_int4(B.beam_id, r + 1, b, col);
-      B.cand_v[before] = v;
+#pragma unroll
+    for (int m = 0; m < kWR; ++m) {
+      const int col = cs + m * kT + tid;
+      bal[m] = __ballot_sync(0xffffffffu, col < a.ntime_out && v[m] > thr);
+      if (lane == 0) w_s[m][warp] = __popc(bal[m]);
     }
     __syncthreads();
-    if (tid == 0) {
-      int t = 0;
-      for (int i = 0; i < kT / 32; ++i) t += w_s[i];
-      base_s += t;
+    int before = base, round = 0;
+#pragma unroll
+    for (int m = 0; m < kWR; ++m) {
+      int pos = before;
+      for (int i = 0; i < kT / 32; ++i) {
+        if (i == warp) pos += __popc(bal[m] & ((1u << lane) - 1u));
+        const int c = w_s[m][i];
+        if (i < warp) pos += c;
+        round += c;
+      }
+      const int col = cs + m * kT + tid;
+      if (((bal[m] >> lane) & 1u) && pos < B.cap) {
+        B.cand_i[pos] = make_int4(B.beam_id, r + 1, b, col);
+        B.cand_v[pos] = v[m];
+      }
+      before = base + round;
     }
+    base += round;
+    __syncthreads();
   }
 }
 

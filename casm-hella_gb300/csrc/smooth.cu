@@ -16,15 +16,16 @@
 // i.e. the DM weights factored out of the 2-D kernel, whose middle row
 // supplies the time taps.  Borders replicate (NPP_BORDER_REPLICATE).
 //
-// Kernels.  k_fir: one block per output row; the row's y values for a
-// 4096-sample chunk are staged in shared memory in a 16-phase layout
-// (Y[x % 16][x / 16]) so that each thread keeps a sliding window of 16
-// outputs in registers and reads one shared word per tap for all 16.  Every
-// width is produced from the same staged chunk; the row-mean partials of
-// the reference's order (thread j sums columns j, j+256, ...) are
+// Kernels.  The FIR stages a row's y values chunk by chunk in shared memory
+// in a 16-phase layout, so that each thread keeps a sliding window of 16
+// outputs in registers and reads one shared word per tap for all 16; every
+// width is produced from the same staged chunk, and the row-mean partials
+// of the reference's order (thread j sums columns j, j+256, ...) are
 // accumulated as the chunk is written, so the plane is written once and
-// read once more for the variance.  Row maxima let the peak pass skip rows
-// that cannot hold a candidate.
+// read once more for the variance.  k_firR (spans up to 2048 samples) does
+// this with constant-offset window loads and two width groups per row;
+// k_fir, with runtime window addresses, takes wider spans.  Row maxima let
+// the peak pass skip rows that cannot hold a candidate.
 #include "hg_internal.h"
 
 #include <algorithm>

@@ -800,6 +800,16 @@ class Ring:
     def end(self):
         _chk(self.L.hella_ring_end(self.h))
 
+    def open_read(self, timeout_ms: int = 1000):
+        """(address, nbytes) of the next filled block, left in place until
+        mark_cleared(); nbytes == 0 at the end of the data."""
+        p, n = _VP(), C.c_size_t()
+        _chk(self.L.hella_ring_open_read(self.h, C.byref(p), C.byref(n), timeout_ms))
+        return (p.value or 0), n.value
+
+    def mark_cleared(self):
+        _chk(self.L.hella_ring_mark_cleared(self.h))
+
     def read(self, timeout_ms: int = 1000):
         """bytes of the next block, or None at the end of the data."""
         p, n = _VP(), C.c_size_t()

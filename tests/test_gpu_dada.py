@@ -61,3 +61,56 @@ def test_dada_gulp_loop_and_batch(hella, oracle):
         assert cands_equal(bgot, want), g
         total += len(got)
     assert total > 0
+
+
+def test_dada_ring_feeds_the_search(hella, oracle):
+    """The DADA loop (casm_hella_refactored.cu:662-670,688-691): a writer
+    thread puts the header and fp16 channel-major gulps into a pinned
+    header/data ring; the reader takes TSAMP and UTC_START from the header,
+    searches every block in place (hella_process_gulp on the ring's own
+    pinned memory) and builds the coincidencer message; candidates equal the
+    oracle's on the same gulps."""
+    import threading
+
+    params, sky = synth.config_plain(seed=45, nchan=128, gulp=2048, dm_max=400.0)
+    sky.bursts[0].amp *= 3
+    G, nch = params["gulp"], params["nchan"]
+    pl = oracle_pipeline(oracle, params)
+    ngulp = pl.min_gulp + 3
+    blocks = [_f16_ft(sky.gulp(g, G), 200 + g) for g in range(ngulp)]
+    ring = hella.Ring(G * nch * 2, 3, pinned=True)
+    header = (f"HDR_VERSION 1.0\nUTC_START 2025-06-01-12:00:00\nPICOSECONDS 0\n"
+              f"TSAMP {params['tsamp'] * 1e6:.3f}\nNCHAN {nch}\nNBIT 16\n")
+
+    def produce():
+        ring.write_header(header)
+        for b in blocks:
+            ring.write(b.tobytes(), timeout_ms=10000)
+        ring.end()
+
+    th = threading.Thread(target=produce)
+    th.start()
+    hdr = ring.read_header(10000)
+    assert hella.header_get(hdr, "NCHAN") == str(nch)
+    s = hella.Search(hella.default_params(**params, input_format=1))
+    dms = s.dm_list()
+    total, g = 0, 0
+    while True:
+        addr, n = ring.open_read(timeout_ms=10000)
+        if n == 0:
+            break
+        assert n == G * nch * 2
+        got, searched = s.process_gulp(addr)
+        ring.mark_cleared()
+        want, so = pl.gulp_step_f16(blocks[g][None])
+        assert searched == so and cands_equal(got, want), g
+        msg = hella.cands_coincidencer(g + 1, got, g * G, dms, utc_start=hella.header_get(hdr, "UTC_START"),
+                                       picoseconds=hella.header_get(hdr, "PICOSECONDS"),
+                                       tsamp=hella.header_get(hdr, "TSAMP"))
+        assert msg.splitlines()[0] == f"{g + 1} 2025-06-01-12:00:00 0 {params['tsamp'] * 1e6:.3f}"
+        assert len(msg.splitlines()) == 1 + len(got)
+        total += len(got)
+        g += 1
+    th.join(timeout=30)
+    ring.close()
+    assert g == ngulp and total > 0

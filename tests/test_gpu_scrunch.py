@@ -48,6 +48,11 @@ def test_scrunch_gulp_loop_and_batch(hella, oracle):
     s = hella.Search(hella.default_params(**dict(params, nbeam=2), scrunches=SCR[:2]))
     pl = oracle_pipeline(oracle, params, nbeam=2, scrunches=SCR[:2])
     bt = hella.Batch(hella.default_params(**dict(params, nbeam=2), scrunches=SCR[:2]))
+    # flag statistics fed from the device's cumulative flag spectrum each gulp
+    # (casm_hella_refactored.cu:708-716), counted like the host model below
+    ntime = s.info.ntime
+    fs = hella.FlagStats(params["nchan"], ntime)
+    prev, want_counts = np.zeros(params["nchan"], np.float32), np.zeros(params["nchan"], np.int64)
     total = 0
     for g in range(pl.min_gulp + 2):
         x = synth.multibeam_gulp(skies, g, params["gulp"])
@@ -56,7 +61,13 @@ def test_scrunch_gulp_loop_and_batch(hella, oracle):
         assert cands_equal(got, want), g
         bgot, counts, _ = bt.process_gulp(x)
         assert cands_equal(bgot, want), g
+        cum = s.flag_spec()
+        fs.update(cum)
+        ref = pl.flagspec()
+        want_counts += (ntime * (ref - prev).astype(np.float64)).astype(np.int64)  # fp32 difference, as in C
+        prev = ref.copy()
         total += len(got)
     assert total > 0
+    assert np.array_equal(fs.counts(), want_counts)
     assert np.array_equal(s.flag_spec().view(np.uint32), pl.flagspec().view(np.uint32))
     assert np.array_equal(bt.flag_spec().view(np.uint32), pl.flagspec().view(np.uint32))

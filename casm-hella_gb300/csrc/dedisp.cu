@@ -17,8 +17,9 @@
 //
 // Staging.  A work item is (beam, tile of DPT trials, 4S samples); the
 // block walks the tables' channels CC at a time.  Host-built tile tables
-// give, per (tile, channel), the delay of the tile's first trial, the delay
-// spread across the tile and the per-trial byte offsets, so every stage is
+// give, per (tile, channel), the smallest delay of the tile's trials (the
+// first trial's, for an ascending DM list), the delay spread across the
+// tile and the per-trial byte offsets, so every stage is
 // one contiguous bulk copy per channel (the packed words [t0 + delay,
 // + S + spread), two copies where the ring wraps) plus one for the offsets.
 // Stage g of a block is issued by warp g mod 8 (lane i copies channel i)
@@ -466,6 +467,17 @@ __global__ void k_transpose_tf(const uint8_t *__restrict__ in, size_t in_stride,
 
 }  // namespace
 
+// Smallest and largest delay of channel c over trials d0..d1 (the first
+// and the last for an ascending DM list).
+static void tile_delay_range(const int *delays, int nchan, int c, int d0, int d1, int *lo, int *hi) {
+  *lo = *hi = delays[(size_t)d0 * nchan + c];
+  for (int d = d0 + 1; d <= d1; ++d) {
+    const int v = delays[(size_t)d * nchan + c];
+    *lo = std::min(*lo, v);
+    *hi = std::max(*hi, v);
+  }
+}
+
 int dedisp_spread(const int *delays, int nchan, const int *chans, int nact, int dm_first,
                   int dm_count, int dpt) {
   const int dlast = dm_first + dm_count - 1;
@@ -473,8 +485,9 @@ int dedisp_spread(const int *delays, int nchan, const int *chans, int nact, int 
   for (int d0 = dm_first; d0 <= dlast; d0 += dpt) {
     const int d1 = std::min(d0 + dpt - 1, dlast);
     for (int k = 0; k < nact; ++k) {
-      const int c = chans[k];
-      spread = std::max(spread, delays[(size_t)d1 * nchan + c] - delays[(size_t)d0 * nchan + c]);
+      int lo, hi;
+      tile_delay_range(delays, nchan, chans[k], d0, d1, &lo, &hi);
+      spread = std::max(spread, hi - lo);
     }
   }
   return spread;
@@ -518,8 +531,9 @@ DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int n
     const int d0 = dm_first + i * t.dpt, d1 = std::min(d0 + t.dpt - 1, dlast);
     for (int k = 0; k < nact; ++k) {
       const int c = chans[k];
-      const int base = delays[(size_t)d0 * nchan + c];
-      t.meta[(size_t)i * nact + k] = make_int4(c, base, delays[(size_t)d1 * nchan + c] - base, 0);
+      int base, top;
+      tile_delay_range(delays, nchan, c, d0, d1, &base, &top);
+      t.meta[(size_t)i * nact + k] = make_int4(c, base, top - base, 0);
       int *o = &t.off[((size_t)i * nact + k) * t.offw];
       for (int m = 0; m < t.dpt; ++m)  // byte offsets into the staged row
         o[m] = 4 * (delays[(size_t)std::min(d0 + m, dlast) * nchan + c] - base);

@@ -118,8 +118,8 @@ struct DedispArgs {
   int mode;                 // pipe balance of the adds (0, 1, 2; 1-2 need dpt >= 8)
   int unit;                 // must be 1
   int max_spread;           // largest tile_meta spread
-  const int4 *tile_meta;    // [ntiles][nact] {channel, delay(c, tile's first trial), spread, 0}
-  const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - delay(c, first trial)), bytes
+  const int4 *tile_meta;    // [ntiles][nact] {channel, smallest delay(c, d) of the tile, spread, 0}
+  const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - that delay), bytes
   int *err;                 // device status word: bit 0 = a staging wait timed out (may be null)
 };
 // Work items of one beam for a tile shape.

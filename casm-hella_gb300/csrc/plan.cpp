@@ -104,10 +104,27 @@ void invalidate_tables(hdd_plan p) {
   p->tab_on_device = false;
 }
 
-void refresh_delays(hdd_plan p) {
-  p->delays = hg::dm_delays(p->dms, p->table);
-  p->max_delay = p->dms.empty() ? 0 : p->delays[(p->dms.size() - 1) * p->nchans + p->nchans - 1];
+// Delays of the plan's DM list; max_delay is the largest of them (the last
+// trial's lowest channel for an ascending list, any trial for another order).
+hdd_error refresh_delays(hdd_plan p) {
   invalidate_tables(p);
+  try {
+    p->delays = hg::dm_delays(p->dms, p->table);
+  } catch (const std::bad_alloc &) {
+    p->dms.clear();
+    p->delays.clear();
+    p->max_delay = 0;
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  p->max_delay = p->delays.empty() ? 0 : *std::max_element(p->delays.begin(), p->delays.end());
+  return HDD_NO_ERROR;
+}
+
+// A trial the kernels can serve: finite, not negative, and a delay that
+// stays far inside int (the delay table grows with channel index).
+bool dm_ok(hdd_plan p, float dm) {
+  if (!(dm >= 0.f) || !(dm < 3.0e38f)) return false;
+  return (double)dm * p->table[p->nchans - 1] + 0.5 < (double)(1 << 30);
 }
 
 void rebuild_chans(hdd_plan p) {
@@ -270,17 +287,37 @@ hdd_error hdd_set_stream(hdd_plan p, void *stream) {
 hdd_error hdd_set_dm_list(hdd_plan p, const hdd_float *dm_list, hdd_size count) {
   if (!p) return HDD_INVALID_PLAN;
   if (!dm_list) return HDD_INVALID_POINTER;
-  p->dms.assign(dm_list, dm_list + count);
-  refresh_delays(p);
-  return HDD_NO_ERROR;
+  // any order; every trial finite, >= 0 and within the delay range
+  for (hdd_size i = 0; i < count; ++i)
+    if (!dm_ok(p, dm_list[i])) return HDD_UNKNOWN_ERROR;
+  if (count > ((size_t)1 << 31) / (size_t)p->nchans) return HDD_MEM_ALLOC_FAILED;  // delay table
+  try {
+    p->dms.assign(dm_list, dm_list + count);
+  } catch (const std::bad_alloc &) {
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  return refresh_delays(p);
 }
 
 hdd_error hdd_generate_dm_list(hdd_plan p, hdd_float dm_start, hdd_float dm_end, hdd_float ti,
                                hdd_float tol) {
   if (!p) return HDD_INVALID_PLAN;
-  p->dms = hg::generate_dm_list(dm_start, dm_end, ti, tol, p->nchans, p->dt, p->f0, p->df);
-  refresh_delays(p);
-  return HDD_NO_ERROR;
+  // dm_end below dm_start gives the single trial dm_start; tol <= 1 would
+  // never advance
+  if (!dm_ok(p, dm_start) || !std::isfinite(dm_end) || !std::isfinite(ti) || !(tol > 1.f) ||
+      !std::isfinite(tol))
+    return HDD_UNKNOWN_ERROR;
+  std::vector<float> dms;
+  try {
+    dms = hg::generate_dm_list(dm_start, dm_end, ti, tol, p->nchans, p->dt, p->f0, p->df);
+  } catch (const std::bad_alloc &) {
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  // the list ends at the first trial >= dm_end, which may pass the range
+  if (!dm_ok(p, dms.back())) return HDD_UNKNOWN_ERROR;
+  if (dms.size() > ((size_t)1 << 31) / (size_t)p->nchans) return HDD_MEM_ALLOC_FAILED;
+  p->dms.swap(dms);
+  return refresh_delays(p);
 }
 
 hdd_error hdd_set_killmask(hdd_plan p, const hdd_bool *killmask) {

@@ -68,6 +68,31 @@ def test_plan_error_codes(hella):
     L.hdd_destroy_plan(h)
 
 
+def test_plan_rejects_dm_lists_the_kernels_cannot_serve(hella):
+    """Negative, NaN, infinite or int-overflowing trials come back as
+    HDD_UNKNOWN_ERROR and leave the plan's list as it was; any order of
+    valid trials is accepted, with max_delay the largest delay of all."""
+    unknown = 16
+    plan = hella.Plan(128, 1e-3, 468.75, -0.5)
+    plan.generate_dm_list(0.0, 50.0, 40.0, 1.3)
+    n0, md0 = plan.dm_count, plan.max_delay
+    L = hella.lib()
+    for bad in ([5.0, -1.0], [float("nan")], [float("inf")], [1e12], [3.0e38]):
+        a = np.asarray(bad, np.float32)
+        assert L.hdd_set_dm_list(plan.h, a.ctypes.data, a.size) == unknown, bad
+        assert (plan.dm_count, plan.max_delay) == (n0, md0)
+    for args in ((-1.0, 50.0, 40.0, 1.3), (0.0, float("nan"), 40.0, 1.3), (0.0, 50.0, 40.0, 1.0),
+                 (0.0, 1e12, 40.0, 1.3)):
+        assert L.hdd_generate_dm_list(plan.h, *args) == unknown, args
+        assert (plan.dm_count, plan.max_delay) == (n0, md0)
+    plan.generate_dm_list(30.0, 10.0, 40.0, 1.3)  # end below start: the single trial 30
+    assert list(plan.dm_list()) == [30.0]
+    plan.set_dm_list(np.asarray([50.0, 0.0, 20.0], np.float32))
+    d = plan.delay_table()
+    assert plan.max_delay == d.max() == d[0, -1]
+    plan.close()
+
+
 def test_search_rejects_bad_params(hella):
     L = hella.lib()
     h = C.c_void_p()

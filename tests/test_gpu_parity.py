@@ -88,6 +88,21 @@ def test_dedisp_sparse_dm_list_uses_small_tiles(hella, oracle):
     assert np.array_equal(plan.dedisperse(x), oracle.dedisperse(x, plan.delay_table()))
 
 
+def test_dedisp_unsorted_dm_list(hella, oracle):
+    """A DM list in no particular order (descending runs, repeats, a jump
+    back to 0): tiles span each channel's smallest to largest delay, and
+    the output length follows the largest delay of any trial."""
+    plan = hella.Plan(256, 1e-3, 468.75, -(468.75 - 375.0) / 256)
+    rng = np.random.default_rng(14)
+    dms = np.concatenate([np.linspace(300, 0, 37), [0.0, 0.0, 250.0], rng.uniform(0, 400, 29),
+                          np.linspace(10, 60, 20)]).astype(np.float32)
+    plan.set_dm_list(dms)
+    assert plan.max_delay == plan.delay_table().max() > plan.delay_table()[-1].max()
+    nsamps = plan.max_delay + 2100
+    x = rng.integers(0, 256, (nsamps, plan.nchans), dtype=np.uint8)
+    assert np.array_equal(plan.dedisperse(x), oracle.dedisperse(x, plan.delay_table()))
+
+
 def test_dedisp_constant_input(hella):
     plan = _random_plan(hella, nchan=384, dm_max=120.0)
     x = np.full((plan.max_delay + 777, plan.nchans), 128, np.uint8)

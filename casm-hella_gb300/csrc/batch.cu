@@ -15,9 +15,11 @@
 // holds the newest NTIME_b samples; the batch reads the same samples at
 // window start (win0 + R - NTIME_b) mod R of the shared ring.  A beam's DM
 // list is the prefix of the longest one (the list is generated trial after
-// trial up to the ceiling), so one set of dedispersion tables serves every
-// beam, each beam computing its own number of trials.  Killed channels are
-// packed as zeros, which drops them from the exact integer sums.
+// trial up to the ceiling), so the plan's dedispersion tables serve every
+// beam, each beam computing its own number of trials.  A beam that kills
+// channels gets tables of its own over its unkilled channels (the same tile
+// shape), so it sums only those; its killed channels are packed as zeros
+// as well.
 //
 // Streaming.  Beams are slots: a dynamic batch sizes every slot for the
 // largest DM list, and slots join and leave between gulps (the layout of
@@ -161,6 +163,12 @@ struct hella_batch {
   hg::GulpPos *d_pos = nullptr;
   std::vector<hg::DedispBeam> dbeams;
   int items_dpt = -1;             // DM tile of the work-item prefix held in d_dbeams
+  std::vector<uint8_t> keep;      // [nbeam][nchan] killmasks (1: channel summed)
+  int4 *d_bmeta = nullptr;        // per-beam tile tables (beams that kill channels)
+  int *d_boff = nullptr, *d_bchans = nullptr;
+  hg::TableJob *d_bjobs = nullptr;
+  size_t bmeta_cap = 0, boff_cap = 0, bchans_cap = 0, bjobs_cap = 0;
+  int btab_dpt = -1, btab_cc = -1;  // tile shape of the per-beam tables; -1: rebuild
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
   std::vector<Lane> lanes;
   std::deque<int> queue;          // lanes in submission order
@@ -260,10 +268,12 @@ hella_status batch_sizes(const hella_batch_params *bp, hdd_plan *plan_out, Sizes
   z->ntime_out = p.gulp;
   z->nbox = 0;
   for (int sm = p.width_min; sm < p.width_max; sm *= 2) z->nbox++;
-  size_t dd_floats = 0, rows = 0;
+  size_t dd_floats = 0, rows = 0, tab_bytes = 0;
   for (int i = 0; i < nb; ++i) {
     dd_floats += (size_t)z->cap_ndms[i] * z->ntime_dd;
     rows += (size_t)z->cap_ndms[i] - 2;
+    // per-beam tile tables: 5-6 bytes per trial and channel (16- or 8-trial tiles)
+    tab_bytes += (size_t)(z->cap_ndms[i] + 15) * nch * 6;
   }
   const size_t R = z->R, cap = p.max_giants;
   const size_t lanes = bp->inflight == 2 ? 2 : 1;
@@ -271,7 +281,8 @@ hella_status batch_sizes(const hella_batch_params *bp, hdd_plan *plan_out, Sizes
              (size_t)nb * nch * (256 * 6 + 16) + (size_t)nb * p.gulp * 6 + dd_floats * 4 + rows * z->nbox * 20 +
              (p.nscrunch > 0 || p.input_format ? (size_t)nb * nch * ((size_t)p.gulp * 6 + 8) : 0) +
              (size_t)nch * 4 +
-             (size_t)nb * cap * 20 + lanes * (size_t)nb * cap * sizeof(hella_cand) + (size_t)nb * 512;
+             (size_t)nb * cap * 20 + lanes * (size_t)nb * cap * sizeof(hella_cand) + (size_t)nb * 512 +
+             tab_bytes;
   z->per_width = rows * z->ntime_out * 4;
   *plan_out = plan;
   return HELLA_OK;
@@ -324,6 +335,7 @@ hella_status upload_layout(hella_batch *b) {
   CK(cudaMemcpy(b->d_member, b->member.data(), nb * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b->d_join, b->join.data(), nb * 4, cudaMemcpyHostToDevice));
   b->items_dpt = -1;  // dedisp_args re-uploads the beams with their item prefix
+  b->btab_dpt = -1;   // and rebuilds the per-beam tables
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;
 }
@@ -338,6 +350,85 @@ void set_slot_sizes(hella_batch *b, int i, int ndms) {
   b->min_gulp[i] = b->ntime[i] / b->p.gulp;  // casm_hella_refactored.cu:632
 }
 
+// Regrows a device table buffer (its contents are rewritten after).
+hella_status grow_table(void **ptr, size_t *cap, size_t need) {
+  if (*cap >= need) return HELLA_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  if (cudaMalloc(ptr, need) != cudaSuccess) {
+    cudaGetLastError();
+    return HELLA_ERR_ALLOC;
+  }
+  *cap = need;
+  return HELLA_OK;
+}
+
+// Tile tables of their own for the member beams that kill channels: the
+// rows of the plan's tables (all channels, same tile shape) of the beam's
+// unkilled channels, so the tiles, delays and offsets are the plan's.
+// Beams that keep every channel read the plan's tables.  Tiles of 1-4
+// trials (very coarse DM lists) keep the plan's tables for every beam.
+hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
+  const int nb = b->nbeam, nch = b->p.nchan;
+  if (tb.nact != nch) return HELLA_ERR_DEDISP;  // the plan keeps every channel
+  std::vector<hg::TableJob> jobs;
+  std::vector<int> chans;
+  std::vector<long> mo(nb, -1);
+  std::vector<int> nact(nb, 0);
+  long meta_n = 0;
+  int max_tiles = 0;
+  try {
+    for (int i = 0; i < nb && tb.dpt >= 8; ++i) {
+      if (!b->member[i]) continue;
+      const int c0 = (int)chans.size();
+      for (int c = 0; c < nch; ++c)
+        if (b->keep[(size_t)i * nch + c]) chans.push_back(c);
+      const int n = (int)chans.size() - c0;
+      if (n == nch) {
+        chans.resize(c0);
+        continue;
+      }
+      const int ntiles = (b->ndms[i] + tb.dpt - 1) / tb.dpt;
+      nact[i] = n;
+      mo[i] = meta_n;
+      jobs.push_back(hg::TableJob{meta_n, c0, n, ntiles});
+      meta_n += (long)ntiles * n;
+      max_tiles = std::max(max_tiles, ntiles);
+    }
+  } catch (const std::bad_alloc &) {
+    return HELLA_ERR_ALLOC;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  hella_status s;
+  if ((s = grow_table((void **)&b->d_bmeta, &b->bmeta_cap, std::max<size_t>(meta_n, 1) * sizeof(int4))) !=
+          HELLA_OK ||
+      (s = grow_table((void **)&b->d_boff, &b->boff_cap, std::max<size_t>(meta_n, 1) * tb.dpt * sizeof(int))) !=
+          HELLA_OK ||
+      (s = grow_table((void **)&b->d_bchans, &b->bchans_cap, std::max<size_t>(chans.size(), 1) * sizeof(int))) !=
+          HELLA_OK ||
+      (s = grow_table((void **)&b->d_bjobs, &b->bjobs_cap, std::max<size_t>(jobs.size(), 1) * sizeof(hg::TableJob))) !=
+          HELLA_OK)
+    return s;
+  if (!jobs.empty()) {
+    CK(cudaMemcpy(b->d_bchans, chans.data(), chans.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_bjobs, jobs.data(), jobs.size() * sizeof(hg::TableJob), cudaMemcpyHostToDevice));
+    CK(hg::gather_tables(tb.meta, tb.off, nch, tb.dpt, b->d_bjobs, (int)jobs.size(), max_tiles, b->d_bchans,
+                         b->d_bmeta, b->d_boff, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+  }
+  for (int i = 0; i < nb; ++i) {
+    hg::DedispBeam &d = b->dbeams[i];
+    d.meta = mo[i] < 0 ? nullptr : b->d_bmeta + mo[i];
+    d.off = mo[i] < 0 ? nullptr : b->d_boff + mo[i] * tb.dpt;
+    d.nact = nact[i];
+  }
+  b->btab_dpt = tb.dpt;
+  b->btab_cc = tb.cc;
+  b->items_dpt = -1;  // the beams go to the device again
+  return HELLA_OK;
+}
+
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
@@ -345,6 +436,8 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
   if (hg::plan_device_tables(b->plan, 0, b->z.ndms_all, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
     return HELLA_ERR_DEDISP;
   if (t.add_mode && tb.dpt < 8) return HELLA_ERR_INVALID_ARG;
+  hella_status s;
+  if ((b->btab_dpt != tb.dpt || b->btab_cc != tb.cc) && (s = beam_tables(b, tb)) != HELLA_OK) return s;
   hg::DedispArgs a{};
   a.beams = b->d_dbeams;
   a.nbeam = b->nbeam;
@@ -515,6 +608,8 @@ void hella_batch_destroy(hella_batch *b) {
   }
   for (void *ptr : b->dallocs) cudaFree(ptr);
   for (void *ptr : b->hallocs) cudaFreeHost(ptr);
+  for (void *ptr : {(void *)b->d_bmeta, (void *)b->d_boff, (void *)b->d_bchans, (void *)b->d_bjobs})
+    if (ptr) cudaFree(ptr);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
   hdd_destroy_plan(b->plan);
@@ -680,10 +775,11 @@ hella_status hella_batch_create(hella_batch **out, const hella_batch_params *bp)
   DA(b->d_pos, sizeof(hg::GulpPos));
 #undef DA
 
-  std::vector<uint8_t> keep((size_t)nb * nch, 1);
+  b->keep.assign((size_t)nb * nch, 1);
   if (bp->killmask)
-    for (size_t i = 0; i < keep.size(); ++i) keep[i] = bp->killmask[i] != 0;
-  b->dbeams.resize(nb);
+    for (size_t i = 0; i < b->keep.size(); ++i) b->keep[i] = bp->killmask[i] != 0;
+  const std::vector<uint8_t> &keep = b->keep;
+  b->dbeams.assign(nb, hg::DedispBeam{});
   std::vector<float> taps;
   std::vector<int> toff, tn;
   hg::smoothing_taps(*p, z.nbox, &taps, &toff, &tn);
@@ -745,11 +841,10 @@ hella_status hella_batch_set_beam(hella_batch *b, int beam, int member, float dm
     const int n = prefix_trials(b->p, b->plan, dm_max);
     if (n < 3) return n < 0 ? HELLA_ERR_DEDISP : HELLA_ERR_INVALID_ARG;
     set_slot_sizes(b, beam, n);
-    std::vector<uint8_t> keep(nch, 1);
-    if (killmask)
-      for (int c = 0; c < nch; ++c) keep[c] = killmask[c] != 0;
+    uint8_t *keep = b->keep.data() + (size_t)beam * nch;
+    for (int c = 0; c < nch; ++c) keep[c] = killmask ? killmask[c] != 0 : 1;
     CK(cudaStreamSynchronize(b->stream));
-    CK(cudaMemcpy(b->d_keep + (size_t)beam * nch, keep.data(), nch, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_keep + (size_t)beam * nch, keep, nch, cudaMemcpyHostToDevice));
     // a fresh ring for the newcomer, as a new single-beam context starts with
     CK(cudaMemset(b->d_plain + (size_t)beam * nch * b->z.R, 0, (size_t)nch * b->z.R));
     CK(cudaMemset(b->d_packed + (size_t)beam * nch * b->z.R, 0, (size_t)nch * b->z.R * 4));

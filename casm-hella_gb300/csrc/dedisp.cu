@@ -51,7 +51,7 @@ __host__ __device__ constexpr int row_words(int max_spread) {
 }
 __host__ __device__ constexpr int off_width(int dpt) { return dpt < 4 ? 4 : dpt; }
 constexpr int kMaxBuf = 4;        // staging buffers (pipeline depth)
-constexpr int kBarBytes = 320;    // full[4] | empty[4] mbarriers | per warp: the item it stages
+constexpr int kBarBytes = 448;    // full[4] | empty[4] mbarriers | per warp: its staging cursor
 
 // Words of one staging buffer: sh [cc] | off [cc][offw] | rows [cc][rowstride];
 // every part is a multiple of 16 bytes.
@@ -140,20 +140,29 @@ struct Item {
   const int *off;
   long w0;            // ring position of the item's first sample
   int t0, tile, dm_count;
+  int nact;           // channels of the item's tables
 };
+
+// Beam of a work item (binary search over the beams' item prefixes).
+__device__ __forceinline__ int beam_of(const DedispArgs &a, int item) {
+  int lo = 0, hi = a.nbeam - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.beams[mid].item0 <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Channels summed for a work item.
+__device__ __forceinline__ int item_nact(const DedispArgs &a, int item) {
+  if (!a.beams) return a.nact;
+  const DedispBeam &bm = a.beams[beam_of(a, item)];
+  return bm.meta ? bm.nact : a.nact;
+}
 
 template <int DPT>
 __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
-  int bi = 0;
-  if (a.beams) {
-    int lo = 0, hi = a.nbeam - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (a.beams[mid].item0 <= item) lo = mid; else hi = mid - 1;
-    }
-    bi = lo;
-  }
-  const DedispBeam bm = a.beams ? a.beams[bi] : a.one;
+  const DedispBeam bm = a.beams ? a.beams[beam_of(a, item)] : a.one;
   const int ntiles = (bm.dm_count + DPT - 1) / DPT;
   const int l = item - bm.item0;
   const int per_group = a.group * a.ntt;
@@ -167,8 +176,10 @@ __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
   it.packed = bm.packed;
   it.out = bm.out;
   it.dm_count = bm.dm_count;
-  it.meta = a.tile_meta + (size_t)it.tile * a.nact;
-  it.off = a.tile_off + (size_t)it.tile * a.nact * off_width(DPT);
+  const bool own = a.beams && bm.meta;
+  it.nact = own ? bm.nact : a.nact;
+  it.meta = (own ? bm.meta : a.tile_meta) + (size_t)it.tile * it.nact;
+  it.off = (own ? bm.off : a.tile_off) + (size_t)it.tile * it.nact * off_width(DPT);
   return it;
 }
 
@@ -196,16 +207,19 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t unit = (uint32_t)a.unit;  // 1, unknown to the compiler
-  // Stage g of the block (its k-th item, stage g % nstage) is staged by
-  // warp g % 8, lane i copying channel i; the item a warp is staging is
-  // kept in shared memory to spare registers.
+  // Stage g of the block (the block's stages counted over its items in
+  // order; an item has ceil(nact / CC) of them, nact its beam's channels)
+  // is staged by warp g % 8, lane i copying channel i.  Each warp keeps a
+  // cursor to its next stage in shared memory to spare registers.
   struct Staged {
     const uint32_t *packed;
     const int4 *meta;
     const int *off;
     long w0;
+    int k, st, nst, nact;  // stage st of the nst stages of block-local item k
   };
-  Staged *staged = reinterpret_cast<Staged *>(reinterpret_cast<char *>(smem) + 64 + 32 * warp);
+  static_assert(64 + NWARP * sizeof(Staged) <= kBarBytes, "staging cursors");
+  Staged *staged = reinterpret_cast<Staged *>(reinterpret_cast<char *>(smem) + 64 + sizeof(Staged) * warp);
 
   if (tid == 0) {
     for (int b = 0; b < nbuf; ++b) {
@@ -215,12 +229,35 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
     mbar_fence_init();
   }
   __syncthreads();
-  const int nstage = (a.nact + CC - 1) / CC;
   if (blockIdx.x >= a.nitems) return;
-  const unsigned g_end = (unsigned)((a.nitems - 1 - blockIdx.x) / gridDim.x + 1) * (unsigned)nstage;
 
+  // lane 0: block-local item k into the cursor (false past the block's items)
+  auto load_item = [&](int k) -> bool {
+    const int item = blockIdx.x + k * gridDim.x;
+    if (item >= a.nitems) return false;
+    const Item it = item_at<DPT>(a, item);
+    *staged = Staged{it.packed, it.meta, it.off, it.w0, k, 0, (it.nact + CC - 1) / CC, it.nact};
+    return true;
+  };
+  // lane 0: the cursor n stages on, over items without channels (false past
+  // the block's last stage)
+  auto advance = [&](int n) -> bool {
+    int st = staged->st + n;
+    while (st >= staged->nst) {
+      st -= staged->nst;
+      if (!load_item(staged->k + 1)) return false;
+    }
+    staged->st = st;
+    return true;
+  };
   unsigned g_next = (unsigned)warp;  // next stage this warp stages
-  int staged_k = -1;                 // block-local item index held in *staged
+  bool p_done;                       // no stage left for this warp
+  {
+    int more = 0;
+    if (lane == 0) more = load_item(0) && advance(warp);
+    p_done = !__shfl_sync(0xffffffffu, more, 0);
+    __syncwarp();
+  }
 
   // Stages stage g_next into buffer g_next % nbuf; `block`: may wait for
   // the buffer to be released, else returns false if it is not free yet.
@@ -238,16 +275,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
         return false;
       }
     }
-    const int k = (int)(g / (unsigned)nstage), st = (int)(g % (unsigned)nstage);
-    if (k != staged_k) {
-      if (lane == 0) {
-        const Item it = item_at<DPT>(a, blockIdx.x + k * gridDim.x);
-        *staged = Staged{it.packed, it.meta, it.off, it.w0};
-      }
-      staged_k = k;
-      __syncwarp();
-    }
-    const int k0 = st * CC, nc = min(CC, a.nact - k0);
+    const int k0 = staged->st * CC, nc = min(CC, staged->nact - k0);
     const uint32_t bar = full_of(b);
     fence_proxy_async();
     if (lane < nc) {
@@ -277,6 +305,10 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
     }
     __syncwarp();
     g_next += NWARP;
+    int more = 0;
+    if (lane == 0) more = advance(NWARP);
+    p_done = !__shfl_sync(0xffffffffu, more, 0);
+    __syncwarp();
     return true;
   };
   // After a wait ran out: record it, let this warp's copies land, end.
@@ -288,6 +320,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
 
   unsigned gs_c = 0;  // stages consumed
   for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    const int nact = item_nact(a, item), nstage = (nact + CC - 1) / CC;
     uint32_t acc_e[DPT], acc_o[DPT], tot[DPT][4];
 #pragma unroll
     for (int m = 0; m < DPT; ++m) {
@@ -299,11 +332,11 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
       {
         // keep up to nbuf stages in flight; the stage about to be read must be issued
         bool to = false;
-        while (g_next < g_end && g_next < gs_c + nbuf)
+        while (!p_done && g_next < gs_c + nbuf)
           if (!issue(g_next <= gs_c, &to)) break;
         if (to) return fail(gs_c);
       }
-      const int b = (int)(gs_c % (unsigned)nbuf), nc = min(CC, a.nact - st * CC);
+      const int b = (int)(gs_c % (unsigned)nbuf), nc = min(CC, nact - st * CC);
       if (!mbar_wait(full_of(b), (gs_c / nbuf) & 1u)) return fail(gs_c);
       const uint32_t rbase = rows_of(b) + (uint32_t)tid * 4u;
       const uint32_t shb = sh_of(b), offb = off_of(b);
@@ -393,6 +426,21 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
       }
     }
   }
+}
+
+// Block (x, job): tiles x, x + gridDim.x, ... of job `job`; a thread per
+// channel of the job copies its table entry and dpt offsets.
+__global__ void k_gather_tables(const int4 *__restrict__ meta, const int *__restrict__ off, int nch, int dpt,
+                                const TableJob *__restrict__ jobs, const int *__restrict__ chans,
+                                int4 *__restrict__ bmeta, int *__restrict__ boff) {
+  const TableJob j = jobs[blockIdx.y];
+  for (int tile = blockIdx.x; tile < j.ntiles; tile += gridDim.x)
+    for (int k = threadIdx.x; k < j.nact; k += blockDim.x) {
+      const size_t src = (size_t)tile * nch + chans[j.chans0 + k];
+      const size_t dst = (size_t)j.meta0 + (size_t)tile * j.nact + k;
+      bmeta[dst] = meta[src];
+      for (int m = 0; m < dpt; ++m) boff[dst * dpt + m] = off[src * dpt + m];
+    }
 }
 
 __global__ void k_pack(const uint8_t *__restrict__ plain, uint32_t *__restrict__ packed,
@@ -595,6 +643,16 @@ cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
     case 1: return launch_cc<1>(a, s);
   }
   return cudaErrorInvalidValue;
+}
+
+cudaError_t gather_tables(const int4 *meta, const int *off, int nch, int dpt, const TableJob *jobs, int njobs,
+                          int max_tiles, const int *chans, int4 *bmeta, int *boff, cudaStream_t s) {
+  if (njobs <= 0 || max_tiles <= 0) return cudaSuccess;
+  if (dpt < 8 || njobs > 65535) return cudaErrorInvalidValue;
+  k_gather_tables<<<dim3((unsigned)std::min(max_tiles, 64), (unsigned)njobs), 256, 0, s>>>(meta, off, nch, dpt,
+                                                                                         jobs, chans, bmeta, boff);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t pack_ring(const uint8_t *plain, uint32_t *packed, int nbeam, int nchan,

@@ -98,6 +98,11 @@ struct DedispBeam {
   long win0;                // ring position of window sample 0
   int dm_count;             // trials of this beam: the first dm_count of the table
   int item0;                // first work item of the beam (prefix over beams)
+  // the beam's own tile tables over its nact channels (laid out as the
+  // launch's tile_meta / tile_off); null: the launch's tables
+  const int4 *meta;
+  const int *off;
+  int nact;
 };
 
 struct DedispArgs {
@@ -122,6 +127,16 @@ struct DedispArgs {
   const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - that delay), bytes
   int *err;                 // device status word: bit 0 = a staging wait timed out (may be null)
 };
+// One beam's tile tables gathered from a launch's tables (all nch channels):
+// rows [meta0, meta0 + ntiles * nact) of the output, channels chans[chans0 ..).
+struct TableJob {
+  long meta0;
+  int chans0, nact, ntiles;
+};
+// Gathers the rows of every job's channels from meta/off (tile shape dpt >= 8)
+// into bmeta / boff.
+cudaError_t gather_tables(const int4 *meta, const int *off, int nch, int dpt, const TableJob *jobs, int njobs,
+                          int max_tiles, const int *chans, int4 *bmeta, int *boff, cudaStream_t s);
 // Work items of one beam for a tile shape.
 inline int dedisp_items(int dm_count, int dpt, int ntt) { return (dm_count + dpt - 1) / dpt * ntt; }
 inline int dedisp_time_tiles(int nout) { return (nout + 4 * kPackS - 1) / (4 * kPackS); }

@@ -36,8 +36,27 @@ def _single(hella, params, ceiling, kill, beam):
 @pytest.mark.parametrize("use_graph,wpp", [(True, 0), (False, 2)])
 def test_batch_equals_independent_runs(hella, use_graph, wpp):
     params, ceilings, kill, skies = _setup()
+    _compare(hella, params, ceilings, kill, skies, widths_per_pass=wpp, use_graph=use_graph)
+
+
+def test_batch_killmask_extremes(hella):
+    """Beams that kill every channel, all but one, none, every other one,
+    and the first 8 (a whole staging step): each beam sums only its own
+    channels and still equals its single-beam context."""
+    params, ceilings, kill, skies = _setup(seed=45)
+    nchan = kill.shape[1]
+    kill[0] = 0
+    kill[1] = 0
+    kill[1, 77] = 1
+    kill[2] = 1
+    kill[3] = np.arange(nchan) % 2
+    kill[4, :8] = 0
+    _compare(hella, params, ceilings, kill, skies)
+
+
+def _compare(hella, params, ceilings, kill, skies, **batch_kw):
     base = hella.default_params(**dict(params, nbeam=NB))
-    bt = hella.Batch(base, dm_max=ceilings, killmask=kill, widths_per_pass=wpp, use_graph=use_graph)
+    bt = hella.Batch(base, dm_max=ceilings, killmask=kill, **batch_kw)
     singles = [_single(hella, params, ceilings[b], kill[b], b) for b in range(NB)]
     assert [bt.info(b).ndms for b in range(NB)] == [s.info.ndms for s in singles]
     assert [bt.info(b).ntime for b in range(NB)] == [s.info.ntime for s in singles]

@@ -469,6 +469,7 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
   a.tile_meta = tb.meta;
   a.tile_off = tb.off;
   a.err = b->d_err;
+  for (int i = 0; i < b->nbeam; ++i) a.varied |= b->dbeams[i].meta != nullptr;
   *out = a;
   return HELLA_OK;
 }

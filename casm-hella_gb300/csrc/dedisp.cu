@@ -37,6 +37,7 @@
 #include "hg_internal.h"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace hg {
 namespace {
@@ -160,7 +161,8 @@ __device__ __forceinline__ int item_nact(const DedispArgs &a, int item) {
   return bm.meta ? bm.nact : a.nact;
 }
 
-template <int DPT>
+// VAR: the beam's own tables when it has them (else the launch's).
+template <int DPT, bool VAR = false>
 __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
   const DedispBeam bm = a.beams ? a.beams[beam_of(a, item)] : a.one;
   const int ntiles = (bm.dm_count + DPT - 1) / DPT;
@@ -176,10 +178,16 @@ __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
   it.packed = bm.packed;
   it.out = bm.out;
   it.dm_count = bm.dm_count;
-  const bool own = a.beams && bm.meta;
-  it.nact = own ? bm.nact : a.nact;
-  it.meta = (own ? bm.meta : a.tile_meta) + (size_t)it.tile * it.nact;
-  it.off = (own ? bm.off : a.tile_off) + (size_t)it.tile * it.nact * off_width(DPT);
+  if constexpr (VAR) {
+    const bool own = a.beams && bm.meta;
+    it.nact = own ? bm.nact : a.nact;
+    it.meta = (own ? bm.meta : a.tile_meta) + (size_t)it.tile * it.nact;
+    it.off = (own ? bm.off : a.tile_off) + (size_t)it.tile * it.nact * off_width(DPT);
+  } else {
+    it.nact = a.nact;
+    it.meta = a.tile_meta + (size_t)it.tile * a.nact;
+    it.off = a.tile_off + (size_t)it.tile * a.nact * off_width(DPT);
+  }
   return it;
 }
 
@@ -191,7 +199,12 @@ __device__ __forceinline__ Item item_at(const DedispArgs &a, int item) {
 // Byte permutes and three-input adds share the half-rate ALU pipe, and
 // multiply-adds the half-rate heavy FMA pipe, so MODE 3 leaves 2.5 ALU
 // and 2 multiply-add instructions per word.
-template <int DPT, int CC, int MODE>
+//
+// VAR: the launch's items differ in their number of stages (beams with
+// tables of their own), so each warp walks a cursor over the items; else
+// every item has ceil(a.nact / CC) stages and stage g maps to item and
+// stage by division.
+template <int DPT, int CC, int MODE, bool VAR>
 __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int rowstride, int nbuf) {
   extern __shared__ __align__(128) uint32_t smem[];
   constexpr int OFFW = off_width(DPT);
@@ -209,15 +222,23 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
   const uint32_t unit = (uint32_t)a.unit;  // 1, unknown to the compiler
   // Stage g of the block (the block's stages counted over its items in
   // order; an item has ceil(nact / CC) of them, nact its beam's channels)
-  // is staged by warp g % 8, lane i copying channel i.  Each warp keeps a
-  // cursor to its next stage in shared memory to spare registers.
-  struct Staged {
+  // is staged by warp g % 8, lane i copying channel i.  The item a warp is
+  // staging (VAR: with a cursor to its next stage) is kept in shared memory
+  // to spare registers.
+  struct StagedFix {
+    const uint32_t *packed;
+    const int4 *meta;
+    const int *off;
+    long w0;
+  };
+  struct StagedVar {
     const uint32_t *packed;
     const int4 *meta;
     const int *off;
     long w0;
     int k, st, nst, nact;  // stage st of the nst stages of block-local item k
   };
+  using Staged = std::conditional_t<VAR, StagedVar, StagedFix>;
   static_assert(64 + NWARP * sizeof(Staged) <= kBarBytes, "staging cursors");
   Staged *staged = reinterpret_cast<Staged *>(reinterpret_cast<char *>(smem) + 64 + sizeof(Staged) * warp);
 
@@ -231,32 +252,43 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
   __syncthreads();
   if (blockIdx.x >= a.nitems) return;
 
-  // lane 0: block-local item k into the cursor (false past the block's items)
+  // lane 0: block-local item k into *staged (false past the block's items)
   auto load_item = [&](int k) -> bool {
     const int item = blockIdx.x + k * gridDim.x;
     if (item >= a.nitems) return false;
-    const Item it = item_at<DPT>(a, item);
-    *staged = Staged{it.packed, it.meta, it.off, it.w0, k, 0, (it.nact + CC - 1) / CC, it.nact};
+    const Item it = item_at<DPT, VAR>(a, item);
+    if constexpr (VAR)
+      *staged = Staged{it.packed, it.meta, it.off, it.w0, k, 0, (it.nact + CC - 1) / CC, it.nact};
+    else
+      *staged = Staged{it.packed, it.meta, it.off, it.w0};
     return true;
   };
   // lane 0: the cursor n stages on, over items without channels (false past
   // the block's last stage)
   auto advance = [&](int n) -> bool {
-    int st = staged->st + n;
-    while (st >= staged->nst) {
-      st -= staged->nst;
-      if (!load_item(staged->k + 1)) return false;
+    if constexpr (VAR) {
+      int st = staged->st + n;
+      while (st >= staged->nst) {
+        st -= staged->nst;
+        if (!load_item(staged->k + 1)) return false;
+      }
+      staged->st = st;
     }
-    staged->st = st;
     return true;
   };
+  const int nstage_u = (a.nact + CC - 1) / CC;  // !VAR: stages of every item
+  const unsigned g_end =                        // !VAR: stages of the block
+      VAR ? 0u : (unsigned)((a.nitems - 1 - blockIdx.x) / gridDim.x + 1) * (unsigned)nstage_u;
   unsigned g_next = (unsigned)warp;  // next stage this warp stages
+  int staged_k = -1;                 // !VAR: block-local item held in *staged
   bool p_done;                       // no stage left for this warp
-  {
+  if constexpr (VAR) {
     int more = 0;
     if (lane == 0) more = load_item(0) && advance(warp);
     p_done = !__shfl_sync(0xffffffffu, more, 0);
     __syncwarp();
+  } else {
+    p_done = false;  // unused: g_end bounds the stages
   }
 
   // Stages stage g_next into buffer g_next % nbuf; `block`: may wait for
@@ -275,7 +307,22 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
         return false;
       }
     }
-    const int k0 = staged->st * CC, nc = min(CC, staged->nact - k0);
+    int st;
+    if constexpr (VAR) {
+      st = staged->st;
+    } else {
+      const int k = (int)(g / (unsigned)nstage_u);
+      st = (int)(g % (unsigned)nstage_u);
+      if (k != staged_k) {
+        if (lane == 0) load_item(k);
+        staged_k = k;
+        __syncwarp();
+      }
+    }
+    int nact_st;
+    if constexpr (VAR) nact_st = staged->nact;
+    else nact_st = a.nact;
+    const int k0 = st * CC, nc = min(CC, nact_st - k0);
     const uint32_t bar = full_of(b);
     fence_proxy_async();
     if (lane < nc) {
@@ -305,10 +352,12 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
     }
     __syncwarp();
     g_next += NWARP;
-    int more = 0;
-    if (lane == 0) more = advance(NWARP);
-    p_done = !__shfl_sync(0xffffffffu, more, 0);
-    __syncwarp();
+    if constexpr (VAR) {
+      int more = 0;
+      if (lane == 0) more = advance(NWARP);
+      p_done = !__shfl_sync(0xffffffffu, more, 0);
+      __syncwarp();
+    }
     return true;
   };
   // After a wait ran out: record it, let this warp's copies land, end.
@@ -320,7 +369,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
 
   unsigned gs_c = 0;  // stages consumed
   for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
-    const int nact = item_nact(a, item), nstage = (nact + CC - 1) / CC;
+    const int nact = VAR ? item_nact(a, item) : a.nact;
+    const int nstage = VAR ? (nact + CC - 1) / CC : nstage_u;
     uint32_t acc_e[DPT], acc_o[DPT], tot[DPT][4];
 #pragma unroll
     for (int m = 0; m < DPT; ++m) {
@@ -332,7 +382,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_dedisp(DedispArgs a, int 
       {
         // keep up to nbuf stages in flight; the stage about to be read must be issued
         bool to = false;
-        while (!p_done && g_next < gs_c + nbuf)
+        while ((VAR ? !p_done : g_next < g_end) && g_next < gs_c + nbuf)
           if (!issue(g_next <= gs_c, &to)) break;
         if (to) return fail(gs_c);
       }
@@ -592,15 +642,15 @@ DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int n
 
 namespace {
 
-template <int DPT, int CC, int MODE>
-cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
+template <int DPT, int CC, int MODE, bool VAR>
+cudaError_t launch_var(const DedispArgs &a, cudaStream_t s) {
   const int rowstride = row_words(a.max_spread);
   int nbuf = a.nbuf ? a.nbuf : dedisp_nbuf(DPT, CC, a.max_spread);
   if (!nbuf) nbuf = 2;  // very coarse DM lists: one block per SM
   if (nbuf < 2 || nbuf > kMaxBuf) return cudaErrorInvalidValue;
   const size_t smem = smem_bytes(DPT, CC, rowstride, nbuf);
   if (smem > 227 * 1024) return cudaErrorInvalidValue;
-  auto kern = k_dedisp<DPT, CC, MODE>;
+  auto kern = k_dedisp<DPT, CC, MODE, VAR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -612,6 +662,18 @@ cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
   kern<<<grid, kDedispThreads, smem, s>>>(a, rowstride, nbuf);
   count_launches(1);
   return cudaGetLastError();
+}
+
+// Items with differing stage counts come only from tables of 8 or more
+// trials per tile.
+template <int DPT, int CC, int MODE>
+cudaError_t launch(const DedispArgs &a, cudaStream_t s) {
+  if constexpr (DPT >= 8) {
+    if (a.varied) return launch_var<DPT, CC, MODE, true>(a, s);
+  } else {
+    if (a.varied) return cudaErrorInvalidValue;
+  }
+  return launch_var<DPT, CC, MODE, false>(a, s);
 }
 
 template <int DPT>
@@ -635,6 +697,7 @@ cudaError_t launch_cc(const DedispArgs &a, cudaStream_t s) {
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
   if (a.nitems <= 0 || a.nout <= 0 || a.nact <= 0) return cudaSuccess;
   if (a.R % 4 != 0 || a.ntt <= 0 || a.group <= 0 || a.nbeam <= 0) return cudaErrorInvalidValue;
+  if (a.varied && !a.beams) return cudaErrorInvalidValue;
   switch (a.dpt) {
     case 16: return launch_cc<16>(a, s);
     case 8: return launch_cc<8>(a, s);

@@ -126,6 +126,7 @@ struct DedispArgs {
   const int4 *tile_meta;    // [ntiles][nact] {channel, smallest delay(c, d) of the tile, spread, 0}
   const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - that delay), bytes
   int *err;                 // device status word: bit 0 = a staging wait timed out (may be null)
+  int varied;               // some beam has tables of its own (dpt >= 8): stage counts differ
 };
 // One beam's tile tables gathered from a launch's tables (all nch channels):
 // rows [meta0, meta0 + ntiles * nact) of the output, channels chans[chans0 ..).

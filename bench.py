@@ -248,6 +248,13 @@ def main():
         step(gi, False)
         gi += 1
     torch.cuda.synchronize()
+    # dedispersion tile shape: the autotuner's pick, timed on this context's own buffers
+    t_tune = time.perf_counter()
+    tune, _ = s.autotune(3)
+    tune_s = time.perf_counter() - t_tune
+    step(gi, False)
+    gi += 1
+    torch.cuda.synchronize()
 
     # ---------------- device-resident timing
     clocks = Clocks(local)
@@ -344,6 +351,7 @@ def main():
                    "tsamp": params["tsamp"],
                    "ndms": info.ndms, "max_delay": info.max_delay, "ntime": info.ntime,
                    "widths": info.nboxcar, "beams_per_gpu": 1, "parallelism": f"replicas{world}",
+                   "tuning": tune.as_dict(), "tune_s": round(tune_s, 2),
                    "l2": (f"inputs {'larger' if info.ndms * info.ntime_dd * 4 > 129e6 else 'smaller'} than L2: "
                           f"{G * nch / 1e6:.0f} MB gulp, {nch * info.ntime * 5 / 1e9:.2f} GB ring, "
                           f"{info.ndms * info.ntime_dd * 4 / 1e9:.2f} GB plane, "

@@ -38,10 +38,10 @@ WORKLOAD = ("full single beam: 2048 ch 375-468.75 MHz, tsamp 0.524288 ms, gulp 6
             "DM 0-2000 tol 1.25, widths 1-256, 7 sigma")
 METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp latency"
 UNIT = "beam·s/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_dedisp launch of this workload, from a
-# single-pass ncu capture of those two metrics on `bench.py --steps 1 --warmup 3 --no-cpu-baseline`
-# (8.09 GB read + 0.686 GB written)
-DEDISP_TRAFFIC_BYTES = 8.777e9
+# dram__bytes_read.sum + dram__bytes_write.sum of the timed k_dedisp launch of this workload
+# (its tile shape as set in main_full), from a single-pass ncu capture of those two metrics on
+# `bench.py --steps 1 --warmup 3 --no-cpu-baseline` (7.99 GB read + 0.673 GB written)
+DEDISP_TRAFFIC_BYTES = 8.664e9
 
 
 def args_():
@@ -248,13 +248,16 @@ def main():
         step(gi, False)
         gi += 1
     torch.cuda.synchronize()
-    # dedispersion tile shape: the autotuner's pick, timed on this context's own buffers
-    t_tune = time.perf_counter()
-    tune, _ = s.autotune(3)
-    tune_s = time.perf_counter() - t_tune
-    step(gi, False)
-    gi += 1
-    torch.cuda.synchronize()
+    # dedispersion tile shape: 16-trial tiles (the deepest staging that fits), DM tiles walked
+    # in groups of 8 per time tile, odd lanes and load addresses by multiply-adds (add mode 2).
+    # Modes 2 and 3 measured 19.40 ms on the full beam against 19.49 for mode 0; the autotuner
+    # lands within 0.3 % of that with groups of 2-4, which read 12 GB from DRAM per launch
+    # against 8.1 GB for groups of 8.
+    s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, 2))
+    try:
+        s.time_dedisp(None, 1)
+    except hg.HellaError:  # DM lists whose tiles hold fewer than 8 trials take add mode 0
+        s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, 0))
 
     # ---------------- device-resident timing
     clocks = Clocks(local)
@@ -353,7 +356,7 @@ def main():
                    "tsamp": params["tsamp"],
                    "ndms": info.ndms, "max_delay": info.max_delay, "ntime": info.ntime,
                    "widths": info.nboxcar, "beams_per_gpu": 1, "parallelism": f"replicas{world}",
-                   "tuning": tune.as_dict(), "tune_s": round(tune_s, 2),
+                   "tuning": s.get_tuning().as_dict(),
                    "l2": (f"inputs {'larger' if info.ndms * info.ntime_dd * 4 > 129e6 else 'smaller'} than L2: "
                           f"{G * nch / 1e6:.0f} MB gulp, {nch * info.ntime * 5 / 1e9:.2f} GB ring, "
                           f"{info.ndms * info.ntime_dd * 4 / 1e9:.2f} GB plane, "

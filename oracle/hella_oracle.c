@@ -606,6 +606,7 @@ struct ho_pipeline {
   int ntime, ndms, max_delay, ntime_dd, nbox, min_gulp, gulp_idx;
   float *dms, *table;
   int32_t *delays;
+  int32_t *killmask; /* [nbeam][nchan] or NULL (every channel summed) */
   uint8_t *ring;
   float *flagspec;
 };
@@ -648,6 +649,7 @@ void ho_pipeline_destroy(ho_pipeline *pl) {
   free(pl->dms);
   free(pl->table);
   free(pl->delays);
+  free(pl->killmask);
   free(pl->ring);
   free(pl->flagspec);
   free(pl);
@@ -671,6 +673,19 @@ const uint8_t *ho_pipeline_ring(const ho_pipeline *pl, int beam) {
 }
 const float *ho_pipeline_flagspec(const ho_pipeline *pl) { return pl->flagspec; }
 
+/* A dedisp plan's killmask for one beam (the reference holds one plan, so one
+ * killmask, per process: casm_hella_refactored.cu:204-212). */
+int ho_pipeline_set_killmask(ho_pipeline *pl, int beam, const int32_t *killmask) {
+  const int nchan = pl->p.nchan;
+  if (beam < 0 || beam >= pl->p.nbeam) return -1;
+  if (!pl->killmask) {
+    pl->killmask = (int32_t *)malloc(sizeof(int32_t) * (size_t)pl->p.nbeam * nchan);
+    for (size_t i = 0; i < (size_t)pl->p.nbeam * nchan; ++i) pl->killmask[i] = 1;
+  }
+  for (int c = 0; c < nchan; ++c) pl->killmask[(size_t)beam * nchan + c] = killmask ? killmask[c] : 1;
+  return 0;
+}
+
 int ho_search_window(const ho_pipeline *pl, const uint8_t *window, int beam,
                      int cap, ho_cand *cands, float *dd_out, float *boxes_out,
                      float *mean_out, float *std_out, float *sigma0) {
@@ -681,7 +696,8 @@ int ho_search_window(const ho_pipeline *pl, const uint8_t *window, int beam,
   float *bx = boxes_out ? boxes_out : (float *)malloc(sizeof(float) * bxn);
   /* dedisperse.cpp:17-48 (ntime_dedisp outputs, first ntime_dd kept) */
   ho_dedisperse(window, pl->ntime, (size_t)p->nchan, p->nchan, pl->delays, pl->ndms,
-                NULL, dd, (size_t)pl->ntime_dd, pl->ntime_dd);
+                pl->killmask ? pl->killmask + (size_t)beam * p->nchan : NULL, dd,
+                (size_t)pl->ntime_dd, pl->ntime_dd);
   ho_smooth_normalise(dd, pl->ndms, pl->ntime_dd, (size_t)pl->ntime_dd, p->wmin, p->wmax,
                       p->smooth_anchor, p->gulp, bx, mean_out, std_out);
   int n = ho_find_peaks(bx, pl->nbox, pl->ndms, p->gulp, p->snr, beam, cap, cands, sigma0);

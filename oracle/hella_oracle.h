@@ -203,6 +203,9 @@ int ho_pipeline_gulp(ho_pipeline *pl, const uint8_t *gulp, ho_cand *cands,
 /* Access to the last gulp's state for stage-level checks. */
 const uint8_t *ho_pipeline_ring(const ho_pipeline *pl, int beam); /* [NTIME][nchan] */
 const float *ho_pipeline_flagspec(const ho_pipeline *pl);
+/* Beam `beam`'s dedispersion killmask (killmask[c] == 0 drops channel c;
+ * NULL: every channel); -1 for a beam outside the pipeline. */
+int ho_pipeline_set_killmask(ho_pipeline *pl, int beam, const int32_t *killmask);
 
 /* Search one window (dedisperse + smooth + find_peaks) of one beam:
  * window u8 [ntime][nchan] with ntime >= ntime_dd + max_delay. */

@@ -106,6 +106,8 @@ def lib() -> C.CDLL:
         L.ho_pipeline_ring.argtypes = [_VP, C.c_int]
         L.ho_pipeline_flagspec.restype = C.POINTER(C.c_float)
         L.ho_pipeline_flagspec.argtypes = [_VP]
+        L.ho_pipeline_set_killmask.restype = C.c_int
+        L.ho_pipeline_set_killmask.argtypes = [_VP, C.c_int, _VP]
         L.ho_search_window.restype = C.c_int
         L.ho_search_window.argtypes = [_VP, _VP, C.c_int, C.c_int, _VP, _VP, _VP, _VP, _VP, _VP]
         L.ho_set_threads.argtypes = [C.c_int]
@@ -246,6 +248,14 @@ class Pipeline:
 
     def flagspec(self) -> np.ndarray:
         return np.ctypeslib.as_array(self.L.ho_pipeline_flagspec(self.h), shape=(self.nchan,)).copy()
+
+    def set_killmask(self, beam: int, killmask):
+        """Beam `beam`'s dedispersion killmask (0 drops a channel; None: all kept)."""
+        km = None if killmask is None else np.ascontiguousarray(killmask, np.int32)
+        if km is not None and km.shape != (self.nchan,):
+            raise ValueError("killmask needs one entry per channel")
+        if self.L.ho_pipeline_set_killmask(self.h, beam, None if km is None else km.ctypes.data) != 0:
+            raise ValueError("beam outside the pipeline")
 
     def gulp_step(self, gulp: np.ndarray):
         gulp = np.ascontiguousarray(gulp, np.uint8)

@@ -226,6 +226,29 @@ def test_gulp_loop_partial_channel_slices(hella, oracle, nchan):
     assert total > 0
 
 
+def test_gulp_loop_killmask(hella, oracle):
+    """A dedisp killmask (a fifth of the channels, runs of them and single
+    ones): candidates of a whole gulp loop identical to the oracle's."""
+    params, sky = synth.config_plain(seed=14, nchan=160, gulp=2048, dm_max=300.0)
+    sky.bursts[0].amp *= 4
+    rng = np.random.default_rng(14)
+    km = (rng.random(params["nchan"]) > 0.15).astype(np.int32)
+    km[40:56] = 0
+    s = _search(hella, params)
+    s.set_killmask(km)
+    pl = oracle_pipeline(oracle, params)
+    pl.set_killmask(0, km)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        x = sky.gulp(g, params["gulp"])[None]
+        got, sg = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert sg == so
+        assert cands_equal(got, want), (g, len(got), len(want))
+        total += len(got)
+    assert total > 0
+
+
 @pytest.mark.parametrize("gulp", [256, 1056, 2080])
 def test_gulp_loop_ragged_gulps(hella, oracle, gulp):
     """Gulps that are not multiples of the FIR's 2048-sample chunks, the ring

@@ -228,3 +228,30 @@ def test_pipeline_ring_is_left_shift(oracle):
     lo = max(0, -first)
     assert lo < pl.ntime - G
     assert np.array_equal(ring[lo:pl.ntime - G], stream[first + lo:3 * G])
+
+
+def test_pipeline_killmask_drops_channels(oracle):
+    """A beam's killmask leaves the dedispersed plane and candidates of a
+    searched window exactly those of the same window with the killed channels
+    zeroed, and leaves the other beam alone."""
+    params, sky = synth.config_plain(seed=13, nchan=128, gulp=2048, dm_max=300.0)
+    sky.bursts[0].amp *= 3
+    params["nbeam"] = 2
+    rng = np.random.default_rng(13)
+    km = (rng.random(params["nchan"]) > 0.15).astype(np.int32)
+    pk = oracle_pipeline(oracle, params)
+    pk.set_killmask(1, km)
+    p0 = oracle_pipeline(oracle, params)
+    win = np.stack([oracle.flag_beam(sky.gulp(g, params["gulp"]))[0] for g in range(pk.min_gulp + 1)])
+    win = win.reshape(-1, params["nchan"])[-pk.ntime:]
+    zeroed = win * km[None, :].astype(np.uint8)
+    a = pk.search_window(win, beam=1)
+    b = p0.search_window(zeroed, beam=1)
+    assert np.array_equal(a["dd"], b["dd"]) and len(a["cands"]) == len(b["cands"])
+    assert np.array_equal(a["cands"], b["cands"])
+    c = pk.search_window(win, beam=0)
+    d = p0.search_window(win, beam=0)
+    assert np.array_equal(c["dd"], d["dd"]) and np.array_equal(c["cands"], d["cands"])
+    with pytest.raises(ValueError):
+        pk.set_killmask(2, km)
+

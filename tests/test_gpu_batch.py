@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import synth
-from helpers import cands_equal
+from helpers import cands_equal, oracle_pipeline
 
 pytestmark = pytest.mark.gpu
 
@@ -39,10 +39,11 @@ def test_batch_equals_independent_runs(hella, use_graph, wpp):
     _compare(hella, params, ceilings, kill, skies, widths_per_pass=wpp, use_graph=use_graph)
 
 
-def test_batch_killmask_extremes(hella):
+def test_batch_killmask_extremes(hella, oracle):
     """Beams that kill every channel, all but one, none, every other one,
     and the first 8 (a whole staging step): each beam sums only its own
-    channels and still equals its single-beam context."""
+    channels and equals its single-beam context and an oracle pipeline with
+    its DM ceiling and killmask."""
     params, ceilings, kill, skies = _setup(seed=45)
     nchan = kill.shape[1]
     kill[0] = 0
@@ -51,13 +52,19 @@ def test_batch_killmask_extremes(hella):
     kill[2] = 1
     kill[3] = np.arange(nchan) % 2
     kill[4, :8] = 0
-    _compare(hella, params, ceilings, kill, skies)
+    _compare(hella, params, ceilings, kill, skies, oracle=oracle)
 
 
-def _compare(hella, params, ceilings, kill, skies, **batch_kw):
+def _compare(hella, params, ceilings, kill, skies, oracle=None, **batch_kw):
     base = hella.default_params(**dict(params, nbeam=NB))
     bt = hella.Batch(base, dm_max=ceilings, killmask=kill, **batch_kw)
     singles = [_single(hella, params, ceilings[b], kill[b], b) for b in range(NB)]
+    pls = []
+    if oracle is not None:
+        for b in range(NB):
+            pl = oracle_pipeline(oracle, params, dm_max=float(ceilings[b]))
+            pl.set_killmask(0, kill[b])
+            pls.append(pl)
     assert [bt.info(b).ndms for b in range(NB)] == [s.info.ndms for s in singles]
     assert [bt.info(b).ntime for b in range(NB)] == [s.info.ntime for s in singles]
     total = 0
@@ -72,6 +79,10 @@ def _compare(hella, params, ceilings, kill, skies, **batch_kw):
             mine = got[off:off + counts[b]]
             off += counts[b]
             assert cands_equal(mine, want), (g, b, len(mine), len(want))
+            if pls:
+                ref, so = pls[b].gulp_step(x[b:b + 1])
+                ref["beam"] = b
+                assert so == sw and cands_equal(mine, ref), (g, b, len(mine), len(ref))
             if sw:
                 assert np.array_equal(bt.copy_dedisp(b), s.copy_dedisp()), (g, b)
             total += len(want)

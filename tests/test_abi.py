@@ -100,3 +100,28 @@ def test_search_rejects_bad_params(hella):
         p = hella.default_params(**bad)
         assert L.hella_create(C.byref(h), C.byref(p)) == 1
     assert L.hella_status_string(6) == b"hbm budget exceeded"
+
+
+def test_batch_bytes_sizing(hella):
+    """hella_batch_bytes (host only): affine in the number of slots, each slot
+    holding at least its ring (5 bytes per channel-sample), its dedispersed
+    plane and its tile tables (6 bytes per trial and channel); per-beam DM
+    ceilings shrink it; a batch without beams is refused."""
+    p = dict(nchan=128, gulp=2048, tsamp=1.048576e-3, plan_dt=1.048576e-3, f0_mhz=468.75,
+             df_mhz=-(468.75 - 375.0) / 128, dm_min=0.0, dm_max=400.0, dm_tol=1.25, ti_us=40.0,
+             width_min=1, width_max=64, snr=7.0)
+    kw = dict(dynamic=True, inflight=2, widths_per_pass=6)
+    size = {n: hella.batch_bytes(hella.default_params(**dict(p, nbeam=n)), **kw) for n in (3, 4, 5)}
+    step = size[4] - size[3]
+    assert size[5] - size[4] == step
+    plan = hella.Plan(p["nchan"], p["plan_dt"], p["f0_mhz"], p["df_mhz"])
+    plan.generate_dm_list(p["dm_min"], p["dm_max"], p["ti_us"], p["dm_tol"])
+    ndms, nch = plan.dm_count, p["nchan"]
+    ntime = 32 * ((p["gulp"] + plan.max_delay + p["width_max"]) // 32 + 1)
+    plan.close()
+    assert step >= nch * ntime * 5 + ndms * (p["gulp"] + p["width_max"]) * 4 + (ndms + 15) * nch * 6
+    lower = hella.batch_bytes(hella.default_params(**dict(p, nbeam=4)), dm_max=np.full(4, 150.0, np.float32),
+                              inflight=2, widths_per_pass=6)
+    assert lower < size[4]
+    with pytest.raises(hella.HellaError):
+        hella.batch_bytes(hella.default_params(**dict(p, nbeam=0)), **kw)

@@ -92,10 +92,13 @@ __device__ __forceinline__ void load_lut_slice(__half *lut_s, const __half *lut,
 // (below 32*floor(w/32)) in time order.  Block = 32 channels x 8 lanes, one
 // chain a thread (65536 chains for 2048 channels: too few for the
 // four-channel form to hide the memory latency); the row bytes are loaded
-// kLaneB at a time so that as many loads are in flight.  The table slice
-// is staged as lut_s[level][channel] through 16-byte loads of eight levels.
-constexpr int kLaneC = 32, kLaneB = 16;
-__global__ void __launch_bounds__(256) k_lane_partials(const uint8_t *__restrict__ gulp,
+// kLaneB at a time so that as many loads are in flight (64 a thread, about
+// 4 MB over the GPU; the two-blocks bound lets the compiler give them the
+// registers, 96, where it would otherwise fit 32 and interleave them with
+// the sums).  The table slice is staged as lut_s[level][channel] through
+// 16-byte loads of eight levels.
+constexpr int kLaneC = 32, kLaneB = 64;
+__global__ void __launch_bounds__(256, 2) k_lane_partials(const uint8_t *__restrict__ gulp,
                                                        const __half *__restrict__ lut,
                                                        float *__restrict__ part, int nchan, int w) {
   __shared__ __half lut_s[256][kLaneC];

@@ -127,9 +127,11 @@ __global__ void __launch_bounds__(256, 2) k_lane_partials(const uint8_t *__restr
 // sums columns j, j+256, ... below nw = 256*floor(w/256).  TS: values
 // divided by half(ts[t]) (divide_by_ts, timeseries.cu:38-55).  VAR:
 // (x - mean)^2 with the fused multiply-add the reference's compiler emits.
+// The two-blocks bound gives the unrolled loads registers (44-64 instead of
+// 32), as in k_lane_partials.
 template <bool VAR, bool TS>
-__global__ void __launch_bounds__(kRowT) k_row_partials(const uint8_t *__restrict__ gulp, FlagState st,
-                                                         int which) {
+__global__ void __launch_bounds__(kRowT, 2) k_row_partials(const uint8_t *__restrict__ gulp, FlagState st,
+                                                            int which) {
   extern __shared__ __align__(16) __half lut4_s[];
   const int b = blockIdx.z, c0 = blockIdx.x * kQC, nchan = st.nchan, w = st.gulp;
   load_lut_slice<kQC>(lut4_s, st.lut, nchan, b, c0);

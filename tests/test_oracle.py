@@ -146,6 +146,29 @@ def test_dedisp_matches_numpy(oracle):
     assert np.array_equal(out, ref.astype(np.float32))
 
 
+def test_dedisp_properties(oracle):
+    """Linearity (a + b with no byte overflow sums to the sum of the planes),
+    a killmask equal to zeroing those channels, a time shift of the input
+    shifting every trial, and DM trials in any order giving their rows."""
+    dms, delays = _plan(oracle, nchan=64, dm_max=80.0)
+    rng = np.random.default_rng(21)
+    nsamps = int(delays.max()) + 400
+    a = rng.integers(0, 128, (nsamps, 64), dtype=np.uint8)
+    b = rng.integers(0, 128, (nsamps, 64), dtype=np.uint8)
+    da, db, dab = (oracle.dedisperse(v, delays) for v in (a, b, a + b))
+    assert np.array_equal(dab, da + db)
+    km = (rng.random(64) > 0.3).astype(np.int32)
+    zeroed = a * km[None, :].astype(np.uint8)
+    assert np.array_equal(oracle.dedisperse(a, delays, killmask=km), oracle.dedisperse(zeroed, delays))
+    k = 37
+    shifted = np.concatenate([np.zeros((k, 64), np.uint8), a])[:nsamps]
+    ds = oracle.dedisperse(shifted, delays)
+    assert np.array_equal(ds[:, k:], da[:, :da.shape[1] - k])
+    perm = rng.permutation(len(dms))
+    dp = oracle.dedisperse(a, delays[perm], nout=da.shape[1])
+    assert np.array_equal(dp, da[perm])
+
+
 # -------------------------------------------------------------- statistics
 
 def test_stddev_truncates_and_matches(oracle):

@@ -95,8 +95,8 @@ hella_status hella_fil_open(hella_fil **out, const char *path, int expect_nchan,
     } else if (key == "period") { ok = get_value(fl->f, &h.period);
     } else if (key == "fch1") { ok = get_value(fl->f, &h.fch1);
     } else if (key == "fchannel") {
-      double v;
-      ok = get_value(fl->f, &v);
+      if (h.nfreq >= HELLA_FIL_MAX_FREQ) return fail(HELLA_ERR_INVALID_ARG);
+      ok = get_value(fl->f, &h.frequency_table[h.nfreq]);
       h.nfreq++;
       h.fch1 = h.foff = 0.0;  // a frequency table is in use
     } else if (key == "foff") { ok = get_value(fl->f, &h.foff);

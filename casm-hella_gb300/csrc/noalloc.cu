@@ -22,13 +22,18 @@ std::mutex g_setup_mu;
 void *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device` (which must be current);
-// the first call per device resolves it.
+// the first call per device resolves it and clears the status word (the
+// first 256 bytes), which later calls only read and clear after reporting.
 hdd_error scratch_for(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return HDD_INVALID_DEVICE_INDEX;
   std::lock_guard<std::mutex> lk(g_setup_mu);
   if (!g_scratch_addr[device]) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return HDD_INTERNAL_GPU_ERROR;
+    }
+    if (cudaMemset(p, 0, 256) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
       cudaGetLastError();
       return HDD_INTERNAL_GPU_ERROR;
     }
@@ -54,7 +59,7 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   if (in_nbits != 8) return HDD_UNSUPPORTED_IN_NBITS;
   if (out_nbits != 32) return HDD_UNSUPPORTED_OUT_NBITS;
   if (nsamps <= (hdd_size)v.max_delay) return HDD_TOO_FEW_NSAMPS;
-  if (nsamps > (hdd_size)(65535u * 32u)) return HDD_STATIC_SCRATCH_EXCEEDED;
+  if (nsamps > (hdd_size)(65535u * 32u)) return HDD_UNKNOWN_ERROR;  // transpose grid limit, as hdd_execute_guru
   const int nout = (int)(nsamps - v.max_delay);
   if (in_stride < (hdd_size)v.nchans) return HDD_INVALID_STRIDE;
   if (out_stride % 4 != 0 || out_stride < (hdd_size)nout * 4) return HDD_INVALID_STRIDE;
@@ -83,9 +88,10 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   uint32_t *d_packed = reinterpret_cast<uint32_t *>(base + o_packed);
   int *d_err = reinterpret_cast<int *>(base + o_err);
 
-  // The tables are rewritten by every call: nothing depends on what the
-  // previous call left in the array.
-  if (cudaMemsetAsync(d_err, 0, sizeof(int), s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+  // The tables, staging copy and packed ring are rewritten by every call.
+  // The status word is not: a staging timeout sets it and it stays set until
+  // a synchronous call reads it, reports it and clears it, so a timeout in an
+  // HDD_ASYNC call surfaces at the next synchronous call.
   if (!tb.meta.empty() &&
       (cudaMemcpyAsync(d_meta, tb.meta.data(), tb.meta.size() * sizeof(int4), cudaMemcpyHostToDevice, s) !=
            cudaSuccess ||
@@ -109,8 +115,12 @@ extern "C" hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps, const h
   if (!(flags & HDD_ASYNC)) {
     if (cudaStreamSynchronize(s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
     int err = 0;
-    if (cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || err)
-      return HDD_INTERNAL_GPU_ERROR;  // err != 0: a staging wait timed out
+    if (cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return HDD_INTERNAL_GPU_ERROR;
+    if (err) {  // a staging wait of this call or of an earlier HDD_ASYNC call timed out
+      if (cudaMemsetAsync(d_err, 0, sizeof(int), s) != cudaSuccess) return HDD_INTERNAL_GPU_ERROR;
+      return HDD_INTERNAL_GPU_ERROR;
+    }
   }
   return HDD_NO_ERROR;
 }

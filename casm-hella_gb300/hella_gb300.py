@@ -64,7 +64,8 @@ class FilHeader(C.Structure):
                [(k, C.c_double) for k in ("tstart", "tsamp", "fch1", "foff", "refdm", "az_start", "za_start",
                                           "src_raj", "src_dej", "period")] + \
                [("isign", C.c_char), ("npuls", C.c_long), ("source_name", C.c_char * 81),
-                ("rawdatafile", C.c_char * 81), ("nfreq", C.c_int), ("header_bytes", C.c_long)]
+                ("rawdatafile", C.c_char * 81), ("nfreq", C.c_int), ("header_bytes", C.c_long),
+                ("frequency_table", C.c_double * 4096)]
 
 
 class RefineParams(C.Structure):

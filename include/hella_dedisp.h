@@ -63,7 +63,7 @@ typedef enum {
 } hdd_error;
 
 /* Execute flags; the reference passes 1<<2 (device pointers,
- * dedisperse.cpp:417). */
+ * dedisperse.cpp:32-38). */
 #define HDD_USE_DEFAULT 0
 #define HDD_HOST_POINTERS (1 << 1)
 #define HDD_DEVICE_POINTERS (1 << 2)
@@ -110,7 +110,7 @@ const int *hdd_get_delay_table(const hdd_plan plan);
 hdd_error hdd_execute(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
                       hdd_size in_nbits, hdd_byte *out, hdd_size out_nbits,
                       unsigned flags);
-/* dedisp_execute_adv (dedisperse.cpp:418): strides in bytes. */
+/* dedisp_execute_adv (dedisperse.cpp:32-38): strides in bytes. */
 hdd_error hdd_execute_adv(hdd_plan plan, hdd_size nsamps, const hdd_byte *in,
                           hdd_size in_nbits, hdd_size in_stride,
                           hdd_byte *out, hdd_size out_nbits,
@@ -139,17 +139,29 @@ const char *hdd_get_error_string(hdd_error error);
  * the library holds that array until the process exits.  The call makes no
  * cudaMalloc/cudaFree and no other allocating call.
  *
- * Limit: the dedispersion tile tables (at most 32 bytes per DM trial per
+ * Limits: the dedispersion tile tables (at most 32 bytes per DM trial per
  * active channel; 5 with the usual 16-trial tiles) plus 5*nchans*R bytes
  * (R = nsamps rounded up to a multiple of 4), each part aligned to 256
  * bytes, must fit in HDD_NOALLOC_SCRATCH_BYTES, else
- * HDD_STATIC_SCRATCH_EXCEEDED.  in and
- * out are device pointers (HDD_HOST_POINTERS is rejected).  The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls share the
- * array and each one overwrites it completely, so nothing carries over from
- * the previous call; two calls whose device work overlaps in time (other
- * streams, other threads) race on it. */
+ * HDD_STATIC_SCRATCH_EXCEEDED.  nsamps above 65535*32 returns
+ * HDD_UNKNOWN_ERROR (the transpose's grid limit, as hdd_execute_guru).  in
+ * and out are device pointers (HDD_HOST_POINTERS is rejected).
+ *
+ * Set-up: the first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current) and clears its status
+ * word with a synchronous cudaMemset; make that first call before any
+ * stream capture.
+ *
+ * Sharing: all calls share the array.  Each call overwrites the tables and
+ * buffers it uses before reading them, so no data carries over from the
+ * previous call; two calls whose device work overlaps in time (other
+ * streams, other threads) race on it.
+ *
+ * Errors on the device: a staging wait that times out sets the status word,
+ * which stays set until a synchronous call (no HDD_ASYNC) reads it.  That
+ * call returns HDD_INTERNAL_GPU_ERROR and clears the word, so it reports a
+ * timeout of its own or of any HDD_ASYNC call before it; an HDD_ASYNC call
+ * itself returns HDD_NO_ERROR once its work is queued. */
 #define HDD_NOALLOC_SCRATCH_BYTES (32ul << 20)
 hdd_error hdd_execute_noalloc(hdd_plan plan, hdd_size nsamps,
                               const hdd_byte *in, hdd_size in_nbits,

@@ -24,6 +24,10 @@ extern "C" {
 #endif
 
 /* ---- SIGPROC filterbank (sigproc.cpp:60-191) */
+/* Entries of a FREQUENCY_START table (the reference's frequency_table[4096],
+ * sigproc.h:49); a file with more returns HELLA_ERR_INVALID_ARG, where the
+ * reference writes past its array. */
+#define HELLA_FIL_MAX_FREQ 4096
 typedef struct {
   int machine_id, telescope_id, data_type, nchans, nbits, nifs, barycentric, pulsarcentric, ibeam, nbeams;
   double tstart, tsamp, fch1, foff, refdm, az_start, za_start, src_raj, src_dej, period;
@@ -32,6 +36,8 @@ typedef struct {
   char source_name[81], rawdatafile[81];
   int nfreq;               /* entries of a FREQUENCY_START table (fch1 = foff = 0 then) */
   long header_bytes;       /* offset of the first sample */
+  double frequency_table[HELLA_FIL_MAX_FREQ]; /* the table's fchannel values, in file order
+                                                 (hdr->frequency_table, sigproc.cpp:121-123) */
 } hella_fil_header;
 
 typedef struct hella_fil hella_fil;

@@ -356,6 +356,11 @@ static void box_filter(const uint16_t *in, uint16_t *out, int nchan, int w,
     }
 }
 
+void ho_box_filter(const uint16_t *in, uint16_t *out, int nchan, int w, int xw,
+                   int yw, float k) {
+  box_filter(in, out, nchan, w, xw, yw, k);
+}
+
 /* calc_bandpass  flagger.cu:50-81: 256 threads per channel, thread t sums
  * its contiguous chunk of floor(w/256) samples in fp16, divides by
  * half(256*floor(w/256)), then an fp16 shared-memory tree. */

@@ -121,6 +121,11 @@ void ho_flag_beam(const uint8_t *gulp, int w, int nchan,
                   const ho_flag_params *fp, uint8_t *out, float *ts_out,
                   float *flagspec, ho_flag_trace *trace);
 
+/* The SCRUNCH box filter alone (convolution.cu:20-55): fp16 planes as bit
+ * patterns [nchan][w], an xw x yw box of taps k. */
+void ho_box_filter(const uint16_t *in, uint16_t *out, int nchan, int w, int xw,
+                   int yw, float k);
+
 /* ------------------------------------------------------------- smoothing
  * smooth.cpp:21-127.  Taps: the reference's 3 x (2sm+1) kernel, computed
  * exactly as smooth.cpp:47-58 (double u, float v, float products, float

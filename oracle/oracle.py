@@ -206,6 +206,30 @@ def flag_beam_f16(ft: np.ndarray, fp: FlagParams | None = None, flagspec=None):
     return out, ts, trace
 
 
+def box_filter(plane: np.ndarray, xw: int, yw: int, k: float) -> np.ndarray:
+    """The SCRUNCH box filter (convolution.cu:20-55) on an fp16 plane given as
+    uint16 bit patterns [nchan][w]."""
+    plane = np.ascontiguousarray(plane, np.uint16)
+    out = np.zeros_like(plane)
+    L = lib()
+    L.ho_box_filter.argtypes = [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float]
+    L.ho_box_filter(plane.ctypes.data, out.ctypes.data, plane.shape[0], plane.shape[1], xw, yw, k)
+    return out
+
+
+def smooth_plane(dd: np.ndarray, sm: int, wmax: int, ntime_out: int, anchor: int = 1) -> np.ndarray:
+    """One width's pre-normalisation plane [ndms-2][ntime_out] (ho_smooth_plane)."""
+    dd = np.ascontiguousarray(dd, np.float32)
+    ndms, ntd = dd.shape
+    out = np.zeros((ndms - 2, ntime_out), np.float32)
+    L = lib()
+    L.ho_smooth_plane.argtypes = [_VP, C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int, _VP, C.c_int,
+                                  C.c_size_t]
+    L.ho_smooth_plane(dd.ctypes.data, ndms, ntd, ntd, sm, wmax, 2 * sm if anchor else 0, out.ctypes.data,
+                      ntime_out, ntime_out)
+    return out
+
+
 def smooth_taps(sm: int) -> np.ndarray:
     k = np.zeros(3 * (2 * sm + 1), np.float32)
     lib().ho_smooth_taps(sm, k.ctypes.data)

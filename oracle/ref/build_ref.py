@@ -1,6 +1,6 @@
 """Build the reference's stage code for the CPU (TEST INFRASTRUCTURE ONLY).
 
-Reads the read-only reference tree (default /root/reference, or $HELLA_REF),
+Reads the read-only reference tree (the first argument, or $HELLA_REF),
 copies the stage sources it needs into a temporary directory, rewrites each
 kernel launch `k<<<grid, block>>>(args)` into a call of the emulator in
 emu_cuda.h, sets NCHAN (a compile-time constant of the reference,
@@ -149,5 +149,15 @@ def build(ref: Path, nchan: int = 256, verbose: bool = False) -> Path:
     return lib
 
 
+def reference_tree(argv: list[str]) -> Path:
+    """The reference tree: argv[1], else $HELLA_REF; there is no default."""
+    path = argv[1] if len(argv) > 1 else os.environ.get("HELLA_REF")
+    if not path:
+        raise SystemExit(f"usage: python {Path(argv[0]).name} <reference tree>  (or set HELLA_REF)")
+    return Path(path)
+
+
 if __name__ == "__main__":
-    build(Path(os.environ.get("HELLA_REF", "/root/reference")), verbose=True)
+    import sys
+
+    build(reference_tree(sys.argv), verbose=True)

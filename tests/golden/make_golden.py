@@ -4,10 +4,10 @@ code (not part of the test run).
 Builds the reference's flagger, statistics, median filter, smoothing and
 peak-finding sources for the CPU under oracle/ref (the CUDA kernels run on
 an emulator; see oracle/ref/emu_cuda.h), runs them on the seeded cases of
-cases.py and records their outputs.  Needs the reference tree (default
-/root/reference, or $HELLA_REF); the tests only read the JSON it writes.
+cases.py and records their outputs.  Needs the reference tree (the first argument, or $HELLA_REF); the tests only
+read the JSON it writes.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference tree>
 """
 from __future__ import annotations
 
@@ -30,7 +30,7 @@ VP = C.c_void_p
 
 
 def main():
-    lib = build_ref.build(Path(os.environ.get("HELLA_REF", "/root/reference")), nchan=cases.NCHAN, verbose=True)
+    lib = build_ref.build(build_ref.reference_tree(sys.argv), nchan=cases.NCHAN, verbose=True)
     R = C.CDLL(str(lib))
     R.ref_flag.argtypes = [VP, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, VP, VP, VP, VP, VP, VP]
     R.ref_stddev_f32.restype = C.c_float

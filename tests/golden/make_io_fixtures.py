@@ -8,7 +8,7 @@ committed because the tree does not travel):
   ref_dada_header.txt  a DADA header from get_dada_header
                    (scripts/convert_fil_to_dada.py:14-30)
 
-Usage: python tests/golden/make_io_fixtures.py /root/reference
+Usage: python tests/golden/make_io_fixtures.py <reference tree>   (or set HELLA_REF)
 """
 import importlib.util
 import sys
@@ -45,4 +45,9 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HELLA_REF")
+    if not tree:
+        raise SystemExit("usage: python make_io_fixtures.py <reference tree>  (or set HELLA_REF)")
+    main(tree)

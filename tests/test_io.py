@@ -38,6 +38,8 @@ def test_fil_checks(hella, tmp_path):
             _w(fh, "HEADER_START")
             for k, fmt, v in keys:
                 _w(fh, k)
+                if fmt is None:
+                    continue
                 if fmt == "s":
                     _w(fh, v)
                 else:
@@ -61,6 +63,15 @@ def test_fil_checks(hella, tmp_path):
     p.write_bytes(struct.pack("<i", 3) + b"abc" + bytes(16))
     with pytest.raises(hella.HellaError):
         hella.Filterbank(p, 32)
+    # a frequency table: the fchannel values are kept in file order, fch1 = foff = 0 (sigproc.cpp:121-123)
+    freqs = [468.75 - 1.5 * i for i in range(32)]
+    tab = base + [("FREQUENCY_START", None, None)] + [("fchannel", "d", v) for v in freqs] + \
+        [("FREQUENCY_END", None, None)]
+    f = hella.Filterbank(write("tab.fil", tab, bytes(32)), 32)
+    assert f.header.nfreq == 32 and (f.header.fch1, f.header.foff) == (0.0, 0.0)
+    assert list(f.header.frequency_table[:32]) == freqs
+    with pytest.raises(hella.HellaError):  # more entries than the table holds
+        hella.Filterbank(write("bigtab.fil", [("fchannel", "d", 400.0)] * 4097 + base), 32)
     t = tmp_path / "trunc.fil"
     t.write_bytes(write("full.fil", base).read_bytes()[:30])
     with pytest.raises(hella.HellaError):

@@ -40,6 +40,37 @@ def test_noalloc_matches_execute_adv_twice(hella):
     plan.close()
 
 
+def test_noalloc_leaves_device_memory_untouched(hella):
+    """The property that defines the entry point: after a first call (which
+    resolves the scratch address and loads the kernels), more calls with
+    other sample counts, synchronous and HDD_ASYNC, change the free device
+    memory by nothing."""
+    torch = pytest.importorskip("torch")
+    L = hella.lib()
+    plan = _plan(hella)
+    plan.set_stream(torch.cuda.current_stream().cuda_stream)
+    sizes = [plan.max_delay + n for n in (3000, 1000, 4099, 257)]
+    rng = np.random.default_rng(7)
+    xs = [torch.from_numpy(rng.integers(0, 256, (n, plan.nchans), dtype=np.uint8)).cuda() for n in sizes]
+    outs = [torch.zeros((plan.dm_count, n - plan.max_delay), dtype=torch.float32, device="cuda") for n in sizes]
+
+    def call(i, flags):
+        n = sizes[i]
+        return L.hdd_execute_noalloc(plan.h, n, xs[i].data_ptr(), 8, plan.nchans, outs[i].data_ptr(), 32,
+                                     (n - plan.max_delay) * 4, flags)
+
+    assert call(0, hella.HDD_DEVICE_POINTERS) == 0  # warm-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for i in (1, 2, 3, 0):
+        assert call(i, hella.HDD_DEVICE_POINTERS | hella.HDD_ASYNC) == 0
+        assert call(i, hella.HDD_DEVICE_POINTERS) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    plan.close()
+
+
 def test_noalloc_rejects_oversize_and_host_pointers(hella):
     L = hella.lib()
     plan = _plan(hella, nchan=2048, dm_max=500.0)
@@ -52,4 +83,8 @@ def test_noalloc_rejects_oversize_and_host_pointers(hella):
     rc = L.hdd_execute_noalloc(plan.h, plan.max_delay + 10, buf.ctypes.data, 8, plan.nchans, buf.ctypes.data,
                                32, 40, hella.HDD_HOST_POINTERS)
     assert hella.HDD_ERRORS[rc] == "HDD_INVALID_FLAG_COMBINATION"
+    # the transpose's grid limit is not a scratch limit: the code hdd_execute_guru gives it
+    rc = L.hdd_execute_noalloc(plan.h, 65535 * 32 + 1, buf.ctypes.data, 8, plan.nchans, buf.ctypes.data,
+                               32, 4 * (65535 * 32 + 1), hella.HDD_DEVICE_POINTERS)
+    assert hella.HDD_ERRORS[rc] == "HDD_UNKNOWN_ERROR"
     plan.close()

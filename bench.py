@@ -16,7 +16,7 @@ the candidates inside the timed region, with per-gulp p50/p99 latency.
 
 --impl reference: the reference path's CPU implementation (the oracle
 port; the reference itself has no CPU path and does not build here) on the
-host cores, one bounded sample per step.
+host cores, one whole searched gulp per step.
 """
 from __future__ import annotations
 
@@ -55,6 +55,9 @@ def args_():
                     help="full: the single-beam headline workload; batched: all beams of the "
                          "multi-beam configuration per step")
     ap.add_argument("--beams", type=int, default=256, help="beams of the batched workload")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the multi-beam leg that the full workload's line carries as `batched`")
+    ap.add_argument("--batched-steps", type=int, default=8, help="timed gulps of that leg")
     ap.add_argument("--seconds", type=float, default=600.0, help="sky seconds of the stream workload")
     ap.add_argument("--cutouts", type=int, default=4096, help="cutouts of the refine workload")
     ap.add_argument("--nchan", type=int, default=0,
@@ -107,6 +110,8 @@ class Clocks:
 
 # ------------------------------------------------------------- workload
 
+DATA_FULL = "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)"
+DATA_PLAIN = "synthetic (seeded noise, 4 RFI channels, 3 broadband impulses, one DM-300 burst)"
 PLAIN_WORKLOAD = ("plain single beam: 512 ch 375-468.75 MHz, tsamp 1.048576 ms, gulp 16384, DM 0-500 tol 1.25 "
                   "(0.5 ms pulse), widths 1-32, 7 sigma, one DM-300 burst")
 
@@ -139,46 +144,50 @@ def workload(rank: int, ngulps: int = 3, which: str = "full", nchan: int = 0, dm
     return params, sky, gulps
 
 
-def cpu_sample(params, gulp, dm_rows: int = 128):
-    """The oracle on one bounded sample of a gulp: the full flagger, then
-    dedispersion + smoothing + standardisation + peaks over `dm_rows` DM
-    trials of the middle of the list; the search part is scaled to all
-    trials.  Returns (seconds for a whole gulp, threads, description)."""
+def oracle_gulps(params, gulps, nsearch: int, nwarm: int = 0):
+    """The oracle pipeline (the reference path restated on the CPU: flag,
+    normalise, requantise, dedisperse every trial, smooth, standardise, find
+    peaks, with the ring carried across gulps) on `nsearch` whole searched
+    gulps, all host threads.  The ring is filled first and `nwarm` gulps are
+    flagged, both untimed; `gulps` are reused in turn.  Returns (seconds per
+    searched gulp, threads, description)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
-    f32 = lambda v: float(np.float32(v))
-    nch, G = params["nchan"], params["gulp"]
-    dms = oracle.dm_list(0.0, f32(params["dm_max"]), f32(params["ti_us"]), f32(params["dm_tol"]), nch,
-                         f32(params["plan_dt"]), f32(params["f0_mhz"]), f32(params["df_mhz"]))
-    delays = oracle.dm_delays(dms, oracle.delay_table(nch, f32(params["plan_dt"]), f32(params["f0_mhz"]),
-                                                      f32(params["df_mhz"])))
-    md = int(delays[-1, -1])
-    wmax = params["width_max"]
-    ntd = G + wmax
-    a = len(dms) // 2 - dm_rows // 2
-    t0 = time.perf_counter()
-    flagged, _, _ = oracle.flag_beam(gulp)
-    t1 = time.perf_counter()
-    reps = (md + ntd + G - 1) // G + 1
-    window = np.ascontiguousarray(np.concatenate([flagged] * reps)[: md + ntd])
-    t2 = time.perf_counter()
-    dd = oracle.dedisperse(window, delays[a:a + dm_rows], nout=ntd)
-    nbox, sm = 0, params["width_min"]
-    while sm < wmax:
-        nbox, sm = nbox + 1, sm * 2
-    boxes = np.zeros((nbox, dm_rows - 2, G), np.float32)
-    m, s = np.zeros(nbox, np.float32), np.zeros(nbox, np.float32)
-    L = oracle.lib()
-    L.ho_smooth_normalise(dd.ctypes.data, dm_rows, ntd, ntd, params["width_min"], wmax, 1, G, boxes.ctypes.data,
-                          m.ctypes.data, s.ctypes.data)
-    cands = np.zeros(10000, oracle.CAND_DTYPE)
-    L.ho_find_peaks(boxes.ctypes.data, nbox, dm_rows, G, params["snr"], 0, 10000, cands.ctypes.data, None)
-    t3 = time.perf_counter()
-    per_gulp = (t1 - t0) + (t3 - t2) * len(dms) / dm_rows
-    desc = (f"oracle port: flagger on a full {nch}x{G} gulp ({t1 - t0:.1f} s) + search over {dm_rows} of "
-            f"{len(dms)} DM trials ({t3 - t2:.1f} s), search scaled linearly to all trials")
-    return per_gulp, os.cpu_count(), desc
+    oracle.set_threads(0)
+    pl = oracle.Pipeline.from_params(params, nbeam=1)
+    gi = 0
+    for _ in range(pl.min_gulp):
+        pl.gulp_step(gulps[gi % len(gulps)][None])
+        gi += 1
+    for _ in range(nwarm):
+        oracle.flag_beam(gulps[gi % len(gulps)])
+    times = []
+    for _ in range(nsearch):
+        t0 = time.perf_counter()
+        _, searched = pl.gulp_step(gulps[gi % len(gulps)][None])
+        times.append(time.perf_counter() - t0)
+        assert searched
+        gi += 1
+    pl.close()
+    cores = os.cpu_count()
+    desc = (f"oracle port on {cores} threads ({cpu_model()}): {nsearch} whole searched gulp(s) of "
+            f"{params['nchan']} ch x {params['gulp']} samples, all {pl.ndms} DM trials, timed end to end "
+            f"({np.mean(times):.1f} s each)")
+    return times, cores, desc
+
+
+def cpu_model() -> str:
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                return v.strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
 
 
 # ---------------------------------------------------------------- main
@@ -348,8 +357,7 @@ def main():
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8",
-        "data": ("synthetic (seeded noise, 4 RFI channels, 3 broadband impulses, one DM-300 burst)"
-                 if a.workload == "plain" else "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)"),
+        "data": DATA_PLAIN if a.workload == "plain" else DATA_FULL,
         "config": {"workload": PLAIN_WORKLOAD if a.workload == "plain" else
                    WORKLOAD.replace("2048 ch", f"{nch} ch").replace("DM 0-2000", f"DM 0-{params['dm_max']:g}"),
                    "nchan": nch, "gulp": G,
@@ -372,11 +380,22 @@ def main():
         "clocks": clk,
         "candidates_per_gulp": float(np.mean(ncand)),
     }
-    if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        per, cores, desc = cpu_sample(params, gulps[0])
-        line["cpu_baseline"] = {"value": round(gulp_s / per, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": desc}
     s.close()
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        times, cores, desc = oracle_gulps(params, gulps, 1)
+        line["cpu_baseline"] = {"value": round(gulp_s / times[0], 4), "unit": UNIT, "cores": cores,
+                                "kind": "port", "sample": desc}
+    if a.workload == "full" and not (a.nchan or a.dm_max) and not a.no_batched:
+        # the multi-beam configuration under the same clock: 256 beams x 1024 ch, one graph per gulp
+        del dev, host
+        torch.cuda.empty_cache()
+        bl = batched_leg(a, rank, world, local, dist, a.batched_steps, min(a.warmup, 3),
+                         cpu=not a.no_cpu_baseline)
+        line["batched"] = {k: bl[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
+                                              "gpu_launches", "roofline", "clocks", "candidates_per_gulp")
+                           if k in bl}
+        if "cpu_baseline" in bl:
+            line["batched"]["cpu_baseline"] = bl["cpu_baseline"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -395,6 +414,17 @@ def batched_sample_params(params, ceiling):
 
 def main_batched(a, rank, world, local, dist):
     """All beams of the multi-beam configuration per step (hella_batch_*)."""
+    line = batched_leg(a, rank, world, local, dist, a.steps, a.warmup, cpu=not a.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool = True) -> dict:
+    """Times `steps` gulps of every beam of the multi-beam configuration
+    (one CUDA graph per gulp) device-resident, then end to end from pinned
+    host memory with two gulps in flight; returns the JSON line's fields."""
     import torch
     import hella_gb300 as hg
     import synth
@@ -423,7 +453,7 @@ def main_batched(a, rank, world, local, dist):
     tune = bt.get_tuning().as_dict()
 
     gi = 0
-    for _ in range(max(i.min_gulp for i in infos) + a.warmup):
+    for _ in range(max(i.min_gulp for i in infos) + warmup):
         bt.process_gulp(dev[gi % ngen].data_ptr(), on_device=True)
         gi += 1
 
@@ -433,12 +463,12 @@ def main_batched(a, rank, world, local, dist):
     if dist:
         dist.barrier()
     dev_ms, ncand = [], []
-    for _ in range(a.steps):
+    for _ in range(steps):
         got, counts, _ = bt.process_gulp(dev[gi % ngen].data_ptr(), on_device=True)
         dev_ms.append(bt.last_gulp_ms())
         ncand.append(len(got))
         gi += 1
-    value, slowest = job_rate(dist, a.steps * NB * gulp_s, float(np.sum(dev_ms)) / 1e3)
+    value, slowest = job_rate(dist, steps * NB * gulp_s, float(np.sum(dev_ms)) / 1e3)
     ms = slowest * 1e3
 
     # ---------------- end to end from pinned host memory: two gulps in flight, the upload of
@@ -455,8 +485,8 @@ def main_batched(a, rank, world, local, dist):
     w0 = time.perf_counter()
     bt.submit(host[gi % ngen].data_ptr())
     gi += 1
-    for k in range(a.steps):
-        if k + 1 < a.steps:
+    for k in range(steps):
+        if k + 1 < steps:
             bt.submit(host[gi % ngen].data_ptr())
             gi += 1
         got, counts, _, l_ms, d_ms = bt.poll()
@@ -466,7 +496,7 @@ def main_batched(a, rank, world, local, dist):
     e2e_s = time.perf_counter() - w0
     # gulp to gulp once the pipeline is full (the first gulp's upload is not overlapped)
     steady = np.diff(polled) * 1e3 if len(polled) > 1 else np.asarray([e2e_s * 1e3])
-    e2e, e2e_s = job_rate(dist, a.steps * NB * gulp_s, e2e_s)
+    e2e, e2e_s = job_rate(dist, steps * NB * gulp_s, e2e_s)
     clk = clocks.stop()
 
     # ---------------- dedispersion roofline: the all-beam launch alone
@@ -480,8 +510,8 @@ def main_batched(a, rank, world, local, dist):
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
             "ms_per_launch": round(dd_ms, 3)}
     line = {
-        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(ms / steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded noise, RFI channels, 0-3 dispersed bursts per beam; drawn on the GPU)",
         "config": {"workload": BATCH_WORKLOAD.format(nb=NB), "beams": NB, "nchan": nch, "gulp": G,
@@ -497,24 +527,25 @@ def main_batched(a, rank, world, local, dist):
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
                 "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1),
                 "device_ms_p50": round(float(np.percentile(e2e_dev, 50)), 2),
-                "period_ms": round(1e3 * e2e_s / a.steps, 2),
+                "period_ms": round(1e3 * e2e_s / steps, 2),
                 "first_gulp_ms": round(1e3 * (polled[0] - w0), 2),
                 "steady_period_ms_p50": round(float(np.percentile(steady, 50)), 2)},
-        "gpu_launches": int(a.steps * 2 * bt.graph_kernels()),
+        "gpu_launches": int(steps * 2 * bt.graph_kernels()),
         "roofline": roof,
         "clocks": clk,
         "candidates_per_gulp": float(np.mean(ncand)),
     }
-    if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        g0 = skies[0].gulp(infos[0].min_gulp, G)
-        per, cores, desc = cpu_sample(batched_sample_params(params, ceilings[0]), g0, dm_rows=64)
-        line["cpu_baseline"] = {"value": round(gulp_s / per, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "beam 0 of the batch: " + desc}
+    if rank == 0 and world == 1 and cpu:
+        gl = [skies[0].gulp(g, G) for g in range(infos[0].min_gulp + 1)]
+        p0 = batched_sample_params(params, ceilings[0])
+        p0["nbeam"] = 1
+        times, cores, desc = oracle_gulps(p0, gl, 1)
+        line["cpu_baseline"] = {"value": round(gulp_s / times[0], 4), "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "beam 0 of the batch (its own DM ceiling), one beam per wall second: "
+                                          + desc + "; beams are independent, so the batch's CPU time scales "
+                                                   f"with the {NB} beams"}
     bt.close()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    return line
 
 
 STREAM_WORKLOAD = ("streaming serving loop: 64 beam requests x 1024 ch, tsamp 1.048576 ms, gulps of 8192 "
@@ -743,23 +774,20 @@ def main_refine(a, rank, world, local, dist):
 
 
 def run_reference(a, rank, world):
-    """The reference path's CPU implementation on the host cores."""
+    """The reference path's CPU implementation on the host cores: each step
+    one whole searched gulp of the workload through the oracle pipeline (no
+    extrapolation); the warm-up fills the ring and flags `warmup` gulps."""
     if rank != 0:
         return
     which = a.workload if a.workload in ("full", "plain") else "full"
-    params, sky, gulps = workload(0, ngulps=1, which=which)
+    params, sky, gulps = workload(0, ngulps=3, which=which)
     gulp_s = params["gulp"] * params["tsamp"]
-    for _ in range(a.warmup):
-        cpu_sample(params, gulps[0], dm_rows=32)
-    times, desc, cores = [], "", os.cpu_count()
-    for _ in range(a.steps):
-        per, cores, desc = cpu_sample(params, gulps[0])
-        times.append(per)
+    times, cores, desc = oracle_gulps(params, gulps, a.steps, nwarm=a.warmup)
     per = float(np.mean(times))
     v = gulp_s / per
     line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded noise, RFI, spikes, 8 dispersed bursts)",
+            "vs_baseline": None, "dtype": "u8", "data": DATA_PLAIN if which == "plain" else DATA_FULL,
             "config": {"workload": PLAIN_WORKLOAD if which == "plain" else WORKLOAD}, "impl": "reference",
             "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -551,14 +551,42 @@ void ho_smooth_plane(const float *dd, int ndms, int ntime_dd, size_t dd_stride,
   free(k3);
 }
 
-int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
-                        size_t dd_stride, int wmin, int wmax, int anchor,
-                        int ntime_out, float *boxes, float *mean, float *std) {
+void ho_smooth_plane_direct(const float *dd, int ndms, int ntime_dd,
+                            size_t dd_stride, int sm, int wmax, int shift,
+                            float *out, int ntime_out, size_t out_stride) {
+  float *k3 = (float *)malloc(sizeof(float) * 3 * (2 * sm + 1));
+  int n = ho_smooth_taps(sm, k3);
+#pragma omp parallel for schedule(static) num_threads(nthreads())
+  for (int r = 0; r < ndms - 2; ++r) {
+    float *o = out + (size_t)r * out_stride;
+    for (int j = 0; j < ntime_out; ++j) {
+      /* output column x = j + wmax/2 of dd row r+1 */
+      int x = j + wmax / 2;
+      float acc = 0.f;
+      for (int kr = 0; kr < 3; ++kr) {
+        const float *row = dd + (size_t)(r + 2 - kr) * dd_stride;
+        for (int i = 0; i < n; ++i) {
+          int xx = x + (2 * sm - shift) - i; /* column i on input x - i (anchor 1) */
+          xx = xx < 0 ? 0 : (xx >= ntime_dd ? ntime_dd - 1 : xx);
+          acc = fmaf(k3[kr * n + i], row[xx], acc);
+        }
+      }
+      o[j] = acc;
+    }
+  }
+  free(k3);
+}
+
+int ho_smooth_normalise_arith(const float *dd, int ndms, int ntime_dd,
+                              size_t dd_stride, int wmin, int wmax, int anchor,
+                              int ntime_out, float *boxes, float *mean,
+                              float *std, int direct) {
   int nb = 0;
   size_t plane = (size_t)(ndms - 2) * ntime_out;
   for (int sm = wmin; sm < wmax; sm *= 2, ++nb)
-    ho_smooth_plane(dd, ndms, ntime_dd, dd_stride, sm, wmax, anchor ? 2 * sm : 0,
-                    boxes + nb * plane, ntime_out, (size_t)ntime_out);
+    (direct ? ho_smooth_plane_direct : ho_smooth_plane)(
+        dd, ndms, ntime_dd, dd_stride, sm, wmax, anchor ? 2 * sm : 0,
+        boxes + nb * plane, ntime_out, (size_t)ntime_out);
   for (int b = 0; b < nb; ++b) {
     float *x = boxes + b * plane;
     float mu = 0.f;
@@ -575,6 +603,13 @@ int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
     }
   }
   return nb;
+}
+
+int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
+                        size_t dd_stride, int wmin, int wmax, int anchor,
+                        int ntime_out, float *boxes, float *mean, float *std) {
+  return ho_smooth_normalise_arith(dd, ndms, ntime_dd, dd_stride, wmin, wmax,
+                                   anchor, ntime_out, boxes, mean, std, 0);
 }
 
 /* ----------------------------------------------------------------- peaks */

@@ -146,6 +146,13 @@ void ho_smooth_plane(const float *dd, int ndms, int ntime_dd, size_t dd_stride,
                      int sm, int wmax, int shift, float *out, int ntime_out,
                      size_t out_stride);
 
+/* ho_smooth_plane with the 3 x (2sm+1) kernel applied directly (every tap
+ * of every row: kernel rows outer, columns inner, one fmaf per tap) instead
+ * of the factored form; the arithmetic of the emulator's NPP stand-in. */
+void ho_smooth_plane_direct(const float *dd, int ndms, int ntime_dd,
+                            size_t dd_stride, int sm, int wmax, int shift,
+                            float *out, int ntime_out, size_t out_stride);
+
 /* smooth(p, scale=1): every width sm = wmin*2^k < wmax, then per-width
  * (x + (-mean)) * (1/std) unless std <= 0.  boxes: [nbox][ndms-2][ntime_out]
  * packed.  mean/std: [nbox] (pre-normalisation statistics).  anchor 1: the
@@ -155,6 +162,11 @@ void ho_smooth_plane(const float *dd, int ndms, int ntime_dd, size_t dd_stride,
 int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
                         size_t dd_stride, int wmin, int wmax, int anchor,
                         int ntime_out, float *boxes, float *mean, float *std);
+/* As ho_smooth_normalise; direct != 0 uses ho_smooth_plane_direct. */
+int ho_smooth_normalise_arith(const float *dd, int ndms, int ntime_dd,
+                              size_t dd_stride, int wmin, int wmax, int anchor,
+                              int ntime_out, float *boxes, float *mean,
+                              float *std, int direct);
 
 /* ----------------------------------------------------------------- peaks */
 typedef struct {

@@ -217,16 +217,17 @@ def box_filter(plane: np.ndarray, xw: int, yw: int, k: float) -> np.ndarray:
     return out
 
 
-def smooth_plane(dd: np.ndarray, sm: int, wmax: int, ntime_out: int, anchor: int = 1) -> np.ndarray:
-    """One width's pre-normalisation plane [ndms-2][ntime_out] (ho_smooth_plane)."""
+def smooth_plane(dd: np.ndarray, sm: int, wmax: int, ntime_out: int, anchor: int = 1,
+                 direct: bool = False) -> np.ndarray:
+    """One width's pre-normalisation plane [ndms-2][ntime_out]: the factored
+    form (ho_smooth_plane), or the kernel tap by tap (ho_smooth_plane_direct)."""
     dd = np.ascontiguousarray(dd, np.float32)
     ndms, ntd = dd.shape
     out = np.zeros((ndms - 2, ntime_out), np.float32)
     L = lib()
-    L.ho_smooth_plane.argtypes = [_VP, C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int, _VP, C.c_int,
-                                  C.c_size_t]
-    L.ho_smooth_plane(dd.ctypes.data, ndms, ntd, ntd, sm, wmax, 2 * sm if anchor else 0, out.ctypes.data,
-                      ntime_out, ntime_out)
+    f = L.ho_smooth_plane_direct if direct else L.ho_smooth_plane
+    f.argtypes = [_VP, C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int, _VP, C.c_int, C.c_size_t]
+    f(dd.ctypes.data, ndms, ntd, ntd, sm, wmax, 2 * sm if anchor else 0, out.ctypes.data, ntime_out, ntime_out)
     return out
 
 
@@ -253,6 +254,18 @@ class Pipeline:
         self.L.ho_pipeline_info(self.h, *[C.byref(x) for x in v])
         self.ntime, self.ndms, self.max_delay, self.ntime_dd, self.nbox, self.min_gulp = [x.value for x in v]
         self.nchan, self.nbeam, self.gulp, self.max_giants = nchan, nbeam, gulp, max_giants
+
+    @classmethod
+    def from_params(cls, params: dict, **over) -> "Pipeline":
+        """From the product's parameter names (hella_params fields)."""
+        p = dict(params)
+        p.update(over)
+        return cls(nchan=p["nchan"], nbeam=p.get("nbeam", 1), gulp=p["gulp"], tsamp=p["tsamp"],
+                   plan_dt=p["plan_dt"], f0=p["f0_mhz"], df=p["df_mhz"], dm_min=p["dm_min"], dm_max=p["dm_max"],
+                   dm_tol=p["dm_tol"], ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
+                   max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
+                   spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15), flag1=p.get("flag1", -1),
+                   flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()))
 
     def close(self):
         if getattr(self, "h", None):
@@ -328,7 +341,10 @@ def median_filter(x: np.ndarray, window: int):
     return out, float(mn)
 
 
-def smooth_normalise(dd: np.ndarray, wmin: int, wmax: int, ntime_out: int, anchor: int = 1):
+def smooth_normalise(dd: np.ndarray, wmin: int, wmax: int, ntime_out: int, anchor: int = 1, direct: bool = False):
+    """smooth(p, 1): (standardised planes, means, stds).  direct: the kernel
+    applied tap by tap (the emulator's NPP stand-in) instead of the factored
+    form the GPU computes."""
     dd = np.ascontiguousarray(dd, np.float32)
     ndms, ntd = dd.shape
     nbox, sm = 0, wmin
@@ -336,8 +352,11 @@ def smooth_normalise(dd: np.ndarray, wmin: int, wmax: int, ntime_out: int, ancho
         nbox, sm = nbox + 1, sm * 2
     boxes = np.zeros((nbox, ndms - 2, ntime_out), np.float32)
     mean, std = np.zeros(nbox, np.float32), np.zeros(nbox, np.float32)
-    lib().ho_smooth_normalise(dd.ctypes.data, ndms, ntd, ntd, wmin, wmax, anchor, ntime_out, boxes.ctypes.data,
-                              mean.ctypes.data, std.ctypes.data)
+    L = lib()
+    L.ho_smooth_normalise_arith.argtypes = [_VP, C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            _VP, _VP, _VP, C.c_int]
+    L.ho_smooth_normalise_arith(dd.ctypes.data, ndms, ntd, ntd, wmin, wmax, anchor, ntime_out, boxes.ctypes.data,
+                                mean.ctypes.data, std.ctypes.data, int(direct))
     return boxes, mean, std
 
 

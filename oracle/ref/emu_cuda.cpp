@@ -164,11 +164,12 @@ const char *cudaGetErrorString(cudaError_t) { return "emulated"; }
 }  // extern "C"
 
 // ------------------------------------------------------------ NPP filters
-// The reference's two NPP filters, with the index placement measured on a
-// GB300 (tap i of kernel column ax-relative applied to input x + ax - i,
-// likewise rows) and replicate borders.  Summation order is the oracle's
-// (NPP's own is not observable), so these pin everything around the filter
-// rather than NPP's internal rounding.
+// Stand-ins for the reference's two NPP filters, with the index placement
+// measured on a GB300 (kernel column i applied to input x + ax - i, likewise
+// rows) and replicate borders.  Their summation order is a plain direct sum
+// defined here (NPP's own is closed), so the fixtures pin everything around
+// the filters; the GPU tests measure this library's filters against NPP
+// itself.
 std::vector<float> g_taps_seen;  // every smoothing kernel passed, in order
 
 static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -198,23 +199,21 @@ extern "C" NppStatus nppiFilterBorder32f_16f_C1R(const Npp16f *pSrc, Npp32s nSrc
 extern "C" NppStatus nppiFilterBorder_32f_C1R(const Npp32f *pSrc, Npp32s nSrcStep, NppiSize oSrcSize, NppiPoint,
                                               Npp32f *pDst, Npp32s nDstStep, NppiSize oSizeROI,
                                               const Npp32f *pKernel, NppiSize ks, NppiPoint anc, NppiBorderType) {
-  // the smoothing kernel: rows weighted 0.3/1/0.3 around the output row,
-  // evaluated in the oracle's factored form (middle-row taps)
+  // the whole kernel it is given (every row and column), the same placement
+  // and order as the fp16 filter above: tap (j, i) on input (y + ay - j,
+  // x + ax - i), kernel rows outer, columns inner, one fmaf per tap
   g_taps_seen.insert(g_taps_seen.end(), pKernel, pKernel + (size_t)ks.width * ks.height);
-  const int W = oSrcSize.width, H = oSrcSize.height, n = ks.width;
-  const float *mid = pKernel + n;  // row 1
-  std::vector<float> yv(W);
+  const int W = oSrcSize.width, H = oSrcSize.height;
   for (int y = 0; y < oSizeROI.height; ++y) {
-    const float *a = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) +
-                                                     (size_t)clampi(y - 1, 0, H - 1) * nSrcStep);
-    const float *b = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) + (size_t)y * nSrcStep);
-    const float *c = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) +
-                                                     (size_t)clampi(y + 1, 0, H - 1) * nSrcStep);
-    for (int x = 0; x < W; ++x) yv[x] = std::fmaf(0.3f, a[x] + c[x], b[x]);
     float *o = reinterpret_cast<float *>(reinterpret_cast<char *>(pDst) + (size_t)y * nDstStep);
     for (int x = 0; x < oSizeROI.width; ++x) {
       float acc = 0.f;
-      for (int k = 0; k < n; ++k) acc = std::fmaf(mid[k], yv[clampi(x + anc.x - (n - 1) + k, 0, W - 1)], acc);
+      for (int j = 0; j < ks.height; ++j) {
+        const float *row = reinterpret_cast<const float *>(reinterpret_cast<const char *>(pSrc) +
+                                                           (size_t)clampi(y + anc.y - j, 0, H - 1) * nSrcStep);
+        for (int i = 0; i < ks.width; ++i)
+          acc = std::fmaf(pKernel[j * ks.width + i], row[clampi(x + anc.x - i, 0, W - 1)], acc);
+      }
       o[x] = acc;
     }
   }

@@ -4,15 +4,7 @@ import numpy as np
 
 
 def oracle_pipeline(oracle, params: dict, **over):
-    p = dict(params)
-    p.update(over)
-    return oracle.Pipeline(
-        nchan=p["nchan"], nbeam=p.get("nbeam", 1), gulp=p["gulp"], tsamp=p["tsamp"], plan_dt=p["plan_dt"],
-        f0=p["f0_mhz"], df=p["df_mhz"], dm_min=p["dm_min"], dm_max=p["dm_max"], dm_tol=p["dm_tol"],
-        ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
-        max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
-        spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15), flag1=p.get("flag1", -1),
-        flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()))
+    return oracle.Pipeline.from_params(params, **over)
 
 
 def small_params(**over):

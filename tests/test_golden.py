@@ -5,7 +5,14 @@ tests/golden/reference_fixtures.json holds what the reference's flagger
 and <half>, median_filter, smooth (taps and standardised planes) and
 find_peaks produced on seeded inputs (tests/golden/cases.py), run on the
 CPU by tests/golden/make_golden.py.  The oracle must reproduce every byte
-and every float bit."""
+and every float bit.
+
+The reference's smoothing FIR is NPP's (closed); the fixtures ran it through
+a stand-in that applies the 3 x (2sm+1) kernel tap by tap.  The oracle's
+direct form reproduces that bit for bit (taps, anchor, crop, statistics,
+normalisation and peak order are pinned); the factored form the GPU
+computes is held to it within the tolerance below, and to NPP itself by
+tests/test_gpu_npp.py."""
 import json
 from pathlib import Path
 
@@ -60,9 +67,48 @@ def test_smooth_and_peaks_match_reference(oracle, i):
     nbox = len(want["taps"]) and sum(1 for b in range(16) if (c["wmin"] << b) < c["wmax"])
     taps = np.concatenate([oracle.smooth_taps(c["wmin"] << b).ravel() for b in range(nbox)])
     assert cases.bits(taps) == want["taps"]
-    boxes, _, _ = oracle.smooth_normalise(cases.smooth_input(c), c["wmin"], c["wmax"], c["ntime_out"], anchor=1)
+    boxes, _, _ = oracle.smooth_normalise(cases.smooth_input(c), c["wmin"], c["wmax"], c["ntime_out"], anchor=1,
+                                          direct=True)
     assert cases.sha(boxes) == want["boxes_sha"]
     cands, _ = oracle.find_peaks(boxes, c["snr"])
     assert len(cands) == want["npeaks"] > 0
     arr = np.stack([cands["snr"].view(np.int32), cands["width"], cands["dm_idx"], cands["samp"]])
     assert cases.sha(arr.astype(np.int32)) == want["peaks_sha"]
+
+
+# Relative tolerance of smoothed (pre-normalisation) planes against the
+# reference's filter.  Normalisation subtracts a mean that is large against
+# the std, so a normalised value carries it as RTOL * (|x| + |mean|) / std.
+RTOL = 1e-5
+
+
+@pytest.mark.parametrize("i", range(len(cases.SMOOTH_CASES)))
+def test_factored_smoothing_against_direct_kernel(oracle, i):
+    """The factored FIR (0.3 * (row above + row below) + row, then the
+    middle-row taps) against the kernel applied tap by tap: planes within
+    RTOL, the same candidates (width, DM, sample) in the same order, S/N
+    within the tolerance carried through the normalisation."""
+    c = cases.SMOOTH_CASES[i]
+    dd = cases.smooth_input(c)
+    worst = 0.0
+    for b in range(16):
+        sm = c["wmin"] << b
+        if sm >= c["wmax"]:
+            break
+        f = oracle.smooth_plane(dd, sm, c["wmax"], c["ntime_out"])
+        d = oracle.smooth_plane(dd, sm, c["wmax"], c["ntime_out"], direct=True)
+        rel = float(np.max(np.abs(f.astype(np.float64) - d) / np.abs(d)))
+        worst = max(worst, rel)
+        assert rel <= RTOL, (sm, rel)
+    assert worst > 0  # the two forms round differently: the check is not vacuous
+    bf, mf, sf = oracle.smooth_normalise(dd, c["wmin"], c["wmax"], c["ntime_out"])
+    bd, md, sd = oracle.smooth_normalise(dd, c["wmin"], c["wmax"], c["ntime_out"], direct=True)
+    # a plane error of RTOL * |x| moves the mean by as much and the std by RTOL * (|mean| + std) at most
+    assert np.all(np.abs(mf - md) <= RTOL * np.abs(md))
+    assert np.all(np.abs(sf - sd) <= RTOL * (np.abs(md) + sd))
+    cf, _ = oracle.find_peaks(bf, c["snr"])
+    cd, _ = oracle.find_peaks(bd, c["snr"])
+    for k in ("width", "dm_idx", "samp"):
+        assert np.array_equal(cf[k], cd[k]), k
+    tol = RTOL * (np.abs(cd["snr"]) * sd[cd["width"]] + 2 * np.abs(md[cd["width"]])) / sd[cd["width"]]
+    assert np.all(np.abs(cf["snr"] - cd["snr"]) <= tol)

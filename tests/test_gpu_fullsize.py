@@ -1,12 +1,16 @@
-"""The full single-beam workload (2048 channels, gulp 65536, DM 0-2000 at
-tolerance 1.25, 2501 trials) at full size: the flagger's output bytes of a
-whole gulp and 48 sampled dedispersed trials of the first searched window
-bit-exact against the oracle, and the candidate lists of two contexts fed the
-same gulps identical (determinism)."""
+"""The benchmarked configurations at full size.  The full single beam (2048
+channels, gulp 65536, DM 0-2000 at tolerance 1.25, 2501 trials): the
+flagger's output bytes of a whole gulp and 48 sampled dedispersed trials of
+the first searched window bit-exact against the oracle, the first searched
+gulp's candidate list bit-exact against the oracle pipeline with the
+injected bursts recovered, and the candidate lists of two contexts fed the
+same gulps identical (determinism).  The multi-beam configuration (256
+beams): sampled beams equal to independent single-beam runs."""
 import numpy as np
 import pytest
 
 import synth
+from helpers import cands_equal, oracle_pipeline
 
 pytestmark = pytest.mark.gpu
 
@@ -53,3 +57,87 @@ def test_full_beam_deterministic(hella):
         assert np.array_equal(ca, cb)
         counts.append(len(ca))
     assert counts[-1] > 0
+
+
+DM_TOL = 2.0  # scripts/verify_injection_fil.py:30-40: loudest candidate within 2 pc/cm^3 of the injected DM
+
+
+def test_full_beam_candidates_and_injection_recovery(hella, oracle):
+    """The benchmarked workload end to end: the first searched gulp's
+    candidate list bit-exact against the oracle pipeline, and every injected
+    burst of injected S/N >= 12 recovered by the reference's criterion,
+    applied per burst: the loudest candidate within wmax samples of its
+    arrival (DM above 20, clear of the broadband spikes) lies within DM_TOL
+    of the injected DM.  (The one burst below that, S/N 8.5 over FWHM 5.2 ms,
+    stays under the 7-sigma threshold in the oracle as well.)"""
+    params, sky = synth.config_full(seed=2)
+    G, wmax = params["gulp"], params["width_max"]
+    s = hella.Search(hella.default_params(**params))
+    oracle.set_threads(0)
+    pl = oracle_pipeline(oracle, params)
+    for g in range(pl.min_gulp + 1):
+        x = sky.gulp(g, G)[None]
+        got, searched = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert searched == so
+        assert cands_equal(got, want), (g, len(got), len(want))
+    assert searched and len(got) > 0
+    dms = s.dm_list()
+    _, ws, _ = synth.first_window(sky, G, params["dm_max"], wmax)
+    found = 0
+    for b in sky.bursts:
+        snr_inj = b.amp / synth.snr_amp(1.0, 16.0, params["nchan"], b.fwhm_ms, params["tsamp"])
+        near = got[(np.abs(got["samp"] + wmax // 2 - (b.t0 - ws)) <= wmax) & (dms[got["dm_idx"]] > 20.0)]
+        if snr_inj < 12.0:
+            continue
+        assert len(near), (b.dm, snr_inj)
+        best = near[np.argmax(near["snr"])]
+        assert abs(dms[best["dm_idx"]] - b.dm) < DM_TOL, (b.dm, float(dms[best["dm_idx"]]))
+        found += 1
+    assert found >= 7
+
+
+def test_batched_config_full_size_sampled_beams(hella):
+    """The multi-beam configuration at full size (256 beams x 1024 channels,
+    gulp 32768, DM ceilings U[1000,2000], killmasks 0-10 %), gulps drawn on
+    the GPU: sampled beams -- the first, the one killing most channels, the
+    highest and the lowest DM ceiling -- equal, bit for bit, a single-beam
+    context with that beam's ceiling and killmask fed the same gulps
+    (candidates and dedispersed plane)."""
+    import torch
+
+    params, ceilings, kill, skies = synth.config_batched(nbeam=256, seed=3)
+    NB, G = params["nbeam"], params["gulp"]
+    frac = 1.0 - kill.mean(1)
+    sample = sorted({0, int(np.argmax(frac)), int(np.argmax(ceilings)), int(np.argmin(ceilings))})
+    assert frac[sample].max() > 0.08
+    singles = {}
+    for b in sample:
+        p = dict(params, dm_max=float(ceilings[b]), beam0=b, nbeam=1)
+        singles[b] = hella.Search(hella.default_params(**p))
+        singles[b].set_killmask(kill[b])
+    ngulp = max(s.info.min_gulp for s in singles.values()) + 1
+    gulps = []
+    for g in range(ngulp):
+        t = torch.empty((NB, G, params["nchan"]), dtype=torch.uint8, device="cuda")
+        for b in range(NB):
+            synth.gulp_device(skies[b], g, G, out=t[b])
+        gulps.append(t)
+    torch.cuda.synchronize()
+    bt = hella.Batch(hella.default_params(**params), dm_max=ceilings, killmask=kill)
+    nfound = 0
+    for g in range(ngulp):
+        got, counts, searched = bt.process_gulp(gulps[g].data_ptr(), on_device=True)
+        offs = np.concatenate([[0], np.cumsum(counts)])
+        for b in sample:
+            want, sw = singles[b].process_gulp(gulps[g][b].cpu().numpy()[None])
+            assert searched[b] == sw, (g, b)
+            mine = got[offs[b]:offs[b + 1]]
+            assert cands_equal(mine, want), (g, b, len(mine), len(want))
+            if sw:
+                assert np.array_equal(bt.copy_dedisp(b), singles[b].copy_dedisp()), (g, b)
+                nfound += len(want)
+    assert searched.all() and nfound > 0
+    bt.close()
+    for s in singles.values():
+        s.close()

@@ -38,10 +38,13 @@ WORKLOAD = ("full single beam: 2048 ch 375-468.75 MHz, tsamp 0.524288 ms, gulp 6
             "DM 0-2000 tol 1.25, widths 1-256, 7 sigma")
 METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp latency"
 UNIT = "beam·s/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of the timed k_dedisp launch of this workload
-# (its tile shape as set in main_full), from a single-pass ncu capture of those two metrics on
-# `bench.py --steps 1 --warmup 3 --no-cpu-baseline` (7.99 GB read + 0.673 GB written)
-DEDISP_TRAFFIC_BYTES = 8.664e9
+# dram__bytes_read.sum + dram__bytes_write.sum of one timed dedispersion launch of the full
+# single beam, by tile shape (hella_tuning fields in order), from single-pass ncu captures of
+# those two metrics on `bench.py --steps 1 --warmup 3 --no-cpu-baseline --no-batched`
+# (profiles/k_dedisp_full_beam.md).  A shape without a capture reports null.
+DEDISP_TRAFFIC = {
+    (0, 4, 8, 0, 8, 2): 8.664e9,  # 16-trial tiles, 8-channel stages, groups of 8, add mode 2: 7.99 + 0.673 GB
+}
 
 
 def args_():
@@ -65,6 +68,8 @@ def args_():
                          "cases that profiling captures use")
     ap.add_argument("--dm-max", type=float, default=0.0,
                     help="DM ceiling of the full workload (0: 2000); a small profiling case")
+    ap.add_argument("--add-mode", type=int, default=2,
+                    help="dedispersion add mode of the single-beam workloads (hella_tuning.add_mode)")
     return ap.parse_args()
 
 
@@ -262,7 +267,7 @@ def main():
     # Modes 2 and 3 measured 19.40 ms on the full beam against 19.49 for mode 0; the autotuner
     # lands within 0.3 % of that with groups of 2-4, which read 12 GB from DRAM per launch
     # against 8.1 GB for groups of 8.
-    s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, 2))
+    s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode))
     try:
         s.time_dedisp(None, 1)
     except hg.HellaError:  # DM lists whose tiles hold fewer than 8 trials take add mode 0
@@ -300,18 +305,24 @@ def main():
     # ---------------- end to end through the C ABI from pinned host memory
     lat = []
     ncand = []
+    e2e_ev = [(ev(), ev()) for _ in range(a.steps)]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     w0 = time.perf_counter()
-    for _ in range(a.steps):
+    for k in range(a.steps):
         q0 = time.perf_counter()
+        e2e_ev[k][0].record(stream)
         cands, searched = s.process_gulp(host[gi % len(host)].data_ptr(), on_device=False)
+        e2e_ev[k][1].record(stream)
         lat.append(time.perf_counter() - q0)
         ncand.append(len(cands))
         gi += 1
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
+    # the stream's own time for each call (upload, search, candidate copy): a host-side stall
+    # shows as latency above it
+    e2e_dev = [e0.elapsed_time(e1) for e0, e1 in e2e_ev]
     e2e, e2e_s = job_rate(dist, a.steps * gulp_s, e2e_s)
 
     clk = clocks.stop()
@@ -324,7 +335,9 @@ def main():
     achieved = adds / dd_t / 1e12
     peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
     roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4), "traffic": DEDISP_TRAFFIC_BYTES if a.workload == "full" and not (a.nchan or a.dm_max) else None,
+            "frac": round(achieved / peak, 4),
+            "traffic": DEDISP_TRAFFIC.get(tuple(s.get_tuning().as_dict().values()))
+            if a.workload == "full" and not (a.nchan or a.dm_max) else None,
             "traffic_unit": "bytes per launch (ncu)",
             "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
@@ -373,7 +386,10 @@ def main():
                 "d2h_bytes_per_step": int(4 + 20 * np.mean(ncand)),
                 "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
-                "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1)},
+                "max_ms": round(1e3 * max(lat), 2), "gulp_ms": round(gulp_s * 1e3, 1),
+                "stream_ms_p50": round(float(np.percentile(e2e_dev, 50)), 2),
+                "stream_ms_p99": round(float(np.percentile(e2e_dev, 99)), 2),
+                "stream_ms_max": round(float(max(e2e_dev)), 2)},
         "gpu_launches": int(launches),
         "roofline": roof,
         "rooflines_other": extra,
@@ -554,7 +570,10 @@ STREAM_WORKLOAD = ("streaming serving loop: 64 beam requests x 1024 ch, tsamp 1.
 
 
 def main_stream(a, rank, world, local, dist):
-    """The serving loop of the streaming configuration (submit/poll)."""
+    """The serving loop of the streaming configuration (submit/poll): the
+    whole schedule of joins and leaves run twice, gulps back to back
+    (throughput) and gulps released at a fixed arrival period (latency from
+    a gulp's arrival to its candidates on the host)."""
     import torch
     import hella_gb300 as hg
     import synth
@@ -563,13 +582,19 @@ def main_stream(a, rank, world, local, dist):
     NB, G, nch = params["nbeam"], params["gulp"], params["nchan"]
     gulp_s = G * params["tsamp"]
     kw = dict(dynamic=True, inflight=2)
-    # admission: slots = the most that fit the HBM budget (here 3/4 of what all 64 requests need)
+    # the HBM budget: 3/4 of what all 64 requests need with every smoothing width's planes held
     need = hg.batch_bytes(hg.default_params(**params), **kw)
     budget = int(0.75 * need)
+    # admission: the most slots whose state fits the budget with one width's planes held at a
+    # time (the smoothing then runs one width per pass; each pass re-reads the dedispersed plane)
+    fit = lambda n, w: hg.batch_bytes(hg.default_params(**dict(params, nbeam=n, hbm_budget=budget)),
+                                      widths_per_pass=w, **kw)
     slots = NB
-    while slots > 1 and hg.batch_bytes(hg.default_params(**dict(params, nbeam=slots, hbm_budget=budget)),
-                                       **kw) > budget:
+    while slots > 1 and fit(slots, 1) > budget:
         slots -= 1
+    per_width = fit(slots, 2) - fit(slots, 1)
+    nbox = len([w for w in range(16) if params["width_min"] << w < params["width_max"]])
+    wpp = int(min(nbox, (budget - (fit(slots, 1) - per_width)) // per_width))
     rng = np.random.default_rng(7 + rank)
     # requests: 48 beams from the start, 16 more at 25% of the run; 12 leave at 50%
     join_at = {b: 0 if b < 48 else ngulps // 4 for b in range(NB)}
@@ -588,88 +613,99 @@ def main_stream(a, rank, world, local, dist):
     del buf
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t_gen
-
-    member = np.zeros(slots, np.int32)
-    bt = hg.Batch(hg.default_params(**dict(params, nbeam=slots, device=local, hbm_budget=budget)),
-                  member=member, **kw)
-    slot_of, free, waiting = {}, list(range(slots)), []
-    admitted = refused_at_once = 0
-    lat, dev_ms, ncand, searched_beams = [], [], [], 0
-    pending = 0
     lanes = [torch.empty((slots, G, nch), dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+
+    def run(period_s: float):
+        """The schedule once; period_s = 0: back to back with two gulps in
+        flight, else gulp g arrives at g * period_s and is polled at once."""
+        bt = hg.Batch(hg.default_params(**dict(params, nbeam=slots, device=local, hbm_budget=budget)),
+                      member=np.zeros(slots, np.int32), widths_per_pass=wpp, **kw)
+        slot_of, free, waiting = {}, list(range(slots)), []
+        st = dict(admitted=0, waited=0, searched=0, lat=[], dev=[], ncand=[], arrival=[])
+        pending = []
+
+        def poll():
+            got, counts, searched, l_ms, d_ms = bt.poll()
+            arrived = pending.pop(0)
+            st["arrival"].append((time.perf_counter() - arrived) * 1e3)
+            st["lat"].append(l_ms), st["dev"].append(d_ms), st["ncand"].append(len(got))
+            st["searched"] += int(searched.sum())
+
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for g in range(ngulps):
+            arrive = t0 + g * period_s
+            if period_s:
+                while time.perf_counter() < arrive:
+                    time.sleep(min(0.002, max(0.0, arrive - time.perf_counter())))
+            # membership changes need an idle batch: drain, then admit / release
+            changes = [b for b, t in leave_at.items() if t == g and b in slot_of]
+            arrivals = [b for b, t in join_at.items() if t == g]
+            if changes or arrivals or (waiting and free):
+                while pending:
+                    poll()
+                for b in changes:
+                    sl = slot_of.pop(b)
+                    bt.set_beam(sl, False)
+                    free.append(sl)
+                for b in arrivals:
+                    waiting.append(b)
+                    if not free:
+                        st["waited"] += 1
+                while waiting and free:
+                    b, sl = waiting.pop(0), free.pop(0)
+                    bt.set_beam(sl, True, params["dm_max"], kills[b])
+                    slot_of[b] = sl
+                    st["admitted"] += 1
+            lane = lanes[g % 2]
+            for b, sl in slot_of.items():
+                lane[sl].copy_(host[g, b])
+            bt.submit(lane.data_ptr())
+            pending.append(arrive if period_s else time.perf_counter())
+            if period_s or len(pending) == 2:
+                poll()
+        while pending:
+            poll()
+        st["wall"] = time.perf_counter() - t0
+        st["kernels"] = int(ngulps * bt.graph_kernels())
+        bt.close()
+        return st
+
     clocks = Clocks(local)
     clocks.start()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for g in range(ngulps):
-        # membership changes need an idle batch: drain, then admit / release
-        changes = [b for b, t in leave_at.items() if t == g and b in slot_of]
-        arrivals = [b for b, t in join_at.items() if t == g]
-        if changes or arrivals or (waiting and free):
-            while pending:
-                got, counts, searched, l_ms, d_ms = bt.poll()
-                lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
-                searched_beams += int(searched.sum())
-                pending -= 1
-            for b in changes:
-                s = slot_of.pop(b)
-                bt.set_beam(s, False)
-                free.append(s)
-            for b in arrivals:
-                waiting.append(b)
-                if not free:
-                    refused_at_once += 1
-            while waiting and free:
-                b, s = waiting.pop(0), free.pop(0)
-                bt.set_beam(s, True, params["dm_max"], kills[b])
-                slot_of[b] = s
-                admitted += 1
-        # this gulp's data of the admitted beams, laid out by slot
-        lane = lanes[g % 2]
-        for b, s in slot_of.items():
-            lane[s].copy_(host[g, b])
-        bt.submit(lane.data_ptr())
-        pending += 1
-        if pending == 2:
-            got, counts, searched, l_ms, d_ms = bt.poll()
-            lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
-            searched_beams += int(searched.sum())
-            pending -= 1
-    while pending:
-        got, counts, searched, l_ms, d_ms = bt.poll()
-        lat.append(l_ms), dev_ms.append(d_ms), ncand.append(len(got))
-        searched_beams += int(searched.sum())
-        pending -= 1
-    wall = time.perf_counter() - t0
+    fast = run(0.0)
+    period = max(0.05, 2.5 * float(np.percentile(fast["dev"], 99)) / 1e3)
+    paced = run(period)
     clk = clocks.stop()
-    beam_gulps = searched_beams
-    value, _ = job_rate(dist, beam_gulps * gulp_s, float(np.sum(dev_ms)) / 1e3)
-    e2e, _ = job_rate(dist, beam_gulps * gulp_s, wall)
+    beam_gulps = fast["searched"]
+    value, _ = job_rate(dist, beam_gulps * gulp_s, float(np.sum(fast["dev"])) / 1e3)
+    e2e, _ = job_rate(dist, beam_gulps * gulp_s, fast["wall"])
+    arr = np.asarray(paced["arrival"])
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": ngulps,
-        "warmup": 0, "ms_per_step": round(float(np.mean(dev_ms)), 3), "higher_is_better": True,
+        "warmup": 0, "ms_per_step": round(float(np.mean(fast["dev"])), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded noise, drifting RFI, bursts 1 per beam per 30 s; drawn on the GPU)",
         "config": {"workload": STREAM_WORKLOAD.format(sec=a.seconds), "beam_requests": NB,
-                   "slots_in_budget": slots, "hbm_budget_gb": round(budget / 1e9, 2), "admitted": admitted,
-                   "waited_for_a_slot": refused_at_once, "gulps": ngulps, "searched_beam_gulps": beam_gulps,
-                   "cadence": "gulps replayed back to back (no real-time wait); latency = submit to results",
+                   "slots_in_budget": slots, "hbm_budget_gb": round(budget / 1e9, 2),
+                   "widths_per_pass": wpp, "admitted": fast["admitted"], "waited_for_a_slot": fast["waited"],
+                   "gulps": ngulps, "searched_beam_gulps": beam_gulps,
+                   "cadence": (f"value and e2e.value: gulps back to back, two in flight; e2e latencies: gulps "
+                               f"released every {period * 1e3:.0f} ms (the 8.6 s real-time period compressed), "
+                               f"arrival to candidates on the host"),
                    "gen_s": round(gen_s, 1), "parallelism": f"replicas{world}"},
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": slots * G * nch,
-                "d2h_bytes_per_step": int(4 * slots + 20 * np.mean(ncand)),
-                "p50_ms": round(float(np.percentile(lat, 50)), 2),
-                "p99_ms": round(float(np.percentile(lat, 99)), 2), "max_ms": round(float(np.max(lat)), 2),
-                "gulp_ms": round(gulp_s * 1e3, 1)},
-        "gpu_launches": None,
+                "d2h_bytes_per_step": int(4 * slots + 20 * np.mean(fast["ncand"])),
+                "p50_ms": round(float(np.percentile(arr, 50)), 2), "p99_ms": round(float(np.percentile(arr, 99)), 2),
+                "max_ms": round(float(arr.max()), 2), "period_ms": round(period * 1e3, 1),
+                "gulp_ms": round(gulp_s * 1e3, 1),
+                "back_to_back_p50_ms": round(float(np.percentile(fast["arrival"], 50)), 2),
+                "back_to_back_p99_ms": round(float(np.percentile(fast["arrival"], 99)), 2)},
+        "gpu_launches": fast["kernels"],
         "clocks": clk,
-        "candidates_per_gulp": float(np.mean(ncand)),
+        "candidates_per_gulp": float(np.mean(fast["ncand"])),
     }
-    try:
-        line["gpu_launches"] = int(ngulps * bt.graph_kernels())
-    except Exception:
-        pass
-    bt.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -432,6 +432,40 @@ hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  if (t.add_mode == 4) {
+    // sub-band sums over every channel: a beam's killed channels are packed
+    // as zeros, so the plan's tables serve every beam
+    hg::SubDeviceTables sb;
+    if (hg::plan_sub_tables(b->plan, 0, b->z.ndms_all, &sb) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
+    if (sb.nact != b->p.nchan) return HELLA_ERR_DEDISP;  // the plan keeps every channel
+    hg::DedispArgs a{};
+    a.beams = b->d_dbeams;
+    a.nbeam = b->nbeam;
+    a.ntt = hg::dedisp_time_tiles(b->z.ntime_dd);
+    int items = 0;
+    for (int i = 0; i < b->nbeam; ++i) {
+      b->dbeams[i].item0 = items;
+      items += hg::dedisp_items(b->dbeams[i].dm_count, hg::kSubDPT, a.ntt);
+    }
+    if (b->items_dpt != hg::kSubDPT) {
+      CK(cudaStreamSynchronize(b->stream));
+      CK(cudaMemcpy(b->d_dbeams, b->dbeams.data(), sizeof(hg::DedispBeam) * b->nbeam, cudaMemcpyHostToDevice));
+      b->items_dpt = hg::kSubDPT;
+    }
+    a.nitems = items;
+    a.group = t.group;
+    a.R = b->z.R;
+    a.dm_first = 0;
+    a.nout = b->z.ntime_dd;
+    a.out_stride = b->z.ntime_dd;
+    a.cc = hg::kSubG;
+    a.nbuf = t.stages;
+    a.unit = 1;
+    a.err = b->d_err;
+    hg::use_sub_tables(&a, sb);
+    *out = a;
+    return HELLA_OK;
+  }
   hg::DeviceTables tb;
   if (hg::plan_device_tables(b->plan, 0, b->z.ndms_all, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
     return HELLA_ERR_DEDISP;

@@ -563,6 +563,296 @@ __global__ void k_transpose_tf(const uint8_t *__restrict__ in, size_t in_stride,
   }
 }
 
+
+// ---------------------------------------------------------------------
+// Add mode 4: sub-band sums shared by the trials of a tile.
+//
+// Within a tile of kSubDPT trials, a group of kSubG adjacent active
+// channels c0..c3 contributes x[c0][t+d0] + x[c1][t+d1] + x[c2][t+d2] +
+// x[c3][t+d3] to trial d (dk = delay(ck, d)).  The relative delays
+// dk - d0 take few distinct values over the tile's trials (3.7 "patterns"
+// per 16 trials and 4 channels on the full beam's DM list), so a stage
+// stages the group's four rows (as the 8-channel stages do), the block
+// builds one row of four-channel sums per pattern in shared memory (16-bit
+// lanes, <= 4 x 255, two words per packed position: samples k = 0,2 and
+// k = 1,3), and each trial adds the row of its pattern at its offset: one
+// 8-byte shared load and two adds per trial and group, against four loads,
+// eight byte permutes and two three-input adds channel by channel.  The
+// sums are integers, so any grouping gives the same totals.
+//
+// Host tables per (tile, group): a record of ints
+//   [npat, pattern words, channels in the group, 0,
+//    toff[16]   byte offset of trial m's read in the pattern rows (+ 8 j),
+//    per pattern: L (words), row offset (words), 0, 0, o0, o1, o2, o3]
+// where pattern p's row holds L words (256 plus the spread of its trials'
+// head delays) and its word q sums staged word sh_k + o_k + q of each
+// channel k.  Pattern rows are built with one block barrier per stage,
+// into two alternating buffers, so a stage's sums and the next stage's
+// building never touch the same buffer.
+constexpr int kSubRecHdr = 20;  // ints before the patterns: header + toff[16]
+
+__device__ __forceinline__ void sts64(uint32_t addr, uint32_t x, uint32_t y) {
+  asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(addr), "r"(x), "r"(y) : "memory");
+}
+__device__ __forceinline__ uint2 lds64(uint32_t addr) {
+  uint2 v;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts128(uint32_t addr, int4 v) {
+  asm volatile("st.shared.v4.s32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+__host__ __device__ constexpr uint32_t sub_buf_bytes(int rowstride, int recb) {
+  return 16u + (uint32_t)recb + (uint32_t)kSubG * (uint32_t)rowstride * 4u;
+}
+__host__ __device__ constexpr uint32_t sub_pat_bytes(int words) {
+  return 64u + (uint32_t)((words + 1) / 2 * 2) * 8u;  // 16-byte multiple: the next buffer's header is read as int4
+}
+
+__global__ void __launch_bounds__(kDedispThreads, 2)
+    k_dedisp_sub(DedispArgs a, int rowstride, int nbuf, int recb, int pwords) {
+  extern __shared__ __align__(128) uint32_t smem[];
+  constexpr int NWARP = kDedispThreads / 32;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t rs4 = (uint32_t)rowstride * 4u;
+  const uint32_t bufb = sub_buf_bytes(rowstride, recb);
+  const uint32_t patb = sub_pat_bytes(pwords);
+  auto full_of = [&](int b) { return sbase + 8u * b; };
+  auto empty_of = [&](int b) { return sbase + 32u + 8u * b; };
+  const uint32_t abort_at = sbase + 64u;
+  auto sh_of = [&](int b) { return sbase + kBarBytes + (uint32_t)b * bufb; };
+  auto rec_of = [&](int b) { return sh_of(b) + 16u; };
+  auto rows_of = [&](int b) { return rec_of(b) + (uint32_t)recb; };
+  auto pat_of = [&](unsigned g) { return sbase + kBarBytes + (uint32_t)nbuf * bufb + (g & 1u) * patb; };
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  struct Staged {  // the item a warp is staging, kept in shared memory to spare registers
+    const uint32_t *packed;
+    const int4 *meta;
+    long w0;
+    int tile, pad;
+  };
+  static_assert(128 + NWARP * sizeof(Staged) <= kBarBytes, "staging cursors");
+  Staged *staged = reinterpret_cast<Staged *>(reinterpret_cast<char *>(smem) + 128 + sizeof(Staged) * warp);
+
+  if (tid == 0) {
+    for (int b = 0; b < nbuf; ++b) {
+      mbar_init(full_of(b), 32);
+      mbar_init(empty_of(b), NWARP);
+    }
+    sts32(abort_at, 0);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= a.nitems) return;
+
+  const int ngroups = (a.nact + kSubG - 1) / kSubG;
+  const unsigned g_end = (unsigned)((a.nitems - 1 - blockIdx.x) / gridDim.x + 1) * (unsigned)ngroups;
+  unsigned g_next = (unsigned)warp;  // next stage this warp stages
+  int staged_k = -1;
+
+  // Stages stage g_next (group g_next % ngroups of the block's item
+  // g_next / ngroups) into buffer g_next % nbuf.
+  auto issue = [&](bool block, bool *timed_out) -> bool {
+    const unsigned g = g_next;
+    const int b = (int)(g % (unsigned)nbuf);
+    if (g >= (unsigned)nbuf) {
+      const uint32_t par = ((g / nbuf) - 1u) & 1u;
+      if (block) {
+        if (!mbar_wait(empty_of(b), par)) {
+          *timed_out = true;
+          return false;
+        }
+      } else if (!mbar_test(empty_of(b), par)) {
+        return false;
+      }
+    }
+    const int k = (int)(g / (unsigned)ngroups), st = (int)(g % (unsigned)ngroups);
+    if (k != staged_k) {
+      if (lane == 0) {
+        const Item it = item_at<kSubDPT>(a, blockIdx.x + k * gridDim.x);
+        *staged = Staged{it.packed, it.meta, it.w0, it.tile, 0};
+      }
+      staged_k = k;
+      __syncwarp();
+    }
+    const int k0 = st * kSubG, nc = min(kSubG, a.nact - k0);
+    const uint32_t bar = full_of(b);
+    fence_proxy_async();
+    if (lane < nc) {
+      const int4 mc = __ldg(staged->meta + k0 + lane);  // {channel, base delay, spread, 0}
+      long p = staged->w0 + mc.y;
+      while (p >= a.R) p -= a.R;
+      const long a4 = p & ~3L;
+      const int sh = (int)(p - a4);
+      const int n16 = (sh + S + mc.z + 3) >> 2;  // 16-byte chunks, <= rowstride / 4
+      sts32(sh_of(b) + lane * 4u, sh);
+      int2 ix = make_int2(0, 0);
+      if (lane == 0) ix = __ldg(a.sub_index + (size_t)staged->tile * ngroups + st);  // {pool int, bytes}
+      mbar_arrive_tx(bar, (uint32_t)n16 * 16u + (uint32_t)ix.y);
+      const uint32_t *src = staged->packed + (size_t)mc.x * a.R;
+      uint32_t dst = rows_of(b) + (uint32_t)lane * rs4;
+      long pos = a4;
+      int left = n16;
+      while (left > 0) {  // the ring may wrap inside the staged window
+        const int n = (int)min((long)left, (a.R - pos) >> 2);
+        bulk_g2s(dst, src + pos, (uint32_t)n * 16u, bar);
+        dst += (uint32_t)n * 16u;
+        left -= n;
+        pos = 0;
+      }
+      if (lane == 0) bulk_g2s(rec_of(b), a.sub_pool + ix.x, (uint32_t)ix.y, bar);
+    } else {
+      mbar_arrive(bar);
+    }
+    __syncwarp();
+    g_next += NWARP;
+    return true;
+  };
+
+  unsigned gs_c = 0;  // stages consumed
+  for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    uint32_t acc_e[kSubDPT], acc_o[kSubDPT], tot[kSubDPT][4];
+#pragma unroll
+    for (int m = 0; m < kSubDPT; ++m) {
+      acc_e[m] = acc_o[m] = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) tot[m][k] = 0u;
+    }
+    for (int st = 0; st < ngroups; ++st) {
+      bool bad = false;
+      {
+        bool to = false;
+        while (g_next < g_end && g_next < gs_c + nbuf)
+          if (!issue(g_next <= gs_c, &to)) break;
+        bad = to;
+      }
+      const int b = (int)(gs_c % (unsigned)nbuf);
+      if (!bad && !mbar_wait(full_of(b), (gs_c / nbuf) & 1u)) bad = true;
+      const uint32_t pb = pat_of(gs_c);
+      if (!bad) {
+        // ---- build the stage's pattern rows (flattened: word w of the rows to thread w % 256)
+        const uint32_t rb = rec_of(b);
+        const int4 hd = lds128(rb);  // npat, words, channels, 0
+        if (tid < 4) sts128(pb + 16u * tid, lds128(rb + 16u + 16u * tid));  // toff[16] for the sums
+        const uint32_t r0 = rows_of(b);
+        const int gc = hd.z;
+        uint32_t shk[kSubG];
+#pragma unroll
+        for (int k = 0; k < kSubG; ++k) shk[k] = k < gc ? lds32(sh_of(b) + 4u * k) : 0u;
+        for (int p = 0; p < hd.x; ++p) {
+          const int4 pa = lds128(rb + 4u * (kSubRecHdr + 8 * p));      // L, row offset
+          const int4 po = lds128(rb + 4u * (kSubRecHdr + 8 * p + 4));  // o0..o3
+          int q = (tid - pa.y) & (S - 1);
+          if (q >= pa.x) continue;
+          uint32_t dst = pb + 64u + 8u * (uint32_t)(pa.y + q);
+          uint32_t ra = r0 + 4u * (shk[0] + po.x + q);
+          uint32_t rbw = r0 + rs4 + 4u * (shk[1] + po.y + q);
+          uint32_t rc = r0 + 2u * rs4 + 4u * (shk[2] + po.z + q);
+          uint32_t rd = r0 + 3u * rs4 + 4u * (shk[3] + po.w + q);
+          if (gc == kSubG) {
+            for (; q < pa.x; q += S) {
+              const uint32_t w0 = lds32(ra), w1 = lds32(rbw), w2 = lds32(rc), w3 = lds32(rd);
+              const uint32_t e = __byte_perm(w0, 0u, 0x4240) + __byte_perm(w1, 0u, 0x4240) +
+                                 (__byte_perm(w2, 0u, 0x4240) + __byte_perm(w3, 0u, 0x4240));
+              const uint32_t o = __byte_perm(w0, 0u, 0x4341) + __byte_perm(w1, 0u, 0x4341) +
+                                 (__byte_perm(w2, 0u, 0x4341) + __byte_perm(w3, 0u, 0x4341));
+              sts64(dst, e, o);
+              dst += 8u * S;
+              ra += 4u * S;
+              rbw += 4u * S;
+              rc += 4u * S;
+              rd += 4u * S;
+            }
+          } else {  // the last group of a channel list that is not a multiple of four
+            for (; q < pa.x; q += S) {
+              uint32_t e = 0u, o = 0u;
+              const uint32_t w0 = lds32(ra);
+              e += __byte_perm(w0, 0u, 0x4240);
+              o += __byte_perm(w0, 0u, 0x4341);
+              if (gc > 1) {
+                const uint32_t w1 = lds32(rbw);
+                e += __byte_perm(w1, 0u, 0x4240);
+                o += __byte_perm(w1, 0u, 0x4341);
+              }
+              if (gc > 2) {
+                const uint32_t w2 = lds32(rc);
+                e += __byte_perm(w2, 0u, 0x4240);
+                o += __byte_perm(w2, 0u, 0x4341);
+              }
+              sts64(dst, e, o);
+              dst += 8u * S;
+              ra += 4u * S;
+              rbw += 4u * S;
+              rc += 4u * S;
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(empty_of(b));  // this warp is done with the staged rows of buffer b
+        if (bad) {
+          if (a.err) atomicOr(a.err, 1);
+          sts32(abort_at, 1);
+        }
+      }
+      __syncthreads();  // the stage's pattern rows are complete (and the previous stage's sums done)
+      if (lds32(abort_at)) {
+        // a wait ran out somewhere in the block: let this warp's copies land, end
+        for (unsigned g = gs_c; g < g_next; ++g)
+          if (g % NWARP == (unsigned)warp) mbar_wait(full_of((int)(g % nbuf)), (g / nbuf) & 1u);
+        return;
+      }
+      // ---- sums: each trial adds its pattern row at its offset
+      const uint32_t rows = pb + 64u + 8u * (uint32_t)tid;
+#pragma unroll
+      for (int q4 = 0; q4 < kSubDPT / 4; ++q4) {
+        const int4 to = lds128(pb + 16u * q4);
+        const int t4[4] = {to.x, to.y, to.z, to.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint2 v = lds64(rows + (uint32_t)t4[j]);
+          acc_e[4 * q4 + j] += v.x;
+          acc_o[4 * q4 + j] += v.y;
+        }
+      }
+      ++gs_c;
+      if ((st + 1) % (256 / kSubG) == 0) {  // 64 groups of <= 1020 per 16-bit lane, then widen
+#pragma unroll
+        for (int m = 0; m < kSubDPT; ++m) {
+          tot[m][0] += acc_e[m] & 0xffffu;
+          tot[m][2] += acc_e[m] >> 16;
+          tot[m][1] += acc_o[m] & 0xffffu;
+          tot[m][3] += acc_o[m] >> 16;
+          acc_e[m] = acc_o[m] = 0u;
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < kSubDPT; ++m) {
+      tot[m][0] += acc_e[m] & 0xffffu;
+      tot[m][2] += acc_e[m] >> 16;
+      tot[m][1] += acc_o[m] & 0xffffu;
+      tot[m][3] += acc_o[m] >> 16;
+    }
+    const Item it = item_at<kSubDPT>(a, item);
+#pragma unroll
+    for (int m = 0; m < kSubDPT; ++m) {
+      const int i = it.tile * kSubDPT + m;
+      if (i >= it.dm_count) break;
+      float *o = it.out + (size_t)i * a.out_stride;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int t = it.t0 + tid + k * S;
+        if (t < a.nout) o[t] = (float)tot[m][k];
+      }
+    }
+  }
+}
+
 }  // namespace
 
 // Smallest and largest delay of channel c over trials d0..d1 (the first
@@ -640,6 +930,76 @@ DedispTables dedisp_tables(const int *delays, int nchan, const int *chans, int n
   return t;
 }
 
+// ---- add mode 4 tables (see k_dedisp_sub)
+SubTables dedisp_sub_tables(const int *delays, int nchan, const int *chans, int nact, int dm_first,
+                            int dm_count) {
+  SubTables t;
+  const int dlast = dm_first + dm_count - 1;
+  t.ntiles = (dm_count + kSubDPT - 1) / kSubDPT;
+  t.ngroups = (nact + kSubG - 1) / kSubG;
+  t.meta.resize((size_t)t.ntiles * nact);
+  t.index.resize((size_t)t.ntiles * t.ngroups);
+  std::vector<int> base(nact), rel(kSubDPT * kSubG), h(kSubDPT), pid(kSubDPT);
+  for (int i = 0; i < t.ntiles; ++i) {
+    const int d0 = dm_first + i * kSubDPT, d1 = std::min(d0 + kSubDPT - 1, dlast), nt = d1 - d0 + 1;
+    for (int k = 0; k < nact; ++k) {
+      int lo, hi;
+      tile_delay_range(delays, nchan, chans[k], d0, d1, &lo, &hi);
+      t.meta[(size_t)i * nact + k] = make_int4(chans[k], lo, hi - lo, 0);
+      base[k] = lo;
+      t.max_spread = std::max(t.max_spread, hi - lo);
+    }
+    for (int g = 0; g < t.ngroups; ++g) {
+      const int k0 = g * kSubG, gc = std::min(kSubG, nact - k0);
+      auto dl = [&](int m, int k) { return delays[(size_t)(d0 + m) * nchan + chans[k0 + k]]; };
+      // patterns: the relative delays of the group's channels, in order of first use
+      std::vector<int> first;  // trial that defines each pattern
+      for (int m = 0; m < nt; ++m) {
+        for (int k = 0; k < gc; ++k) rel[m * kSubG + k] = dl(m, k) - dl(m, 0);
+        h[m] = dl(m, 0) - base[k0];
+        int p = 0;
+        for (; p < (int)first.size(); ++p)
+          if (std::equal(&rel[m * kSubG], &rel[m * kSubG] + gc, &rel[first[p] * kSubG])) break;
+        if (p == (int)first.size()) first.push_back(m);
+        pid[m] = p;
+      }
+      const int npat = (int)first.size();
+      std::vector<int> rec(kSubRecHdr + 8 * npat, 0);
+      int words = 0;
+      for (int p = 0; p < npat; ++p) {
+        int qlo = 1 << 30, qhi = -1;
+        for (int m = 0; m < nt; ++m)
+          if (pid[m] == p) {
+            qlo = std::min(qlo, h[m]);
+            qhi = std::max(qhi, h[m]);
+          }
+        int *pr = &rec[kSubRecHdr + 8 * p];
+        pr[0] = S + qhi - qlo;  // L
+        pr[1] = words;          // row offset
+        for (int k = 0; k < gc; ++k)
+          pr[4 + k] = base[k0] + qlo + rel[first[p] * kSubG + k] - base[k0 + k];  // >= 0, see the kernel
+        for (int m = 0; m < nt; ++m)
+          if (pid[m] == p) rec[4 + m] = 8 * (words + h[m] - qlo);
+        words += pr[0];
+      }
+      rec[0] = npat;
+      rec[1] = words;
+      rec[2] = gc;
+      t.index[(size_t)i * t.ngroups + g] = make_int2((int)t.pool.size(), (int)(rec.size() * 4));
+      t.pool.insert(t.pool.end(), rec.begin(), rec.end());
+      t.max_words = std::max(t.max_words, words);
+      t.max_rec = std::max(t.max_rec, (int)(rec.size() * 4));
+    }
+  }
+  return t;
+}
+
+// Shared memory of the add-mode-4 kernel with `nbuf` staging buffers.
+size_t dedisp_sub_smem(int max_spread, int max_words, int max_rec, int nbuf) {
+  return kBarBytes + (size_t)nbuf * sub_buf_bytes(row_words(max_spread), max_rec) +
+         2 * (size_t)sub_pat_bytes(max_words);
+}
+
 namespace {
 
 template <int DPT, int CC, int MODE, bool VAR>
@@ -692,12 +1052,46 @@ cudaError_t launch_cc(const DedispArgs &a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
+// Add mode 4: staging depth 3 (2 if 3 does not fit) within the two-blocks
+// budget, else the deepest that fits one block per SM.
+cudaError_t launch_sub(const DedispArgs &a, cudaStream_t s) {
+  if (a.dpt != kSubDPT || a.varied || !a.sub_index || !a.sub_pool || a.sub_words < S || a.sub_rec < 16 ||
+      a.sub_rec % 16 != 0)
+    return cudaErrorInvalidValue;
+  const int rowstride = row_words(a.max_spread);
+  int nbuf = a.nbuf;
+  if (!nbuf) {
+    nbuf = 2;
+    for (int nb = 3; nb >= 2; --nb)
+      if (dedisp_sub_smem(a.max_spread, a.sub_words, a.sub_rec, nb) <= kSmemBudget) {
+        nbuf = nb;
+        break;
+      }
+  }
+  if (nbuf < 2 || nbuf > kMaxBuf) return cudaErrorInvalidValue;
+  const size_t smem = dedisp_sub_smem(a.max_spread, a.sub_words, a.sub_rec, nbuf);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_dedisp_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dedisp_sub, kDedispThreads, smem)) !=
+      cudaSuccess)
+    return e;
+  const int grid = std::max(1, std::min(a.nitems, std::max(1, per_sm) * sms));
+  k_dedisp_sub<<<grid, kDedispThreads, smem, s>>>(a, rowstride, nbuf, a.sub_rec, a.sub_words);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
   if (a.nitems <= 0 || a.nout <= 0 || a.nact <= 0) return cudaSuccess;
   if (a.R % 4 != 0 || a.ntt <= 0 || a.group <= 0 || a.nbeam <= 0) return cudaErrorInvalidValue;
   if (a.varied && !a.beams) return cudaErrorInvalidValue;
+  if (a.mode == 4) return launch_sub(a, s);
   switch (a.dpt) {
     case 16: return launch_cc<16>(a, s);
     case 8: return launch_cc<8>(a, s);

@@ -120,13 +120,19 @@ struct DedispArgs {
   int dpt;                  // DM trials per tile (16, 8, 4, 2 or 1)
   int cc;                   // channels per pipeline stage (8 or 16)
   int nbuf;                 // staging buffers, 2..4 (0: deepest that fits)
-  int mode;                 // pipe balance of the adds (0, 1, 2; 1-2 need dpt >= 8)
+  int mode;                 // pipe balance of the adds (0-3; 1-3 need dpt >= 8), or 4: sub-band
+                            // sums of four channels per pattern (dpt 16, tables below)
   int unit;                 // must be 1
   int max_spread;           // largest tile_meta spread
   const int4 *tile_meta;    // [ntiles][nact] {channel, smallest delay(c, d) of the tile, spread, 0}
   const int *tile_off;      // [ntiles][nact][max(dpt,4)] 4*(delay(c,d) - that delay), bytes
   int *err;                 // device status word: bit 0 = a staging wait timed out (may be null)
   int varied;               // some beam has tables of its own (dpt >= 8): stage counts differ
+  // mode 4: per (tile, group of four channels of tile_meta) a record in sub_pool
+  const int2 *sub_index;    // [ntiles][ngroups] {offset in sub_pool (ints), record bytes}
+  const int *sub_pool;
+  int sub_words;            // most pattern-row words of a record
+  int sub_rec;              // largest record, bytes (a multiple of 16)
 };
 // One beam's tile tables gathered from a launch's tables (all nch channels):
 // rows [meta0, meta0 + ntiles * nact) of the output, channels chans[chans0 ..).
@@ -159,6 +165,21 @@ struct DedispTables {
 };
 DedispTables dedisp_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
                            int dm_first, int dm_count, int dpt = 0, int cc = 8);
+// Tables of add mode 4 (sub-band sums shared by a 16-trial tile's trials,
+// groups of four consecutive active channels); meta as DedispTables.meta
+// for 16-trial tiles.
+constexpr int kSubG = 4;
+constexpr int kSubDPT = 16;
+struct SubTables {
+  int ntiles = 0, ngroups = 0, max_spread = 0, max_words = 0, max_rec = 0;
+  std::vector<int4> meta;
+  std::vector<int2> index;
+  std::vector<int> pool;
+};
+SubTables dedisp_sub_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
+                            int dm_first, int dm_count);
+// Shared memory of one add-mode-4 block.
+size_t dedisp_sub_smem(int max_spread, int max_words, int max_rec, int nbuf);
 // Largest delay spread over the active channels of any dpt-trial tile.
 int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int nact,
                   int dm_first, int dm_count, int dpt);

@@ -24,6 +24,18 @@ struct DeviceTables {
 };
 hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out, int dpt = 0,
                              int cc = 8);
+// Add-mode-4 tables for trials [first, first + count) over the plan's
+// active channels: host copy cached per range, device copy uploaded on first use.
+struct SubDeviceTables {
+  const int4 *meta;
+  const int2 *index;
+  const int *pool;
+  int max_spread, max_words, max_rec, nact;
+};
+hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out);
+// Points a launch at add-mode-4 tables (16-trial tiles; items must be counted
+// for that tile size).
+void use_sub_tables(DedispArgs *a, const SubDeviceTables &t);
 // Launch arguments for one beam over a plan's device tables.
 DedispArgs single_beam_args(const DeviceTables &tb, const uint32_t *packed, long R, long win0,
                             int dm_first, int dm_count, int nout, float *out, long out_stride,

@@ -16,7 +16,7 @@ inline bool tuning_ok(const hella_tuning &t) {
                       t.dm_per_block == 4 || t.dm_per_block == 8 || t.dm_per_block == 16;
   return dpt_ok && (t.chan_chunk == 8 || t.chan_chunk == 16) &&
          (t.stages == 0 || (t.stages >= 2 && t.stages <= 4)) && t.group >= 1 && t.group <= 4096 &&
-         t.add_mode >= 0 && t.add_mode <= 3;
+         t.add_mode >= 0 && t.add_mode <= 4 && (t.add_mode != 4 || t.dm_per_block == 0 || t.dm_per_block == 16);
 }
 
 // Coordinate search from `start`: add mode, channel chunk, DM tile, pipeline
@@ -48,7 +48,7 @@ inline hella_status tune_shapes(const hella_tuning &start,
     return HELLA_OK;
   };
   for (int round = 0; round < 2; ++round) {
-    for (int m = 0; m <= 3; ++m) {
+    for (int m = 0; m <= 3; ++m) {  // add mode 4 measured slower on every workload: not searched
       hella_tuning t = best;
       t.add_mode = m;
       if ((s = try_shape(t)) != HELLA_OK) return s;

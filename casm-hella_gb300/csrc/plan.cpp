@@ -93,6 +93,14 @@ struct hdd_plan_struct {
   uint8_t *d_in = nullptr, *d_plain = nullptr, *d_out = nullptr;
   uint32_t *d_packed = nullptr;
   size_t in_cap = 0, plain_cap = 0, out_cap = 0, packed_cap = 0;
+  // add-mode-4 tables of the last DM range used, host and device
+  hg::SubTables sub;
+  int sub_first = -1, sub_count = -1;
+  bool sub_on_device = false;
+  int4 *d_smeta = nullptr;
+  int2 *d_sindex = nullptr;
+  int *d_spool = nullptr;
+  size_t smeta_cap = 0, sindex_cap = 0, spool_cap = 0;
 };
 
 namespace {
@@ -102,6 +110,8 @@ thread_local int t_device = 0;
 void invalidate_tables(hdd_plan p) {
   p->tab_first = p->tab_count = p->tab_dpt = p->tab_cc = -1;
   p->tab_on_device = false;
+  p->sub_first = p->sub_count = -1;
+  p->sub_on_device = false;
 }
 
 // Delays of the plan's DM list; max_delay is the largest of them (the last
@@ -187,6 +197,61 @@ hdd_error plan_device_tables(hdd_plan p, int first, int count, DeviceTables *out
   return HDD_NO_ERROR;
 }
 
+hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out) {
+  if (p->sub_first != first || p->sub_count != count) {
+    try {
+      p->sub = dedisp_sub_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first, count);
+    } catch (const std::bad_alloc &) {
+      p->sub_first = p->sub_count = -1;
+      return HDD_MEM_ALLOC_FAILED;
+    }
+    p->sub_first = first;
+    p->sub_count = count;
+    p->sub_on_device = false;
+  }
+  const SubTables &t = p->sub;
+  if (!p->sub_on_device) {
+    hdd_error e;
+    if ((e = grow((void **)&p->d_smeta, &p->smeta_cap, std::max<size_t>(t.meta.size(), 1) * sizeof(int4))) !=
+            HDD_NO_ERROR ||
+        (e = grow((void **)&p->d_sindex, &p->sindex_cap, std::max<size_t>(t.index.size(), 1) * sizeof(int2))) !=
+            HDD_NO_ERROR ||
+        (e = grow((void **)&p->d_spool, &p->spool_cap, std::max<size_t>(t.pool.size(), 1) * sizeof(int))) !=
+            HDD_NO_ERROR)
+      return e;
+    if (!t.meta.empty() &&
+        (cudaMemcpy(p->d_smeta, t.meta.data(), t.meta.size() * sizeof(int4), cudaMemcpyHostToDevice) !=
+             cudaSuccess ||
+         cudaMemcpy(p->d_sindex, t.index.data(), t.index.size() * sizeof(int2), cudaMemcpyHostToDevice) !=
+             cudaSuccess ||
+         cudaMemcpy(p->d_spool, t.pool.data(), t.pool.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+             cudaSuccess))
+      return HDD_MEM_COPY_FAILED;
+    p->sub_on_device = true;
+  }
+  out->meta = p->d_smeta;
+  out->index = p->d_sindex;
+  out->pool = p->d_spool;
+  out->max_spread = t.max_spread;
+  out->max_words = t.max_words;
+  out->max_rec = t.max_rec;
+  out->nact = (int)p->chans.size();
+  return HDD_NO_ERROR;
+}
+
+void use_sub_tables(DedispArgs *a, const SubDeviceTables &t) {
+  a->dpt = kSubDPT;
+  a->mode = 4;
+  a->nact = t.nact;
+  a->max_spread = t.max_spread;
+  a->tile_meta = t.meta;
+  a->tile_off = nullptr;
+  a->sub_index = t.index;
+  a->sub_pool = t.pool;
+  a->sub_words = t.max_words;
+  a->sub_rec = t.max_rec;
+}
+
 DedispArgs single_beam_args(const DeviceTables &tb, const uint32_t *packed, long R, long win0,
                             int dm_first, int dm_count, int nout, float *out, long out_stride,
                             int *err) {
@@ -263,6 +328,9 @@ void hdd_destroy_plan(hdd_plan p) {
   cudaFree(p->d_plain);
   cudaFree(p->d_packed);
   cudaFree(p->d_out);
+  cudaFree(p->d_smeta);
+  cudaFree(p->d_sindex);
+  cudaFree(p->d_spool);
   delete p;
 }
 

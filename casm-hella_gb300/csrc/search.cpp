@@ -222,6 +222,28 @@ hella_status upload_beam(hella_ctx *c, int cap, int beam_id) {
 // Dedisperses `beam`'s window into the plane with tile shape t.
 hella_status dedisperse_beam(hella_ctx *c, int beam, const hella_tuning &t) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  if (t.add_mode == 4) {  // sub-band sums: tables of their own, 16-trial tiles
+    hg::SubDeviceTables sb;
+    if (hg::plan_sub_tables(c->plan, 0, c->ndms, &sb) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
+    if (sb.nact == 0) {
+      CK(cudaMemsetAsync(c->d_dd, 0, (size_t)c->ndms * c->ntime_dd * 4, c->stream));
+      return HELLA_OK;
+    }
+    const hg::DeviceTables tb{sb.meta, nullptr, hg::kSubDPT, sb.max_spread, sb.nact, hg::kSubG};
+    hg::DedispArgs a = hg::single_beam_args(tb, c->d_packed + (size_t)beam * c->p.nchan * c->R, c->R,
+                                            c->win0, 0, c->ndms, c->ntime_dd, c->d_dd, c->ntime_dd,
+                                            c->d_err);
+    hg::use_sub_tables(&a, sb);
+    a.group = t.group;
+    a.nbuf = t.stages;
+    const cudaError_t e = hg::dedisperse(a, c->stream);
+    if (e == cudaErrorInvalidValue) {  // the DM list's tiles do not fit this kernel's staging
+      cudaGetLastError();
+      return HELLA_ERR_INVALID_ARG;
+    }
+    CK(e);
+    return HELLA_OK;
+  }
   hg::DeviceTables tb;
   if (hg::plan_device_tables(c->plan, 0, c->ndms, &tb, t.dm_per_block, t.chan_chunk) != HDD_NO_ERROR)
     return HELLA_ERR_DEDISP;

@@ -106,7 +106,11 @@ typedef struct {
   int add_mode;           /* 0: three-input adds; 1: load addresses as
                              multiply-adds (FMA pipe); 2: 1 + odd lanes too;
                              3: odd lanes as multiply-adds, addresses as
-                             two-input adds (1-3 need dm_per_block >= 8) */
+                             two-input adds (1-3 need dm_per_block >= 8);
+                             4: sums of four adjacent channels built once
+                             per delay pattern of a 16-trial tile and shared
+                             by its trials (dm_per_block 0 or 16; chan_chunk
+                             and the per-beam killmask tables unused) */
 } hella_tuning;
 
 /* Derived sizes (casm_hella_refactored.cu:184-224). */

@@ -61,6 +61,10 @@ def args_():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the multi-beam leg that the full workload's line carries as `batched`")
     ap.add_argument("--batched-steps", type=int, default=8, help="timed gulps of that leg")
+    ap.add_argument("--widths-per-pass", type=int, default=0,
+                    help="smoothing widths whose planes the batched context holds at once (0: as many "
+                         "as the free device memory allows); fewer hold less memory and re-read the "
+                         "dedispersed planes once per extra pass")
     ap.add_argument("--seconds", type=float, default=600.0, help="sky seconds of the stream workload")
     ap.add_argument("--cutouts", type=int, default=4096, help="cutouts of the refine workload")
     ap.add_argument("--nchan", type=int, default=0,
@@ -474,7 +478,7 @@ def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool 
     torch.cuda.synchronize()
     t_c = time.perf_counter()
     bt = hg.Batch(hg.default_params(**params, device=local, autotune=1), dm_max=ceilings, killmask=kill,
-                  inflight=2)
+                  inflight=2, widths_per_pass=a.widths_per_pass)
     create_s = time.perf_counter() - t_c
     infos = [bt.info(b) for b in range(NB)]
     tune = bt.get_tuning().as_dict()
@@ -545,7 +549,8 @@ def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool 
                    "tsamp": params["tsamp"], "ndms_min": min(i.ndms for i in infos),
                    "ndms_max": max(i.ndms for i in infos), "ntime_max": max(i.ntime for i in infos),
                    "widths": infos[0].nboxcar, "tuning": tune, "create_s": round(create_s, 2),
-                   "device_gb": round(infos[0].device_bytes / 1e9, 1), "parallelism": f"replicas{world}",
+                   "device_gb": round(infos[0].device_bytes / 1e9, 1), "widths_per_pass": a.widths_per_pass or "all",
+                   "parallelism": f"replicas{world}",
                    "real_time_x": round(value / NB, 2),
                    "l2": f"inputs larger than L2: {NB * G * nch / 1e9:.1f} GB gulp per step"},
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": NB * G * nch,

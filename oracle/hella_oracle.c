@@ -1,7 +1,7 @@
 /*
  * hella_oracle.c -- CPU restatement of casm-hella's per-gulp FRB search.
  *
- * TEST INFRASTRUCTURE ONLY (the checker, never the product): see
+ * TEST INFRASTRUCTURE ONLY (compared against, never the product): see
  * hella_oracle.h for the contract, the arithmetic conventions and what is
  * pinned.  Build: oracle/Makefile (gcc -O3 -fopenmp -ffp-contract=off).
  */

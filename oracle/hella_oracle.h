@@ -1,7 +1,7 @@
 /*
  * hella_oracle.h -- CPU restatement of casm-hella's per-gulp FRB search.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path:
+ * TEST INFRASTRUCTURE ONLY.  The GPU path is compared against this library:
  * only the tests, the smoke check and the CPU-baseline leg of the benchmark
  * may load it.  The product (libhella_gb300.so) never links or calls it.
  *

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/build/libhella_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
-benchmark's CPU-baseline leg, as the checker.  Never used by the product.
+benchmark's CPU-baseline leg, to compare the GPU path against.  Never used by the product.
 """
 from __future__ import annotations
 

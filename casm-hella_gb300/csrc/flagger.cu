@@ -233,6 +233,45 @@ __global__ void __launch_bounds__(kBeamT) k_beam_sum(FlagState st, int which) {
   }
 }
 
+// med_filter_bandpass (median_filter.cpp:85-107, median_filter :36-77) with
+// a window of win (odd) channels: channel i in [h, nchan - h) takes the
+// middle element of its sorted window (h = win / 2), the first h channels
+// take channel h's value and the last h channel nchan - h - 1's.  Any sort
+// leaves the same middle element, so the values are the reference's.  One
+// block per beam, in place: the row is staged in shared memory first.
+__global__ void __launch_bounds__(kBeamT) k_bp_median(float *__restrict__ bp, int nchan, int win) {
+  __shared__ float row[kMaxChan];
+  float *r = bp + (size_t)blockIdx.x * nchan;
+  for (int c = threadIdx.x; c < nchan; c += blockDim.x) row[c] = r[c];
+  __syncthreads();
+  const int h = win / 2;
+  for (int c = threadIdx.x; c < nchan; c += blockDim.x) {
+    const int i = min(max(c, h), nchan - h - 1);
+    float w[kMaxBpMedian];
+    for (int k = 0; k < win; ++k) {  // insertion sort of the window
+      const float v = row[i - h + k];
+      int j = k - 1;
+      while (j >= 0 && w[j] > v) {
+        w[j + 1] = w[j];
+        --j;
+      }
+      w[j + 1] = v;
+    }
+    r[c] = w[h];
+  }
+}
+
+// k_lane_finish for mode, then the bandpass median filter where the
+// reference's bandpass_correct applies it (modes 0, 2 and 3: every bandpass
+// that data are divided by; not the spectral-flag bandpass of mode 1).
+unsigned lane_finish(const FlagState &st, int mode, int fin_blocks, cudaStream_t s) {
+  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, mode);
+  if (mode == 1 || st.bp_median <= 1) return 1;
+  float *bp = mode == 0 ? st.bp1 : mode == 2 ? st.bp3 : st.bpx;
+  k_bp_median<<<st.nbeam, kBeamT, 0, s>>>(bp, st.nchan, st.bp_median);
+  return 2;
+}
+
 // measure_ts: per sample, fp16 running sum over channels in channel order,
 // then ts = float(sum) / nchan.  Block = 128 consecutive samples; rows and
 // table slices are staged through shared memory 64 channels at a time.
@@ -544,9 +583,9 @@ cudaError_t scrunch_planes(const FlagState &st, const void *gulp, uint8_t *plain
   };
   auto bandpass_correct = [&](int mode, const float *bp) {
     k_plane_lanes<<<fin_blocks, 256, 0, s>>>(st);
-    k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, mode);
+    launches += lane_finish(st, mode, fin_blocks, s);
     k_plane_div<<<eb, 256, 0, s>>>(st, bp);
-    launches += 3;
+    launches += 2;
   };
   if (st.f16_input) {
     // the DADA path (transpose.cu:87-90): the gulp is the fp16 plane; bandpass_flag on it
@@ -618,7 +657,7 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   // bandpass_flag: bandpass_correct (calc_bandpass_new, divide_by_bp)
   k_build_lut<<<lutg, 256, 0, s>>>(st, 0);
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
-  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 0);
+  unsigned extra = lane_finish(st, 0, fin_blocks, s) - 1;
   k_build_lut<<<lutg, 256, 0, s>>>(st, 1);
   // normalize_data: calculate_stddev (mean pass, variance pass)
   k_row_partials<false, false><<<rowg, kRowT, kLutSlice, s>>>(gulp, st, 0);
@@ -632,13 +671,13 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
   k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 1);
   if (st.nscrunch > 0) {
-    count_launches(11);
+    count_launches(11 + extra);
     return scrunch_planes(st, gulp, plain, R, wpos, dpos, s);
   }
   // apply_scrunch(8,8,100,flag=0,ts=1): bandpass_correct ...
   k_build_lut<<<lutg, 256, 0, s>>>(st, 3);
   k_lane_partials<<<laneg, 256, 0, s>>>(gulp, st.lut, st.part, st.nchan, st.gulp);
-  k_lane_finish<<<fin_blocks, 256, 0, s>>>(st, 2);
+  extra += lane_finish(st, 2, fin_blocks, s) - 1;
   k_build_lut<<<lutg, 256, 0, s>>>(st, 4);
   // ... ts_correct ...
   k_ts<<<dim3((st.gulp + kTsT - 1) / kTsT, st.nbeam), kTsT, 0, s>>>(gulp, st);
@@ -652,7 +691,7 @@ cudaError_t flag_impl(const FlagState &st, const void *gulp_in, uint8_t *plain, 
   // transpose_output into the ring
   k_flag_out<<<dim3(st.nchan / kOutC, (st.gulp + kOutT - 1) / kOutT, st.nbeam), 256, 0, s>>>(gulp, st, plain,
                                                                                          R, wpos, dpos);
-  count_launches(24);
+  count_launches(24 + extra);
   return cudaGetLastError();
 }
 }  // namespace

@@ -59,7 +59,10 @@ struct FlagState {
   float *flagspec;          // [nchan] flag fractions accumulated over beams and gulps
   int f16_input;            // gulps arrive as fp16 [nbeam][nchan][gulp] (DADA input):
                             // every stage then runs on the planes
+  int bp_median;            // window of the bandpass median filter (1: identity)
 };
+// Largest bandpass median window (hella_params.bp_median).
+constexpr int kMaxBpMedian = 63;
 // Largest SCRUNCH widths the box filter stages in shared memory.
 constexpr int kMaxScrunch = 64;
 

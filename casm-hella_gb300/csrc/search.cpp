@@ -72,6 +72,8 @@ hella_status validate_params(const hella_params *p) {
   if (p->smooth_anchor != 0 && p->smooth_anchor != 1) return HELLA_ERR_INVALID_ARG;
   if (p->nscrunch < 0 || p->nscrunch > HELLA_MAX_SCRUNCH) return HELLA_ERR_INVALID_ARG;
   if (p->input_format != HELLA_INPUT_U8_TF && p->input_format != HELLA_INPUT_F16_FT) return HELLA_ERR_INVALID_ARG;
+  if (p->bp_median < 1 || p->bp_median % 2 == 0 || p->bp_median > hg::kMaxBpMedian || p->bp_median >= p->nchan)
+    return HELLA_ERR_INVALID_ARG;
   for (int i = 0; i < p->nscrunch; ++i) {
     const hella_scrunch &sc = p->scrunch[i];
     if (sc.tscrunch < 1 || sc.tscrunch > kMaxScrunch || sc.fscrunch < 1 || sc.fscrunch > kMaxScrunch ||
@@ -91,6 +93,7 @@ void flag_scrunch_params(const hella_params &p, FlagState *f) {
   f->flag_lo = p.flag1;
   f->flag_hi = p.flag2;
   f->f16_input = p.input_format == HELLA_INPUT_F16_FT;
+  f->bp_median = p.bp_median;
 }
 
 size_t gulp_bytes(const hella_params &p) {
@@ -313,6 +316,7 @@ void hella_params_default(hella_params *p) {
   p->flag2 = -1;
   p->max_giants = HELLA_MAX_GIANTS;
   p->smooth_anchor = 1;
+  p->bp_median = 1;
 }
 
 void hella_destroy(hella_ctx *c) {

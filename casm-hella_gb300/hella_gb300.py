@@ -48,7 +48,7 @@ class HellaParams(C.Structure):
         ("spec_min", C.c_float), ("spec_max", C.c_float), ("flag1", C.c_int), ("flag2", C.c_int),
         ("nscrunch", C.c_int), ("scrunch", HellaScrunch * HELLA_MAX_SCRUNCH),
         ("max_giants", C.c_int), ("beam0", C.c_int), ("smooth_anchor", C.c_int), ("device", C.c_int),
-        ("hbm_budget", C.c_size_t), ("autotune", C.c_int), ("input_format", C.c_int),
+        ("hbm_budget", C.c_size_t), ("autotune", C.c_int), ("input_format", C.c_int), ("bp_median", C.c_int),
     ]
 
 

@@ -88,6 +88,12 @@ typedef struct {
                        filterbank gulps; HELLA_INPUT_F16_FT (1): fp16
                        [nbeam][nchan][gulp], the DADA input (INPUT DADA,
                        casm_hella_refactored.cu:78, transpose.cu:87-90) */
+  int bp_median;    /* NMEDFILT (definitions.h:39): odd window of the median
+                       filter every bandpass correction applies to the
+                       bandpass before dividing by it (med_filter_bandpass,
+                       median_filter.cpp:85-107); 1 (the reference's value,
+                       the default) is the identity; at most 63 and below
+                       nchan */
 } hella_params;
 
 #define HELLA_INPUT_U8_TF 0

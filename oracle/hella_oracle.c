@@ -275,16 +275,15 @@ float ho_median_filter(const float *in, float *out, int size, int window) {
   return median_filter(in, out, size, window);
 }
 
-#define NMEDFILT 1 /* definitions.h:39 */
-
 /* bandpass_correct  flagger.cu:244-269 (+ med_filter_bandpass
- * median_filter.cpp:85-107 with NMEDFILT=1, the identity) and divide_by_bp
+ * median_filter.cpp:85-107 with a window of NMEDFILT, definitions.h:39: 1,
+ * the identity, in the reference's build) and divide_by_bp
  * flagger.cu:180-194. */
-static void bandpass_correct(uint16_t *d, int nchan, int w, float *bp_out) {
+static void bandpass_correct(uint16_t *d, int nchan, int w, float *bp_out, int nmedfilt) {
   float *bp = (float *)malloc(sizeof(float) * (size_t)nchan);
   float *mbp = (float *)malloc(sizeof(float) * (size_t)nchan);
   calc_bandpass_new(d, nchan, w, bp);
-  median_filter(bp, mbp, nchan, NMEDFILT);
+  median_filter(bp, mbp, nchan, nmedfilt > 1 ? nmedfilt : 1);
 #pragma omp parallel for schedule(static) num_threads(nthreads())
   for (int c = 0; c < nchan; ++c) {
     uint16_t *row = d + (size_t)c * w;
@@ -387,7 +386,7 @@ static void apply_scrunch(uint16_t *d, uint16_t *mask, uint16_t *smooth,
                           int flag, int ts, const ho_flag_params *fp,
                           float *flagspec, float *bp_out, float *ts_out,
                           float *mean_o, float *std_o) {
-  bandpass_correct(d, nchan, w, bp_out);
+  bandpass_correct(d, nchan, w, bp_out, fp->bp_median);
   if (ts == 1) ts_correct(d, nchan, w, ts_out);
   normalize_data(d, nchan, w, mean_o, std_o);
   if (flag == 1) {
@@ -465,7 +464,7 @@ static void flag_plane(uint16_t *d, int w, int nchan, const ho_flag_params *fp, 
   float *bp = (float *)malloc(sizeof(float) * (size_t)nchan);
   float m1, s1, m2, s2;
   /* bandpass_flag  flagger.cu:216-242 */
-  bandpass_correct(d, nchan, w, tr ? tr->bp1 : NULL);
+  bandpass_correct(d, nchan, w, tr ? tr->bp1 : NULL, fp->bp_median);
   normalize_data(d, nchan, w, &m1, &s1);
   calc_bandpass_new(d, nchan, w, bp);
   for (int c = 0; c < nchan; ++c) {

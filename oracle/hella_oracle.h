@@ -96,6 +96,8 @@ typedef struct {
   int flag1, flag2;         /* FLAG1 / FLAG2 channel range (scrunch path) */
   int nscrunch;
   const ho_scrunch *scrunches;
+  int bp_median;            /* NMEDFILT (definitions.h:39): odd window of the
+                               bandpass median filter; 0 or 1 = identity */
 } ho_flag_params;
 
 /* Intermediate values of one beam's flagging, for stage-level checks. */

@@ -23,7 +23,7 @@ class Scrunch(C.Structure):
 
 class FlagParams(C.Structure):
     _fields_ = [("spec_min", C.c_float), ("spec_max", C.c_float), ("flag1", C.c_int), ("flag2", C.c_int),
-                ("nscrunch", C.c_int), ("scrunches", C.POINTER(Scrunch))]
+                ("nscrunch", C.c_int), ("scrunches", C.POINTER(Scrunch)), ("bp_median", C.c_int)]
 
 
 class FlagTrace(C.Structure):
@@ -167,9 +167,9 @@ def stddev_f32(x: np.ndarray, width=None):
     return float(m[0]), float(s)
 
 
-def flag_params(spec_min=-0.05, spec_max=0.15, flag1=-1, flag2=-1, scrunches=()):
+def flag_params(spec_min=-0.05, spec_max=0.15, flag1=-1, flag2=-1, scrunches=(), bp_median=1):
     arr = (Scrunch * max(1, len(scrunches)))(*[Scrunch(t, f, n, th) for (t, f, th, n) in scrunches])
-    fp = FlagParams(spec_min, spec_max, flag1, flag2, len(scrunches), arr)
+    fp = FlagParams(spec_min, spec_max, flag1, flag2, len(scrunches), arr, bp_median)
     fp._keep = arr
     return fp
 
@@ -242,8 +242,8 @@ class Pipeline:
 
     def __init__(self, *, nchan, nbeam, gulp, tsamp, plan_dt, f0, df, dm_min, dm_max, dm_tol, ti_us, wmin,
                  wmax, snr, max_giants=10000, anchor=0, spec_min=-0.05, spec_max=0.15, flag1=-1, flag2=-1,
-                 scrunches=()):
-        self.fp = flag_params(spec_min, spec_max, flag1, flag2, scrunches)
+                 scrunches=(), bp_median=1):
+        self.fp = flag_params(spec_min, spec_max, flag1, flag2, scrunches, bp_median)
         self.p = Params(nchan, nbeam, gulp, tsamp, plan_dt, f0, df, dm_min, dm_max, dm_tol, ti_us, wmin, wmax,
                         snr, max_giants, anchor, self.fp)
         self.L = lib()
@@ -265,7 +265,7 @@ class Pipeline:
                    dm_tol=p["dm_tol"], ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
                    max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
                    spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15), flag1=p.get("flag1", -1),
-                   flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()))
+                   flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()), bp_median=p.get("bp_median", 1))
 
     def close(self):
         if getattr(self, "h", None):

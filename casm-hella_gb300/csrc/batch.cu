@@ -526,6 +526,7 @@ hg::SmoothArgs smooth_args(hella_batch *b, int w0, int nw) {
   a.tap_off = b->d_tapoff;
   a.tap_n = b->d_tapn;
   a.snr = b->p.snr;
+  a.nogate = b->p.always_find_peaks != 0;
   return a;
 }
 

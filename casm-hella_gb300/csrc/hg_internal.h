@@ -221,6 +221,7 @@ struct SmoothArgs {
   float snr;
   int split;                // FIR: first width of the second width group
                             // (w0 + nw: one group); set by smooth_planes
+  int nogate;               // peaks whatever sigma0 (DEBUG_ALWAYS_FIND_PEAKS)
 };
 // Shared memory of the FIR launch.
 size_t fir_smem_bytes(const SmoothArgs &a);

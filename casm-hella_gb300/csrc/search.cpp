@@ -74,6 +74,7 @@ hella_status validate_params(const hella_params *p) {
   if (p->input_format != HELLA_INPUT_U8_TF && p->input_format != HELLA_INPUT_F16_FT) return HELLA_ERR_INVALID_ARG;
   if (p->bp_median < 1 || p->bp_median % 2 == 0 || p->bp_median > hg::kMaxBpMedian || p->bp_median >= p->nchan)
     return HELLA_ERR_INVALID_ARG;
+  if (p->always_find_peaks != 0 && p->always_find_peaks != 1) return HELLA_ERR_INVALID_ARG;
   for (int i = 0; i < p->nscrunch; ++i) {
     const hella_scrunch &sc = p->scrunch[i];
     if (sc.tscrunch < 1 || sc.tscrunch > kMaxScrunch || sc.fscrunch < 1 || sc.fscrunch > kMaxScrunch ||
@@ -188,6 +189,7 @@ hg::SmoothArgs smooth_args(hella_ctx *c) {
   a.tap_off = c->d_tapoff;
   a.tap_n = c->d_tapn;
   a.snr = c->p.snr;
+  a.nogate = c->p.always_find_peaks != 0;
   return a;
 }
 

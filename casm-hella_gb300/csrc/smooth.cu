@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(kFin) k_stat_finish(SmoothArgs a) {
       const float sig = __fsqrt_rn(s);
       B.gate[1] = sig;
       B.gate[2] = __fmul_rn(a.snr, sig);
-      B.gate[3] = (sig < 5 && (double)sig > 0.1) ? 1.f : 0.f;  // definitions.h:71-72
+      B.gate[3] = (a.nogate || (sig < 5 && (double)sig > 0.1)) ? 1.f : 0.f;  // definitions.h:66,71-72
     }
   } else {
     const float sd = __fsqrt_rn(s), mean = B.stats[b * 4 + 0];

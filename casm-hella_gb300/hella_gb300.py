@@ -49,6 +49,7 @@ class HellaParams(C.Structure):
         ("nscrunch", C.c_int), ("scrunch", HellaScrunch * HELLA_MAX_SCRUNCH),
         ("max_giants", C.c_int), ("beam0", C.c_int), ("smooth_anchor", C.c_int), ("device", C.c_int),
         ("hbm_budget", C.c_size_t), ("autotune", C.c_int), ("input_format", C.c_int), ("bp_median", C.c_int),
+        ("always_find_peaks", C.c_int),
     ]
 
 

@@ -94,6 +94,10 @@ typedef struct {
                        median_filter.cpp:85-107); 1 (the reference's value,
                        the default) is the identity; at most 63 and below
                        nchan */
+  int always_find_peaks; /* DEBUG_ALWAYS_FIND_PEAKS (definitions.h:66,
+                       peaks.cu:60): 1 searches for peaks whatever the
+                       width-0 deviation; 0 (the reference's value, the
+                       default) only when 0.1 < sigma0 < 5 */
 } hella_params;
 
 #define HELLA_INPUT_U8_TF 0

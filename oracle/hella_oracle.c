@@ -615,12 +615,18 @@ int ho_smooth_normalise(const float *dd, int ndms, int ntime_dd,
 
 int ho_find_peaks(const float *boxes, int nbox, int ndms, int ntime_out,
                   float snr, int beam, int cap, ho_cand *out, float *sigma0) {
+  return ho_find_peaks_gate(boxes, nbox, ndms, ntime_out, snr, beam, cap, out, sigma0, 1);
+}
+
+int ho_find_peaks_gate(const float *boxes, int nbox, int ndms, int ntime_out,
+                       float snr, int beam, int cap, ho_cand *out, float *sigma0,
+                       int gate) {
   int h = ndms - 2;
   size_t plane = (size_t)h * ntime_out;
   float mean = 0.f;
   float s0 = ho_stddev_f32(boxes, ntime_out, h, (size_t)ntime_out, &mean);
   if (sigma0) *sigma0 = s0;
-  if (!(s0 < 5 && s0 > 0.1)) return 0; /* definitions.h:71-72, peaks.cu:60 */
+  if (gate && !(s0 < 5 && s0 > 0.1)) return 0; /* definitions.h:66,71-72, peaks.cu:60 */
   float thr = snr * s0;
   int n = 0;
   for (int b = 0; b < nbox && n < cap; ++b) {
@@ -739,7 +745,8 @@ int ho_search_window(const ho_pipeline *pl, const uint8_t *window, int beam,
                 (size_t)pl->ntime_dd, pl->ntime_dd);
   ho_smooth_normalise(dd, pl->ndms, pl->ntime_dd, (size_t)pl->ntime_dd, p->wmin, p->wmax,
                       p->smooth_anchor, p->gulp, bx, mean_out, std_out);
-  int n = ho_find_peaks(bx, pl->nbox, pl->ndms, p->gulp, p->snr, beam, cap, cands, sigma0);
+  int n = ho_find_peaks_gate(bx, pl->nbox, pl->ndms, p->gulp, p->snr, beam, cap, cands, sigma0,
+                             !p->always_find_peaks);
   if (!dd_out) free(dd);
   if (!boxes_out) free(bx);
   return n;

@@ -180,6 +180,10 @@ typedef struct {
  * (0.1 < sigma < 5); every sample above snr*sigma, width-major then DM row
  * then time, until `cap` candidates.  Returns the number written; *sigma0
  * receives the gate value. */
+/* As ho_find_peaks; gate = 0 skips the sigma0 gate (DEBUG_ALWAYS_FIND_PEAKS). */
+int ho_find_peaks_gate(const float *boxes, int nbox, int ndms, int ntime_out,
+                       float snr, int beam, int cap, ho_cand *out, float *sigma0,
+                       int gate);
 int ho_find_peaks(const float *boxes, int nbox, int ndms, int ntime_out,
                   float snr, int beam, int cap, ho_cand *out, float *sigma0);
 
@@ -199,6 +203,7 @@ typedef struct {
   int max_giants;  /* MAX_GIANTS = 10000 */
   int smooth_anchor;
   ho_flag_params flag;
+  int always_find_peaks; /* DEBUG_ALWAYS_FIND_PEAKS (definitions.h:66): skip the sigma0 gate */
 } ho_params;
 
 typedef struct ho_pipeline ho_pipeline;

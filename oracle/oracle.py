@@ -37,7 +37,7 @@ class Params(C.Structure):
                 ("plan_dt", C.c_double), ("f0_mhz", C.c_double), ("df_mhz", C.c_double),
                 ("dm_min", C.c_float), ("dm_max", C.c_float), ("dm_tol", C.c_float), ("ti_us", C.c_float),
                 ("wmin", C.c_int), ("wmax", C.c_int), ("snr", C.c_float), ("max_giants", C.c_int),
-                ("smooth_anchor", C.c_int), ("flag", FlagParams)]
+                ("smooth_anchor", C.c_int), ("flag", FlagParams), ("always_find_peaks", C.c_int)]
 
 
 class Cand(C.Structure):
@@ -242,10 +242,10 @@ class Pipeline:
 
     def __init__(self, *, nchan, nbeam, gulp, tsamp, plan_dt, f0, df, dm_min, dm_max, dm_tol, ti_us, wmin,
                  wmax, snr, max_giants=10000, anchor=0, spec_min=-0.05, spec_max=0.15, flag1=-1, flag2=-1,
-                 scrunches=(), bp_median=1):
+                 scrunches=(), bp_median=1, always_find_peaks=0):
         self.fp = flag_params(spec_min, spec_max, flag1, flag2, scrunches, bp_median)
         self.p = Params(nchan, nbeam, gulp, tsamp, plan_dt, f0, df, dm_min, dm_max, dm_tol, ti_us, wmin, wmax,
-                        snr, max_giants, anchor, self.fp)
+                        snr, max_giants, anchor, self.fp, always_find_peaks)
         self.L = lib()
         self.h = self.L.ho_pipeline_create(C.byref(self.p))
         if not self.h:
@@ -265,7 +265,8 @@ class Pipeline:
                    dm_tol=p["dm_tol"], ti_us=p["ti_us"], wmin=p["width_min"], wmax=p["width_max"], snr=p["snr"],
                    max_giants=p.get("max_giants", 10000), anchor=p.get("smooth_anchor", 1),
                    spec_min=p.get("spec_min", -0.05), spec_max=p.get("spec_max", 0.15), flag1=p.get("flag1", -1),
-                   flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()), bp_median=p.get("bp_median", 1))
+                   flag2=p.get("flag2", -1), scrunches=p.get("scrunches", ()), bp_median=p.get("bp_median", 1),
+                   always_find_peaks=p.get("always_find_peaks", 0))
 
     def close(self):
         if getattr(self, "h", None):
@@ -360,10 +361,14 @@ def smooth_normalise(dd: np.ndarray, wmin: int, wmax: int, ntime_out: int, ancho
     return boxes, mean, std
 
 
-def find_peaks(boxes: np.ndarray, snr: float, beam: int = 0, cap: int = 10000):
+def find_peaks(boxes: np.ndarray, snr: float, beam: int = 0, cap: int = 10000, gate: bool = True):
     boxes = np.ascontiguousarray(boxes, np.float32)
     nbox, h, nt = boxes.shape
     out = np.zeros(cap, CAND_DTYPE)
     s0 = np.zeros(1, np.float32)
-    n = lib().ho_find_peaks(boxes.ctypes.data, nbox, h + 2, nt, snr, beam, cap, out.ctypes.data, s0.ctypes.data)
+    L = lib()
+    L.ho_find_peaks_gate.restype = C.c_int
+    L.ho_find_peaks_gate.argtypes = [_VP, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, _VP, _VP, C.c_int]
+    n = L.ho_find_peaks_gate(boxes.ctypes.data, nbox, h + 2, nt, snr, beam, cap, out.ctypes.data, s0.ctypes.data,
+                             int(gate))
     return out[:n], float(s0[0])

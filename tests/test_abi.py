@@ -97,7 +97,8 @@ def test_search_rejects_bad_params(hella):
     L = hella.lib()
     h = C.c_void_p()
     for bad in (dict(nchan=100), dict(gulp=100), dict(width_max=1), dict(dm_tol=1.0), dict(smooth_anchor=3),
-                dict(bp_median=0), dict(bp_median=4), dict(bp_median=65), dict(nchan=32, bp_median=33)):
+                dict(bp_median=0), dict(bp_median=4), dict(bp_median=65), dict(nchan=32, bp_median=33),
+                dict(always_find_peaks=2)):
         p = hella.default_params(**bad)
         assert L.hella_create(C.byref(h), C.byref(p)) == 1
     assert L.hella_status_string(6) == b"hbm budget exceeded"

@@ -317,3 +317,22 @@ def test_plain_config_full_size(hella, oracle):
     assert searched and len(got)
     best = got[np.argmax(got["snr"])]
     assert abs(s.dm_list()[best["dm_idx"]] - 300.0) < 2.0
+
+
+def test_always_find_peaks_switch(hella, oracle):
+    """DEBUG_ALWAYS_FIND_PEAKS (definitions.h:66) as `always_find_peaks`: a
+    gulp loop with the gate off gives the oracle's candidates with its gate
+    off (here sigma0 is near 1, so also the gated ones)."""
+    params, sky = synth.config_plain(seed=19, nchan=128, gulp=2048, dm_max=200.0)
+    params["always_find_peaks"] = 1
+    sky.bursts[0].amp *= 3
+    s = _search(hella, params)
+    pl = oracle_pipeline(oracle, params)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        x = sky.gulp(g, params["gulp"])[None]
+        got, sg = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert sg == so and cands_equal(got, want), (g, len(got), len(want))
+        total += len(got)
+    assert total > 0

@@ -278,3 +278,15 @@ def test_pipeline_killmask_drops_channels(oracle):
     with pytest.raises(ValueError):
         pk.set_killmask(2, km)
 
+
+
+def test_peak_gate_and_its_switch(oracle):
+    """find_peaks searches only when the width-0 plane's deviation sigma0 lies
+    in (0.1, 5) (peaks.cu:60, definitions.h:71-72); with the gate off
+    (DEBUG_ALWAYS_FIND_PEAKS) it searches at SNR x sigma0 whatever sigma0."""
+    rng = np.random.default_rng(3)
+    boxes = (rng.standard_normal((2, 10, 512)) * 7.0).astype(np.float32)  # sigma0 about 7
+    c, s0 = oracle.find_peaks(boxes, 2.0)
+    assert s0 > 5 and len(c) == 0
+    c, s0 = oracle.find_peaks(boxes, 2.0, gate=False)
+    assert len(c) > 0 and np.all(c["snr"] > 2.0 * np.float32(s0))

@@ -39,6 +39,14 @@ def test_batch_equals_independent_runs(hella, use_graph, wpp):
     _compare(hella, params, ceilings, kill, skies, widths_per_pass=wpp, use_graph=use_graph)
 
 
+def test_batch_with_median_window_and_gate_off(hella, oracle):
+    """The runtime NMEDFILT and DEBUG_ALWAYS_FIND_PEAKS reach every beam of
+    the batch: equal to single-beam contexts and oracle pipelines with them."""
+    params, ceilings, kill, skies = _setup(seed=47)
+    params.update(bp_median=5, always_find_peaks=1)
+    _compare(hella, params, ceilings, kill, skies, oracle=oracle)
+
+
 def test_batch_killmask_extremes(hella, oracle):
     """Beams that kill every channel, all but one, none, every other one,
     and the first 8 (a whole staging step): each beam sums only its own

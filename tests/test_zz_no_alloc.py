@@ -18,7 +18,9 @@ def _plan(hella, nchan=256, dm_max=150.0):
     return plan
 
 
-def test_noalloc_matches_execute_adv_twice(hella):
+def test_noalloc_matches_execute_adv_twice(hella, oracle):
+    """Two calls in a row, each on new data, equal to hdd_execute_adv on the
+    same device buffers and, as integer sums, to the oracle's brute force."""
     torch = pytest.importorskip("torch")
     L = hella.lib()
     plan = _plan(hella)
@@ -37,6 +39,8 @@ def test_noalloc_matches_execute_adv_twice(hella):
         torch.cuda.synchronize()
         # integer sums in fp32: the tolerance the parity tests use for them is exact equality
         assert torch.equal(got, ref), call
+        want = oracle.dedisperse(x.cpu().numpy(), plan.delay_table(), nout=nout)
+        assert np.array_equal(got.cpu().numpy(), want), call
     plan.close()
 
 

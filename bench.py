@@ -40,10 +40,13 @@ METRIC = "real-time factor (beam·s searched per s) at DM 0–2000; p99 gulp lat
 UNIT = "beam·s/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one timed dedispersion launch of the full
 # single beam, by tile shape (hella_tuning fields in order), from single-pass ncu captures of
-# those two metrics on `bench.py --steps 1 --warmup 3 --no-cpu-baseline --no-batched`
-# (profiles/k_dedisp_full_beam.md).  A shape without a capture reports null.
+# those two metrics on `bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-batched` (one pass
+# each, checked on the 512-channel case first).  A shape without a capture reports null.
 DEDISP_TRAFFIC = {
     (0, 4, 8, 0, 8, 2): 8.664e9,  # 16-trial tiles, 8-channel stages, groups of 8, add mode 2: 7.99 + 0.673 GB
+    # pair rows (add mode 5), 8 pairs a stage, groups of 8: k_pair_build 0.707 read + 5.78 written,
+    # k_pair_sum 13.18 read + 0.654 written (profiles/k_pair_full_beam.md)
+    (16, 4, 16, 0, 8, 5): 20.32e9,
 }
 
 
@@ -72,8 +75,9 @@ def args_():
                          "cases that profiling captures use")
     ap.add_argument("--dm-max", type=float, default=0.0,
                     help="DM ceiling of the full workload (0: 2000); a small profiling case")
-    ap.add_argument("--add-mode", type=int, default=2,
-                    help="dedispersion add mode of the single-beam workloads (hella_tuning.add_mode)")
+    ap.add_argument("--add-mode", type=int, default=5,
+                    help="dedispersion add mode of the single-beam workloads (hella_tuning.add_mode; 5: pair "
+                         "rows, else the channel-by-channel kernel's pipe balance)")
     return ap.parse_args()
 
 
@@ -274,16 +278,19 @@ def main():
         step(gi, False)
         gi += 1
     torch.cuda.synchronize()
-    # dedispersion tile shape: 16-trial tiles (the deepest staging that fits), DM tiles walked
-    # in groups of 8 per time tile, odd lanes and load addresses by multiply-adds (add mode 2).
-    # Modes 2 and 3 measured 19.40 ms on the full beam against 19.49 for mode 0; the autotuner
-    # lands within 0.3 % of that with groups of 2-4, which read 12 GB from DRAM per launch
-    # against 8.1 GB for groups of 8.
-    s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode))
-    try:
-        s.time_dedisp(None, 1)
-    except hg.HellaError:  # DM lists whose tiles hold fewer than 8 trials take add mode 0
-        s.set_tuning(hg.HellaTuning(0, 4, 8, 0, 8, 0))
+    # dedispersion: pair rows (add mode 5: 16-trial tiles, 8 pairs a stage, the deepest staging
+    # that fits, DM tiles walked in groups of 8 per time tile), 12.6 ms on the full beam against
+    # 19.4 ms for the channel-by-channel kernel's best shape (add mode 2, multiply-add odd lanes
+    # and addresses).  DM lists whose tiles do not fit the mode fall back to 2, then 0.
+    shapes = [hg.HellaTuning(16, 4, 16, 0, 8, 5)] if a.add_mode == 5 else []
+    shapes += [hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode if a.add_mode != 5 else 2), hg.HellaTuning(0, 4, 8, 0, 8, 0)]
+    for shape in shapes:
+        try:
+            s.set_tuning(shape)
+            s.time_dedisp(None, 1)
+            break
+        except hg.HellaError:
+            continue
 
     # ---------------- device-resident timing
     clocks = Clocks(local)
@@ -346,17 +353,29 @@ def main():
     nact = nch
     adds = float(info.ndms) * nact * info.ntime_dd
     dd_t = float(np.mean(dd_ms)) / 1e3
-    peak_int = hg.int_add_peak(local)
+    peak_int = 2 * hg.int_add_peak(local) / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
+    peak_smem = hg.smem_read_peak(local) / 1e12
     achieved = adds / dd_t / 1e12
-    peak = 2 * peak_int / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
-    roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4),
-            "traffic": DEDISP_TRAFFIC.get(tuple(s.get_tuning().as_dict().values()))
-            if a.workload == "full" and not (a.nchan or a.dm_max) else None,
-            "traffic_unit": "bytes per launch (ncu)",
-            "kernel": "k_dedisp", "work_per_launch": f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples",
-            "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
-            "ms_per_launch": round(dd_t * 1e3, 3)}
+    pairs = s.get_tuning().add_mode == 5
+    work = f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples"
+    traffic = (DEDISP_TRAFFIC.get(tuple(s.get_tuning().as_dict().values()))
+               if a.workload == "full" and not (a.nchan or a.dm_max) else None)
+    int_roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak_int, 3), "unit": "Tadd/s",
+                "frac": round(achieved / peak_int, 4),
+                "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 "
+                               "lanes: the byte-splitting channel-by-channel kernel's bound",
+                "ms_per_launch": round(dd_t * 1e3, 3)}
+    smem_roof = {"bound": "smem", "achieved": round(achieved, 3), "peak": round(peak_smem, 3), "unit": "TB/s",
+                 "frac": round(achieved / peak_smem, 4),
+                 "peak_source": "measured: conflict-free 16-byte shared-memory loads on all SMs "
+                                "(hella_smem_read_peak); one byte read per channel-sample",
+                 "ms_per_launch": round(dd_t * 1e3, 3)}
+    if pairs:  # the pair rows' sums read one shared-memory byte per channel-sample: that is their bound
+        roof = dict(smem_roof, kernel="k_pair_build + k_pair_sum (add mode 5, timed together)",
+                    work_per_launch=work, traffic=traffic, traffic_unit="bytes per launch (ncu, both kernels)")
+    else:
+        roof = dict(int_roof, kernel="k_dedisp", work_per_launch=work, traffic=traffic,
+                    traffic_unit="bytes per launch (ncu)")
     hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") if (
         ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
     sm_t = float(np.mean(sm_ms)) / 1e3
@@ -374,12 +393,13 @@ def main():
                     "frac": round(flag_bytes / fl_t / 1e9 / hbm, 4), "ms_per_launch": round(fl_t * 1e3, 3),
                     "note": "9 u8 passes + 1 u8 write per sample"},
     }
+    extra["dedisp_int32" if pairs else "dedisp_smem"] = int_roof if pairs else smem_roof
     if roof["traffic"]:
         # the dominant kernel against HBM: its measured DRAM traffic over the launch time
         gbs = roof["traffic"] / dd_t / 1e9
         extra["dedisp_hbm"] = {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
                                "frac": round(gbs / hbm, 4), "ms_per_launch": round(dd_t * 1e3, 3),
-                               "note": "k_dedisp's ncu DRAM bytes per launch over its time: not HBM bound"}
+                               "note": "the dedispersion's ncu DRAM bytes per launch over its time"}
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": a.steps,

@@ -431,7 +431,7 @@ hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
 
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
-  if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  if (!hg::tuning_ok(t) || t.add_mode == 5) return HELLA_ERR_INVALID_ARG;  // add mode 5: single beam only
   if (t.add_mode == 4) {
     // sub-band sums over every channel: a beam's killed channels are packed
     // as zeros, so the plan's tables serve every beam
@@ -992,7 +992,7 @@ hella_status hella_batch_get_tuning(const hella_batch *b, hella_tuning *t) {
 }
 
 hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t) {
-  if (!b || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
+  if (!b || !t || !hg::tuning_ok(*t) || t->add_mode == 5) return HELLA_ERR_INVALID_ARG;
   if (any_busy(b)) return HELLA_ERR_STATE;
   b->tune = *t;
   b->tune.samples_per_thread = 4;

@@ -35,6 +35,7 @@
 // beam run in groups of `group` DM tiles per time tile, so that blocks
 // resident together read overlapping windows of the ring through L2.
 #include "hg_internal.h"
+#include "hg_ptx.h"
 
 #include <algorithm>
 #include <type_traits>
@@ -44,7 +45,6 @@ namespace {
 
 constexpr int S = kPackS;
 constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
-constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr int row_words(int max_spread) {
   // sh + S + spread words (sh < 4) rounded up to 16-byte chunks
@@ -61,76 +61,6 @@ __host__ __device__ constexpr int buf_words(int dpt, int cc, int rowstride) {
 }
 size_t smem_bytes(int dpt, int cc, int rowstride, int nbuf) {
   return kBarBytes + (size_t)nbuf * buf_words(dpt, cc, rowstride) * 4;
-}
-
-// ---- shared-memory, mbarrier and bulk-copy primitives (PTX ISA 8.x)
-__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
-  uint32_t v;
-  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
-  return v;
-}
-__device__ __forceinline__ int4 lds128(uint32_t addr) {
-  int4 v;
-  asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "r"(addr));
-  return v;
-}
-__device__ __forceinline__ void sts32(uint32_t addr, int v) {
-  asm volatile("st.shared.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// Waits for the phase of `parity` to complete; false after ~kWaitCycles.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try(bar, parity)) return true;
-  const long long t0 = clock64();
-  for (;;) {
-    if (mbar_try(bar, parity)) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-// Global -> shared bulk copy of `bytes` (multiple of 16, both ends 16-byte
-// aligned) completing on `bar`.
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
 }
 
 // Where one work item reads and writes.
@@ -1092,6 +1022,7 @@ cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
   if (a.R % 4 != 0 || a.ntt <= 0 || a.group <= 0 || a.nbeam <= 0) return cudaErrorInvalidValue;
   if (a.varied && !a.beams) return cudaErrorInvalidValue;
   if (a.mode == 4) return launch_sub(a, s);
+  if (a.mode == 5) return dedisperse_pairs(a, s);
   switch (a.dpt) {
     case 16: return launch_cc<16>(a, s);
     case 8: return launch_cc<8>(a, s);
@@ -1176,6 +1107,31 @@ __global__ void k_int_add_peak(unsigned *out, int iters, unsigned seed) {
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 ^ y0 ^ x1 ^ y1 ^ x2 ^ y2 ^ x3 ^ y3;
 }
+
+// Shared-memory reads: every thread reads 16 bytes a load, a warp 512
+// consecutive bytes (no bank conflicts), from a 32 KiB block buffer, at an
+// address that moves with the iteration.  The loads are volatile, so none
+// is merged with another or moved out of the loop, and their values are
+// folded into the stored result.
+__global__ void __launch_bounds__(256) k_smem_read_peak(unsigned *out, int iters) {
+  __shared__ __align__(16) uint32_t buf[8192];
+  for (int i = threadIdx.x; i < 8192; i += blockDim.x) buf[i] = i * 2654435761u;
+  __syncthreads();
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(buf);
+  uint32_t acc = 0;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t w = ((threadIdx.x + (uint32_t)k * 256u + (uint32_t)i * 32u) & 2047u) * 16u;
+      int4 v;
+      asm volatile("ld.volatile.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+                   : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                   : "r"(base + w));
+      acc += (uint32_t)(v.x ^ v.y) + (uint32_t)(v.z ^ v.w);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
 }  // namespace
 
 void count_launches(unsigned n) { g_launches += n; }
@@ -1209,5 +1165,34 @@ extern "C" hella_status hella_int_add_peak(int device, double *adds_per_s) {
   cudaEventDestroy(e1);
   cudaFree(out);
   *adds_per_s = (double)blocks * threads * iters * 16 * 8 / (best * 1e-3);
+  return st;
+}
+
+extern "C" hella_status hella_smem_read_peak(int device, double *bytes_per_s) {
+  if (!bytes_per_s) return HELLA_ERR_INVALID_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return HELLA_ERR_CUDA;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const int blocks = sms * 6, threads = 256, iters = 2048;
+  unsigned *out = nullptr;
+  cudaEvent_t e0, e1;
+  if (cudaMalloc(&out, (size_t)blocks * threads * 4) != cudaSuccess) return HELLA_ERR_ALLOC;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0);
+    hg::k_smem_read_peak<<<blocks, threads>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  const hella_status st = cudaGetLastError() == cudaSuccess ? HELLA_OK : HELLA_ERR_CUDA;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *bytes_per_s = (double)blocks * threads * iters * 8 * 16 / (best * 1e-3);
   return st;
 }

@@ -36,6 +36,30 @@ hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out
 // Points a launch at add-mode-4 tables (16-trial tiles; items must be counted
 // for that tile size).
 void use_sub_tables(DedispArgs *a, const SubDeviceTables &t);
+// Add-mode-5 tables (pair rows) for trials [first, first + count) over the
+// plan's active channels with cc pairs per stage and ntt time tiles: host
+// copy cached per range and shape, device copy and row buffer set up on
+// first use.
+struct PairDeviceTables {
+  const int4 *rinfo;
+  const long long *roff;
+  const int *rwords;
+  const int *prow;
+  const int2 *prange;
+  const int4 *rec;
+  const int *tile_st;
+  uint32_t *rows;
+  int npair, span, stage, nact, cc;
+  long npos;
+};
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, PairDeviceTables *out);
+// Frees the add-mode-5 device tables and rows (set up again on next use).
+void plan_pair_release(hdd_plan p);
+// Device bytes those tables and their rows take (builds the host copy).
+hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, size_t *bytes);
+// Points a single-beam launch at add-mode-5 tables (16-trial tiles; items
+// must be counted for that tile size).
+void use_pair_tables(DedispArgs *a, const PairDeviceTables &t);
 // Launch arguments for one beam over a plan's device tables.
 DedispArgs single_beam_args(const DeviceTables &tb, const uint32_t *packed, long R, long win0,
                             int dm_first, int dm_count, int nout, float *out, long out_stride,

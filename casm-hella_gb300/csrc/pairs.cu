@@ -1,0 +1,477 @@
+// pairs.cu -- add mode 5 of the dedispersion: pair rows (hg_internal.h).
+//
+// Same exact integer sums as k_dedisp (out[d][t] = sum over active channels
+// c of x[c][t + delay(c, d)], the operation casm-hella obtains from
+// dedisp_execute_adv, src/hella/src/dedisperse.cpp:17-48), computed in two
+// launches per window:
+//
+// k_pair_build: one block per (pair, 4096 window positions).  Both
+//   channels' packed words of the chunk (plus the pair's relative-delay
+//   range for the second channel) are read from the ring once into shared
+//   memory as 16-bit lanes (bytes 0 and 2 of a packed word are the samples
+//   p and p + 512), then every row of the pair is written from them:
+//   row(r)[p] = x[c0][p] + x[c1][p + r].  Reads are the ring once per
+//   pair; writes the rows, coalesced.
+//
+// k_pair_sum: the persistent staging pipeline of k_dedisp (work item =
+//   16-trial tile x 1024 output samples, stages issued warp by warp with
+//   cp.async.bulk onto full/empty mbarriers, every wait bounded) over stage
+//   records instead of channels.  A stage stages the windows of the rows
+//   its pairs use (lane i copies row i) and the record's trial offsets;
+//   thread j then reads, per pair and trial, the words j and j + 256 of
+//   the trial's window: four output samples (j, j+256, j+512, j+768) in two
+//   SWAR registers of 16-bit lanes, two pairs per three-input add.  The
+//   lanes are widened into 32-bit totals every kPairLaneCap pairs.
+//
+// Per pair and trial the inner loop is two shared loads and one add for
+// eight channel-samples, against two loads, four byte permutes and two adds
+// in k_dedisp; shared-memory traffic stays one byte per channel-sample, so
+// the sums are bound by shared-memory bandwidth rather than ALU issue.
+#include "hg_internal.h"
+#include "hg_ptx.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace hg {
+namespace {
+
+constexpr int S = kPackS;
+constexpr int kTileSamples = 4 * S;
+constexpr int kBuildCH = 4096;            // window positions per build block
+constexpr int kBarHdr = 448;              // full[4] | empty[4] | per-warp staging cursors
+constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
+constexpr int kMaxBuf = 4;
+
+__host__ __device__ constexpr int stage_hdr_bytes(int cc) { return 16 + cc * kPairDPT * 4; }
+
+__global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
+  extern __shared__ uint32_t sm[];
+  const int k = blockIdx.y;
+  const long P0 = (long)blockIdx.x * kBuildCH;
+  const int r0 = a.pair_prow[k], r1 = a.pair_prow[k + 1];
+  bool any = false;
+  for (int r = r0; r < r1; ++r) {
+    const int4 in = a.pair_rinfo[r];
+    if (P0 < (long)in.w + a.pair_rwords[r] && P0 + kBuildCH > (long)in.w) any = true;
+  }
+  if (!any) return;
+  const int4 i0 = a.pair_rinfo[r0];
+  const int2 rr = a.pair_prange[k];
+  const long R = a.R;
+  uint32_t *sa = sm, *sb = sm + kBuildCH;
+  // window position p lies at ring word (win0 + p) mod R
+  const uint32_t *pa = a.one.packed + (size_t)i0.x * R;
+  const long ba = (a.one.win0 + P0) % R;
+  for (int i = threadIdx.x; i < kBuildCH; i += blockDim.x) {
+    long p = ba + i;
+    if (p >= R) p %= R;
+    sa[i] = __byte_perm(pa[p], 0u, 0x4240);
+  }
+  if (i0.y >= 0) {
+    const uint32_t *pb = a.one.packed + (size_t)i0.y * R;
+    long bb = (a.one.win0 + P0 + rr.x) % R;
+    if (bb < 0) bb += R;
+    const int nb = kBuildCH + rr.y - rr.x;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      long p = bb + i;
+      if (p >= R) p %= R;
+      sb[i] = __byte_perm(pb[p], 0u, 0x4240);
+    }
+  }
+  __syncthreads();
+  for (int r = r0; r < r1; ++r) {
+    const int4 in = a.pair_rinfo[r];
+    const long lo = max(P0, (long)in.w), hi = min(P0 + kBuildCH, (long)in.w + a.pair_rwords[r]);
+    uint32_t *dst = a.pair_rows + a.pair_roff[r] - in.w;
+    if (i0.y >= 0) {
+      const int sh = in.z - rr.x;
+      for (long p = lo + threadIdx.x; p < hi; p += blockDim.x) dst[p] = sa[p - P0] + sb[p - P0 + sh];
+    } else {
+      for (long p = lo + threadIdx.x; p < hi; p += blockDim.x) dst[p] = sa[p - P0];
+    }
+  }
+}
+
+__device__ __forceinline__ void pair_item(const DedispArgs &a, int ntiles, int l, int *tile, int *tt) {
+  const int per_group = a.group * a.ntt;
+  const int g = l / per_group, r = l - g * per_group;
+  const int gsz = min(a.group, ntiles - g * a.group);
+  *tt = r / gsz;
+  *tile = g * a.group + (r - *tt * gsz);
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, int bufbytes, int nbuf) {
+  extern __shared__ __align__(128) uint32_t smem[];
+  constexpr int DPT = kPairDPT;
+  constexpr int NWARP = kDedispThreads / 32;
+  constexpr int HB = stage_hdr_bytes(CC);
+  const int REC = pair_rec_int4(CC);
+  const int ntiles = (a.one.dm_count + DPT - 1) / DPT;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  auto full_of = [&](int b) { return sbase + 8u * b; };
+  auto empty_of = [&](int b) { return sbase + 32u + 8u * b; };
+  auto buf_of = [&](int b) { return sbase + kBarHdr + (uint32_t)b * (uint32_t)bufbytes; };
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // the stage a warp stages next: stage st of the nst stages of block-local item k
+  struct Cursor {
+    int k, st, s0, nst, t0;
+  };
+  static_assert(64 + NWARP * sizeof(Cursor) <= kBarHdr, "staging cursors");
+  Cursor *cur = reinterpret_cast<Cursor *>(reinterpret_cast<char *>(smem) + 64) + warp;
+  if (tid == 0) {
+    for (int b = 0; b < nbuf; ++b) {
+      mbar_init(full_of(b), 32);      // every lane of the staging warp arrives once per fill
+      mbar_init(empty_of(b), NWARP);  // one arrival per warp once it is done reading
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= a.nitems) return;
+
+  auto load_item = [&](int k) -> bool {  // lane 0
+    const int item = blockIdx.x + k * gridDim.x;
+    if (item >= a.nitems) return false;
+    int tile, tt;
+    pair_item(a, ntiles, item, &tile, &tt);
+    const int s0 = a.pair_tile_st[tile];
+    *cur = Cursor{k, 0, s0, a.pair_tile_st[tile + 1] - s0, tt * kTileSamples};
+    return true;
+  };
+  auto advance = [&](int n) -> bool {  // lane 0
+    int st = cur->st + n;
+    while (st >= cur->nst) {
+      st -= cur->nst;
+      if (!load_item(cur->k + 1)) return false;
+    }
+    cur->st = st;
+    return true;
+  };
+  unsigned g_next = (unsigned)warp;  // next stage this warp stages
+  bool p_done;                       // no stage left for this warp
+  {
+    int more = 0;
+    if (lane == 0) more = load_item(0) && advance(warp);
+    p_done = !__shfl_sync(0xffffffffu, more, 0);
+    __syncwarp();
+  }
+  auto issue = [&](bool block, bool *timed_out) -> bool {
+    const unsigned g = g_next;
+    const int b = (int)(g % (unsigned)nbuf);
+    if (g >= (unsigned)nbuf) {
+      const uint32_t par = ((g / nbuf) - 1u) & 1u;
+      if (block) {
+        if (!mbar_wait(empty_of(b), par)) {
+          *timed_out = true;
+          return false;
+        }
+      } else if (!mbar_test(empty_of(b), par)) {
+        return false;
+      }
+    }
+    const int4 *r = a.pair_rec + (size_t)(cur->s0 + cur->st) * REC;
+    const int t0 = cur->t0;
+    const int nrows = __ldg(&r->y);
+    const uint32_t bar = full_of(b);
+    fence_proxy_async();
+    if (lane < nrows) {
+      const int4 rw = __ldg(r + 1 + CC * DPT / 4 + lane);  // {first word lo, hi, words, byte slot}
+      const long start = (long)(((unsigned long long)(unsigned)rw.y << 32) | (unsigned)rw.x);
+      const uint32_t nb = (uint32_t)rw.z * 4u;
+      mbar_arrive_tx(bar, nb + (lane == 0 ? (uint32_t)HB : 0u));
+      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, a.pair_rows + start + t0, nb, bar);
+      if (lane == 0) bulk_g2s(buf_of(b), r, HB, bar);
+    } else {
+      mbar_arrive(bar);
+    }
+    __syncwarp();
+    g_next += NWARP;
+    int more = 0;
+    if (lane == 0) more = advance(NWARP);
+    p_done = !__shfl_sync(0xffffffffu, more, 0);
+    __syncwarp();
+    return true;
+  };
+  // After a wait ran out: record it, let this warp's copies land, end.
+  auto fail = [&](unsigned gs_c) {
+    if (lane == 0 && a.err) atomicOr(a.err, 1);
+    for (unsigned g = gs_c; g < g_next; ++g)
+      if (g % NWARP == (unsigned)warp) mbar_wait(full_of((int)(g % nbuf)), (g / nbuf) & 1u);
+  };
+
+  unsigned gs_c = 0;  // stages consumed
+  for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    int tile, tt;
+    pair_item(a, ntiles, item, &tile, &tt);
+    const int nstage = a.pair_tile_st[tile + 1] - a.pair_tile_st[tile];
+    uint32_t acc_a[DPT], acc_b[DPT], tot[DPT][4];  // acc_a: samples j, j+512; acc_b: j+256, j+768
+#pragma unroll
+    for (int m = 0; m < DPT; ++m) {
+      acc_a[m] = acc_b[m] = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) tot[m][k] = 0u;
+    }
+    int npairs = 0;  // pairs in the 16-bit lanes
+    for (int st = 0; st < nstage; ++st) {
+      {
+        bool to = false;
+        while (!p_done && g_next < gs_c + nbuf)
+          if (!issue(g_next <= gs_c, &to)) break;
+        if (to) return fail(gs_c);
+      }
+      const int b = (int)(gs_c % (unsigned)nbuf);
+      if (!mbar_wait(full_of(b), (gs_c / nbuf) & 1u)) return fail(gs_c);
+      const uint32_t hb = buf_of(b), ob = hb + 16u, rb = hb + (uint32_t)HB + (uint32_t)tid * 4u;
+      const int ng = (int)lds32(hb);
+      auto add2 = [&](int i) {  // pairs i and i + 1
+#pragma unroll
+        for (int q = 0; q < DPT / 4; ++q) {
+          const int4 x1 = lds128(ob + (uint32_t)(i * DPT + 4 * q) * 4u);
+          const int4 x2 = lds128(ob + (uint32_t)((i + 1) * DPT + 4 * q) * 4u);
+          const int o1[4] = {x1.x, x1.y, x1.z, x1.w}, o2[4] = {x2.x, x2.y, x2.z, x2.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int m = 4 * q + j;
+            const uint32_t p1 = rb + (uint32_t)o1[j], p2 = rb + (uint32_t)o2[j];
+            acc_a[m] += lds32(p1) + lds32(p2);
+            acc_b[m] += lds32(p1 + 4u * S) + lds32(p2 + 4u * S);
+          }
+        }
+      };
+      auto add1 = [&](int i) {
+#pragma unroll
+        for (int q = 0; q < DPT / 4; ++q) {
+          const int4 x1 = lds128(ob + (uint32_t)(i * DPT + 4 * q) * 4u);
+          const int o1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int m = 4 * q + j;
+            const uint32_t p1 = rb + (uint32_t)o1[j];
+            acc_a[m] += lds32(p1);
+            acc_b[m] += lds32(p1 + 4u * S);
+          }
+        }
+      };
+      if (ng == CC) {
+#pragma unroll
+        for (int i = 0; i < CC; i += 2) add2(i);
+      } else {
+        int i = 0;
+        for (; i + 1 < ng; i += 2) add2(i);
+        if (i < ng) add1(i);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty_of(b));  // this warp is done with buffer b
+      ++gs_c;
+      npairs += ng;
+      if (npairs + CC > kPairLaneCap) {
+#pragma unroll
+        for (int m = 0; m < DPT; ++m) {
+          tot[m][0] += acc_a[m] & 0xffffu;
+          tot[m][2] += acc_a[m] >> 16;
+          tot[m][1] += acc_b[m] & 0xffffu;
+          tot[m][3] += acc_b[m] >> 16;
+          acc_a[m] = acc_b[m] = 0u;
+        }
+        npairs = 0;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < DPT; ++m) {
+      tot[m][0] += acc_a[m] & 0xffffu;
+      tot[m][2] += acc_a[m] >> 16;
+      tot[m][1] += acc_b[m] & 0xffffu;
+      tot[m][3] += acc_b[m] >> 16;
+    }
+    const int t0 = tt * kTileSamples;
+#pragma unroll
+    for (int m = 0; m < DPT; ++m) {
+      const int i = tile * DPT + m;
+      if (i >= a.one.dm_count) break;
+      float *o = a.one.out + (size_t)i * a.out_stride;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int t = t0 + tid + k * S;
+        if (t < a.nout) o[t] = (float)tot[m][k];
+      }
+    }
+  }
+}
+
+template <int CC>
+cudaError_t launch_sum(const DedispArgs &a, cudaStream_t s) {
+  const int bufbytes = stage_hdr_bytes(CC) + a.pair_stage;
+  int nbuf = a.nbuf;
+  if (!nbuf) {  // deepest pipeline within the two-blocks budget, else two buffers
+    nbuf = 2;
+    for (int nb = kMaxBuf; nb >= 2; --nb)
+      if (kBarHdr + (size_t)nb * bufbytes <= kSmemBudget) {
+        nbuf = nb;
+        break;
+      }
+  }
+  if (nbuf < 2 || nbuf > kMaxBuf) return cudaErrorInvalidValue;
+  const size_t smem = kBarHdr + (size_t)nbuf * bufbytes;
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  auto kern = k_pair_sum<CC>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDedispThreads, smem)) != cudaSuccess)
+    return e;
+  const int grid = std::max(1, std::min(a.nitems, std::max(1, per_sm) * sms));
+  kern<<<grid, kDedispThreads, smem, s>>>(a, bufbytes, nbuf);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, int nact, int dm_first,
+                              int dm_count, int cc, int ntt) {
+  PairTables t;
+  t.cc = cc;
+  t.ntt = ntt;
+  t.ntiles = (dm_count + kPairDPT - 1) / kPairDPT;
+  t.npair = (nact + 1) / 2;
+  const int stage_max = pair_stage_budget(cc);
+  auto dl = [&](int d, int c) { return delays[(size_t)(dm_first + d) * nchan + c]; };
+  // rows: per pair, one per distinct relative delay, in increasing r
+  std::vector<int> row_of((size_t)dm_count * t.npair), rel(dm_count), u;
+  t.prow.assign(t.npair + 1, 0);
+  t.prange.resize(t.npair);
+  for (int k = 0; k < t.npair; ++k) {
+    const int c0 = chans[2 * k], c1 = 2 * k + 1 < nact ? chans[2 * k + 1] : -1;
+    for (int d = 0; d < dm_count; ++d) rel[d] = c1 >= 0 ? dl(d, c1) - dl(d, c0) : 0;
+    u = rel;
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    const int base = (int)t.rinfo.size();
+    for (int v : u) t.rinfo.push_back(make_int4(c0, c1, v, 1 << 30));
+    for (int d = 0; d < dm_count; ++d) {
+      const int id = base + (int)(std::lower_bound(u.begin(), u.end(), rel[d]) - u.begin());
+      row_of[(size_t)d * t.npair + k] = id;
+      t.rinfo[id].w = std::min(t.rinfo[id].w, dl(d, c0));
+    }
+    t.prange[k] = make_int2(u.front(), u.back());
+    t.max_span = std::max(t.max_span, u.back() - u.front());
+    t.prow[k + 1] = (int)t.rinfo.size();
+  }
+  t.nrows = (int)t.rinfo.size();
+  std::vector<long long> need(t.nrows, 0);
+  // stage records
+  const int REC = pair_rec_int4(cc);
+  const int offs0 = 4, rows0 = 4 + cc * kPairDPT;  // int positions in a record
+  std::vector<int> rec(REC * 4);
+  struct Fix {
+    size_t rec_int;  // int index of the row entry in t.rec
+    int row, bal;
+  };
+  std::vector<Fix> fixes;
+  std::vector<Fix> pending;
+  int ng = 0, nr = 0, bytes = 0;
+  auto flush = [&]() {
+    const size_t at = t.rec.size() * 4;
+    for (Fix f : pending) fixes.push_back(Fix{at + f.rec_int, f.row, f.bal});
+    pending.clear();
+    rec[0] = ng;
+    rec[1] = nr;
+    const size_t n0 = t.rec.size();
+    t.rec.resize(n0 + REC);
+    std::memcpy(&t.rec[n0], rec.data(), rec.size() * sizeof(int));
+    t.max_stage = std::max(t.max_stage, bytes);
+    std::fill(rec.begin(), rec.end(), 0);
+    ng = nr = bytes = 0;
+  };
+  int ids[kPairDPT], av[kPairDPT];
+  t.tile_st.push_back(0);
+  for (int i = 0; i < t.ntiles; ++i) {
+    const int d0 = i * kPairDPT, nt = std::min(kPairDPT, dm_count - d0);
+    for (int k = 0; k < t.npair; ++k) {
+      const int c0 = chans[2 * k];
+      int uid[kPairDPT], ub[kPairDPT], us[kPairDPT], nu = 0;
+      for (int m = 0; m < nt; ++m) {
+        ids[m] = row_of[(size_t)(d0 + m) * t.npair + k];
+        av[m] = dl(d0 + m, c0) - t.rinfo[ids[m]].w;
+        int j = 0;
+        while (j < nu && uid[j] != ids[m]) ++j;
+        if (j == nu) {
+          uid[nu] = ids[m];
+          ub[nu] = us[nu] = av[m];
+          ++nu;
+        } else {
+          ub[j] = std::min(ub[j], av[m]);
+          us[j] = std::max(us[j], av[m]);
+        }
+      }
+      int add = 0, bal[kPairDPT], nw[kPairDPT];
+      for (int j = 0; j < nu; ++j) {
+        const int sh = ub[j] & 3;
+        bal[j] = ub[j] - sh;
+        nw[j] = (2 * S + (us[j] - ub[j]) + sh + 3) / 4 * 4;
+        add += nw[j] * 4;
+      }
+      if (ng > 0 && (ng == cc || nr + nu > kPairRowsMax || bytes + add > stage_max)) flush();
+      for (int j = 0; j < nu; ++j) {
+        const int slot = bytes;
+        for (int m = 0; m < nt; ++m)
+          if (ids[m] == uid[j]) rec[offs0 + ng * kPairDPT + m] = slot + (av[m] - bal[j]) * 4;
+        int *rw = &rec[rows0 + 4 * nr];
+        rw[2] = nw[j];
+        rw[3] = slot;
+        pending.push_back(Fix{(size_t)(rows0 + 4 * nr), uid[j], bal[j]});
+        need[uid[j]] = std::max(need[uid[j]], (long long)bal[j] + nw[j]);
+        ++nr;
+        bytes += nw[j] * 4;
+      }
+      ++ng;
+    }
+    if (ng > 0) flush();
+    t.tile_st.push_back((int)(t.rec.size() / REC));
+  }
+  // row lengths and offsets (multiples of 4 words: every copy starts 16-byte aligned)
+  t.roff.resize(t.nrows);
+  t.rwords.resize(t.nrows);
+  long long off = 0;
+  for (int r = 0; r < t.nrows; ++r) {
+    const long long w = ((long long)(ntt - 1) * kTileSamples + need[r] + 3) / 4 * 4;
+    t.roff[r] = off;
+    t.rwords[r] = (int)w;
+    off += w;
+    t.npos = std::max(t.npos, (long)(t.rinfo[r].w + w));
+  }
+  t.words = (long)off;
+  int *ri = reinterpret_cast<int *>(t.rec.data());
+  for (const Fix &f : fixes) {
+    const unsigned long long start = (unsigned long long)(t.roff[f.row] + f.bal);
+    ri[f.rec_int] = (int)(unsigned)(start & 0xffffffffull);
+    ri[f.rec_int + 1] = (int)(unsigned)(start >> 32);
+  }
+  return t;
+}
+
+cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
+  if (a.beams || a.dpt != kPairDPT || a.mode != 5 || !a.pair_rows || !a.pair_rec || !a.pair_tile_st ||
+      !a.pair_rinfo || !a.pair_roff || !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 ||
+      a.pair_npair > 65535 || a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0)
+    return cudaErrorInvalidValue;
+  if (a.R <= 0 || a.one.win0 < 0) return cudaErrorInvalidValue;
+  const size_t bsmem = (size_t)(2 * kBuildCH + a.pair_span) * 4;
+  if (bsmem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_pair_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
+  if (e != cudaSuccess) return e;
+  const dim3 grid((unsigned)((a.pair_npos + kBuildCH - 1) / kBuildCH), (unsigned)a.pair_npair);
+  k_pair_build<<<grid, 256, bsmem, s>>>(a);
+  count_launches(1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  switch (a.cc) {
+    case 4: return launch_sum<4>(a, s);
+    case 8: return launch_sum<8>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace hg

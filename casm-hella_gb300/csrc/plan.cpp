@@ -101,6 +101,17 @@ struct hdd_plan_struct {
   int2 *d_sindex = nullptr;
   int *d_spool = nullptr;
   size_t smeta_cap = 0, sindex_cap = 0, spool_cap = 0;
+  // add-mode-5 tables of the last DM range and shape used, host and device, and the rows
+  hg::PairTables pair;
+  int pair_first = -1, pair_count = -1, pair_cc = -1, pair_ntt = -1;
+  bool pair_on_device = false;
+  int4 *d_prinfo = nullptr, *d_prec = nullptr;
+  long long *d_proff = nullptr;
+  int *d_prwords = nullptr, *d_pprow = nullptr, *d_ptile = nullptr;
+  int2 *d_pprange = nullptr;
+  uint32_t *d_prows = nullptr;
+  size_t prinfo_cap = 0, prec_cap = 0, proff_cap = 0, prwords_cap = 0, pprow_cap = 0, ptile_cap = 0,
+         pprange_cap = 0, prows_cap = 0;
 };
 
 namespace {
@@ -112,6 +123,8 @@ void invalidate_tables(hdd_plan p) {
   p->tab_on_device = false;
   p->sub_first = p->sub_count = -1;
   p->sub_on_device = false;
+  p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = -1;
+  p->pair_on_device = false;
 }
 
 // Delays of the plan's DM list; max_delay is the largest of them (the last
@@ -239,6 +252,121 @@ hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out
   return HDD_NO_ERROR;
 }
 
+namespace {
+
+// Host pair tables of the range and shape, built when they differ from the cached ones.
+hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt) {
+  if (p->pair_first == first && p->pair_count == count && p->pair_cc == cc && p->pair_ntt == ntt)
+    return HDD_NO_ERROR;
+  try {
+    p->pair = dedisp_pair_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first, count,
+                                 cc, ntt);
+  } catch (const std::bad_alloc &) {
+    p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = -1;
+    return HDD_MEM_ALLOC_FAILED;
+  }
+  p->pair_first = first;
+  p->pair_count = count;
+  p->pair_cc = cc;
+  p->pair_ntt = ntt;
+  p->pair_on_device = false;
+  return HDD_NO_ERROR;
+}
+
+template <class T>
+size_t vbytes(const std::vector<T> &v) {
+  return std::max<size_t>(v.size(), 1) * sizeof(T);
+}
+
+}  // namespace
+
+hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, size_t *bytes) {
+  const hdd_error e = pair_host_tables(p, first, count, cc, ntt);
+  if (e != HDD_NO_ERROR) return e;
+  const PairTables &t = p->pair;
+  *bytes = vbytes(t.rinfo) + vbytes(t.roff) + vbytes(t.rwords) + vbytes(t.prow) + vbytes(t.prange) +
+           vbytes(t.rec) + vbytes(t.tile_st) + std::max<size_t>((size_t)t.words, 4) * 4;
+  return HDD_NO_ERROR;
+}
+
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, PairDeviceTables *out) {
+  hdd_error e = pair_host_tables(p, first, count, cc, ntt);
+  if (e != HDD_NO_ERROR) return e;
+  const PairTables &t = p->pair;
+  if (!p->pair_on_device) {
+    auto up = [&](void **d, size_t *cap, const void *src, size_t n) -> hdd_error {
+      hdd_error r = grow(d, cap, std::max<size_t>(n, 16));
+      if (r != HDD_NO_ERROR) return r;
+      if (n && cudaMemcpy(*d, src, n, cudaMemcpyHostToDevice) != cudaSuccess) return HDD_MEM_COPY_FAILED;
+      return HDD_NO_ERROR;
+    };
+    if ((e = up((void **)&p->d_prinfo, &p->prinfo_cap, t.rinfo.data(), t.rinfo.size() * sizeof(int4))) !=
+            HDD_NO_ERROR ||
+        (e = up((void **)&p->d_proff, &p->proff_cap, t.roff.data(), t.roff.size() * sizeof(long long))) !=
+            HDD_NO_ERROR ||
+        (e = up((void **)&p->d_prwords, &p->prwords_cap, t.rwords.data(), t.rwords.size() * sizeof(int))) !=
+            HDD_NO_ERROR ||
+        (e = up((void **)&p->d_pprow, &p->pprow_cap, t.prow.data(), t.prow.size() * sizeof(int))) != HDD_NO_ERROR ||
+        (e = up((void **)&p->d_pprange, &p->pprange_cap, t.prange.data(), t.prange.size() * sizeof(int2))) !=
+            HDD_NO_ERROR ||
+        (e = up((void **)&p->d_prec, &p->prec_cap, t.rec.data(), t.rec.size() * sizeof(int4))) != HDD_NO_ERROR ||
+        (e = up((void **)&p->d_ptile, &p->ptile_cap, t.tile_st.data(), t.tile_st.size() * sizeof(int))) !=
+            HDD_NO_ERROR ||
+        (e = grow((void **)&p->d_prows, &p->prows_cap, std::max<size_t>((size_t)t.words, 4) * 4)) != HDD_NO_ERROR)
+      return e;
+    p->pair_on_device = true;
+  }
+  out->rinfo = p->d_prinfo;
+  out->roff = p->d_proff;
+  out->rwords = p->d_prwords;
+  out->prow = p->d_pprow;
+  out->prange = p->d_pprange;
+  out->rec = p->d_prec;
+  out->tile_st = p->d_ptile;
+  out->rows = p->d_prows;
+  out->npair = t.npair;
+  out->span = t.max_span;
+  out->stage = t.max_stage;
+  out->nact = (int)p->chans.size();
+  out->cc = t.cc;
+  out->npos = t.npos;
+  return HDD_NO_ERROR;
+}
+
+void plan_pair_release(hdd_plan p) {
+  if (!p || !(p->d_prinfo || p->d_prows)) return;
+  cudaSetDevice(p->device);
+  void **bufs[] = {(void **)&p->d_prinfo, (void **)&p->d_proff, (void **)&p->d_prwords, (void **)&p->d_pprow,
+                   (void **)&p->d_pprange, (void **)&p->d_prec, (void **)&p->d_ptile, (void **)&p->d_prows};
+  size_t *caps[] = {&p->prinfo_cap, &p->proff_cap, &p->prwords_cap, &p->pprow_cap,
+                    &p->pprange_cap, &p->prec_cap, &p->ptile_cap, &p->prows_cap};
+  for (int i = 0; i < 8; ++i) {
+    cudaFree(*bufs[i]);
+    *bufs[i] = nullptr;
+    *caps[i] = 0;
+  }
+  p->pair_on_device = false;
+}
+
+void use_pair_tables(DedispArgs *a, const PairDeviceTables &t) {
+  a->dpt = kPairDPT;
+  a->mode = 5;
+  a->cc = t.cc;
+  a->nact = t.nact;
+  a->pair_rinfo = t.rinfo;
+  a->pair_roff = t.roff;
+  a->pair_rwords = t.rwords;
+  a->pair_prow = t.prow;
+  a->pair_prange = t.prange;
+  a->pair_rec = t.rec;
+  a->pair_tile_st = t.tile_st;
+  a->pair_rows = t.rows;
+  a->pair_npair = t.npair;
+  a->pair_span = t.span;
+  a->pair_stage = t.stage;
+  a->pair_npos = t.npos;
+}
+
 void use_sub_tables(DedispArgs *a, const SubDeviceTables &t) {
   a->dpt = kSubDPT;
   a->mode = 4;
@@ -331,6 +459,14 @@ void hdd_destroy_plan(hdd_plan p) {
   cudaFree(p->d_smeta);
   cudaFree(p->d_sindex);
   cudaFree(p->d_spool);
+  cudaFree(p->d_prinfo);
+  cudaFree(p->d_proff);
+  cudaFree(p->d_prwords);
+  cudaFree(p->d_pprow);
+  cudaFree(p->d_pprange);
+  cudaFree(p->d_prec);
+  cudaFree(p->d_ptile);
+  cudaFree(p->d_prows);
   delete p;
 }
 

@@ -223,6 +223,7 @@ def lib() -> C.CDLL:
     _sig(L, "hella_autotune", C.c_int, [_VP, C.c_int, C.POINTER(HellaTuning), C.POINTER(C.c_float)])
     _sig(L, "hella_fp16_selftest", C.c_int, [C.c_int, C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint32)])
     _sig(L, "hella_int_add_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)])
+    _sig(L, "hella_smem_read_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)])
     _sig(L, "hella_kernel_launches", C.c_ulonglong, [])
     _lib = L
     return L
@@ -264,6 +265,13 @@ def int_add_peak(device: int = 0) -> float:
     """Measured 32-bit integer adds per second (register-only chains)."""
     v = C.c_double()
     _chk(lib().hella_int_add_peak(device, C.byref(v)))
+    return v.value
+
+
+def smem_read_peak(device: int = 0) -> float:
+    """Measured shared-memory bytes per second read by all SMs (16-byte loads)."""
+    v = C.c_double()
+    _chk(lib().hella_smem_read_peak(device, C.byref(v)))
     return v.value
 
 

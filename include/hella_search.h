@@ -120,7 +120,15 @@ typedef struct {
                              4: sums of four adjacent channels built once
                              per delay pattern of a 16-trial tile and shared
                              by its trials (dm_per_block 0 or 16; chan_chunk
-                             and the per-beam killmask tables unused) */
+                             and the per-beam killmask tables unused);
+                             5: pair rows -- adjacent active channels summed
+                             once per window and relative delay into rows
+                             in device memory, then summed by 16-trial tiles
+                             (dm_per_block 0 or 16; chan_chunk/2 pairs per
+                             stage).  Single-beam contexts only; the rows
+                             (about 5.8 GB for 2048 channels, DM 0-2000,
+                             gulp 65536) are held while the mode is set and
+                             count against hbm_budget (HELLA_ERR_BUDGET) */
 } hella_tuning;
 
 /* Derived sizes (casm_hella_refactored.cu:184-224). */
@@ -310,6 +318,10 @@ hella_status hella_fp16_selftest(int device, unsigned long long *mismatches,
  * events); the dedispersion roofline's denominator.  Synchronous.
  * hella_kernel_launches: kernels this library has launched in this process. */
 hella_status hella_int_add_peak(int device, double *adds_per_s);
+/* hella_smem_read_peak: shared-memory bytes per second the device's SMs
+ * read with conflict-free 16-byte loads (all SMs, measured), the ceiling of
+ * add mode 5's summing kernel, which reads one byte per channel-sample. */
+hella_status hella_smem_read_peak(int device, double *bytes_per_s);
 unsigned long long hella_kernel_launches(void);
 
 #ifdef __cplusplus

@@ -1,0 +1,184 @@
+"""Add mode 5 of the dedispersion: pair rows.  Adjacent active channels are
+summed once per window and relative delay into rows in HBM, and each
+16-trial tile sums the rows of its trials' relative delays.  Integer sums
+in any grouping are the same numbers, so every plane must be bit-exact
+against the oracle's channel-by-channel sums and against the other add
+modes: odd active-channel counts (the last channel alone), pairs of
+non-adjacent active channels, a single active channel, both stage widths,
+the ring's window wrapping over gulps, the full single beam, and the
+tuner choosing among all modes."""
+import numpy as np
+import pytest
+
+import synth
+from helpers import cands_equal, oracle_pipeline
+
+pytestmark = pytest.mark.gpu
+
+MODE5 = (0, 4, 8, 0, 8, 5)     # dm_per_block, samples, chan_chunk, stages, group, add_mode
+MODE5_16 = (16, 4, 16, 0, 8, 5)
+
+
+def _window(hella, params, sky, killmask=None, gulps=None):
+    s = hella.Search(hella.default_params(**params))
+    if killmask is not None:
+        s.set_killmask(killmask)
+    n = s.info.min_gulp + 1 if gulps is None else gulps
+    for g in range(n):
+        s.clear_peaks()
+        s.load_gulp(sky.gulp(g, params["gulp"])[None])
+        s.fast_flagger()
+        if g < n - 1:
+            s.rewind()
+    return s
+
+
+def _oracle_plane(oracle, params, s, win, killmask):
+    f32 = lambda v: float(np.float32(v))
+    delays = oracle.dm_delays(s.dm_list(), oracle.delay_table(params["nchan"], f32(params["plan_dt"]),
+                                                              f32(params["f0_mhz"]), f32(params["df_mhz"])))
+    return oracle.dedisperse(win, delays, killmask=killmask, nout=s.info.ntime_dd)
+
+
+@pytest.mark.parametrize("shape", [MODE5, MODE5_16])
+@pytest.mark.parametrize("nchan,dm_max,kill", [(128, 400.0, 0), (160, 300.0, 1), (256, 1000.0, 2), (96, 60.0, 3),
+                                               (64, 800.0, 4)])
+def test_pair_rows_planes_exact(hella, oracle, nchan, dm_max, kill, shape):
+    params, sky = synth.config_plain(seed=50 + kill, nchan=nchan, gulp=2048, dm_max=dm_max)
+    km = None
+    rng = np.random.default_rng(kill)
+    if kill == 1:  # 17 killed channels: 143 active, the last one alone
+        km = np.ones(nchan, np.int32)
+        km[rng.choice(nchan, 17, replace=False)] = 0
+    elif kill == 2:  # runs and single channels: pairs of channels far apart, an odd count
+        km = (rng.random(nchan) > 0.1).astype(np.int32)
+        km[40:57] = 0
+        while int(km.sum()) % 2 != 1:
+            km[int(rng.integers(0, nchan))] = 0
+    elif kill == 3:  # a single active channel
+        km = np.zeros(nchan, np.int32)
+        km[33] = 1
+    elif kill == 4:  # every other channel killed: every pair spans a killed one
+        km = np.zeros(nchan, np.int32)
+        km[::2] = 1
+    s = _window(hella, params, sky, km)
+    win = s.copy_window(0)
+    s.set_tuning(hella.HellaTuning(*shape))
+    s.dedisperse(0)
+    got = s.copy_dedisp()
+    want = _oracle_plane(oracle, params, s, win, km)
+    assert np.array_equal(got, want)
+    s.set_tuning(hella.HellaTuning(0, 4, 8, 0, 8, 0))
+    s.dedisperse(0)
+    assert np.array_equal(s.copy_dedisp(), got)
+    s.close()
+
+
+def test_pair_rows_window_wraps(hella, oracle):
+    """Windows that start anywhere in the ring (gulps 3..6 of a ring of
+    about two gulps): every window's plane exact."""
+    params, sky = synth.config_plain(seed=61, nchan=96, gulp=1024, dm_max=200.0)
+    s = hella.Search(hella.default_params(**params))
+    s.set_tuning(hella.HellaTuning(*MODE5))
+    checked = 0
+    for g in range(s.info.min_gulp + 5):
+        s.clear_peaks()
+        s.load_gulp(sky.gulp(g, params["gulp"])[None])
+        s.fast_flagger()
+        if g >= s.info.min_gulp:
+            win = s.copy_window(0)
+            s.dedisperse(0)
+            assert np.array_equal(s.copy_dedisp(), _oracle_plane(oracle, params, s, win, None)), g
+            checked += 1
+        s.rewind()
+    assert checked == 5
+    s.close()
+
+
+def test_pair_rows_gulp_loop_candidates(hella, oracle):
+    params, sky = synth.config_plain(seed=15, nchan=160, gulp=2048, dm_max=300.0)
+    sky.bursts[0].amp *= 4
+    km = (np.random.default_rng(15).random(params["nchan"]) > 0.15).astype(np.int32)
+    s = hella.Search(hella.default_params(**params))
+    s.set_killmask(km)
+    s.set_tuning(hella.HellaTuning(*MODE5))
+    pl = oracle_pipeline(oracle, params)
+    pl.set_killmask(0, km)
+    total = 0
+    for g in range(pl.min_gulp + 2):
+        x = sky.gulp(g, params["gulp"])[None]
+        got, sg = s.process_gulp(x)
+        want, so = pl.gulp_step(x)
+        assert sg == so and cands_equal(got, want), (g, len(got), len(want))
+        total += len(got)
+    assert total > 0
+    s.close()
+
+
+def test_pair_rows_full_beam(hella):
+    """The full single beam (2048 channels, 2501 trials): the whole plane
+    identical to add mode 2's, both stage widths, and faster."""
+    params, sky = synth.config_full(seed=2)
+    s = _window(hella, params, sky)
+    s.set_tuning(hella.HellaTuning(0, 4, 8, 0, 8, 2))
+    s.dedisperse(0)
+    ref = s.copy_dedisp()
+    for shape in (MODE5, MODE5_16):
+        s.set_tuning(hella.HellaTuning(*shape))
+        s.dedisperse(0)
+        assert np.array_equal(s.copy_dedisp(), ref), shape
+    ms5 = s.time_dedisp(hella.HellaTuning(*MODE5_16), 3)
+    ms2 = s.time_dedisp(hella.HellaTuning(0, 4, 8, 0, 8, 2), 3)
+    print(f"full beam dedispersion: add mode 5 {ms5:.2f} ms (rows built and summed), add mode 2 {ms2:.2f} ms")
+    assert ms5 < ms2
+    s.close()
+
+
+def test_pair_rows_budget_and_batch(hella):
+    """The rows count against the HBM budget: a budget with room for the
+    context but not for the rows refuses the mode, and the tuner passes
+    over it; the batched context does not take the mode."""
+    params, sky = synth.config_plain(seed=16, nchan=256, gulp=2048, dm_max=1000.0)
+    held = hella.Search(hella.default_params(**params))
+    dev = held.info.device_bytes
+    held.close()
+    s = hella.Search(hella.default_params(**params, hbm_budget=1 << 40))
+    s.set_tuning(hella.HellaTuning(*MODE5))
+    s.time_dedisp(None, 1)  # an ample budget
+    s.close()
+    # the smallest budget (to 64 KiB) the context is created with
+    lo, hi = 0, dev + (64 << 20)
+    while hi - lo > (64 << 10):
+        mid = (lo + hi) // 2
+        try:
+            hella.Search(hella.default_params(**params, hbm_budget=mid)).close()
+            hi = mid
+        except hella.HellaError:
+            lo = mid
+    ntt = -(-(params["gulp"] + params["width_max"]) // 1024)
+    rows_at_least = (params["nchan"] // 2) * ((ntt - 1) * 1024 + 512) * 4  # one row per pair
+    assert hi - dev < rows_at_least, (hi, dev)
+    s = hella.Search(hella.default_params(**params, hbm_budget=hi))
+    s.set_tuning(hella.HellaTuning(*MODE5))
+    with pytest.raises(hella.HellaError):
+        s.time_dedisp(None, 1)
+    best, _ = s.autotune(1)
+    assert best.add_mode != 5
+    s.close()
+    bt = hella.Batch(hella.default_params(**dict(params, nbeam=2)))
+    with pytest.raises(hella.HellaError):
+        bt.set_tuning(hella.HellaTuning(*MODE5))
+    bt.close()
+
+
+def test_autotune_keeps_sums_exact(hella, oracle):
+    """The tuner times every add mode including pair rows; whatever it keeps
+    gives the oracle's plane."""
+    params, sky = synth.config_plain(seed=17, nchan=256, gulp=4096, dm_max=1000.0)
+    s = _window(hella, params, sky)
+    win = s.copy_window(0)
+    best, ms = s.autotune(1)
+    assert s.get_tuning().add_mode == best.add_mode and ms > 0
+    s.dedisperse(0)
+    assert np.array_equal(s.copy_dedisp(), _oracle_plane(oracle, params, s, win, None))
+    s.close()

@@ -169,6 +169,8 @@ struct hella_batch {
   hg::TableJob *d_bjobs = nullptr;
   size_t bmeta_cap = 0, boff_cap = 0, bchans_cap = 0, bjobs_cap = 0;
   int btab_dpt = -1, btab_cc = -1;  // tile shape of the per-beam tables; -1: rebuild
+  int *d_prend = nullptr;         // add mode 5: [nbeam][npair] end of the rows each beam builds
+  int prend_cc = -1;              // pairs per stage of the tables d_prend was made for; -1: remake
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
   std::vector<Lane> lanes;
   std::deque<int> queue;          // lanes in submission order
@@ -336,6 +338,7 @@ hella_status upload_layout(hella_batch *b) {
   CK(cudaMemcpy(b->d_join, b->join.data(), nb * 4, cudaMemcpyHostToDevice));
   b->items_dpt = -1;  // dedisp_args re-uploads the beams with their item prefix
   b->btab_dpt = -1;   // and rebuilds the per-beam tables
+  b->prend_cc = -1;   // and the per-beam row ends of add mode 5
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;
 }
@@ -431,7 +434,59 @@ hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
 
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
-  if (!hg::tuning_ok(t) || t.add_mode == 5) return HELLA_ERR_INVALID_ARG;  // add mode 5: single beam only
+  if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
+  if (t.add_mode == 5) {
+    // pair rows over every channel (killed channels are packed as zeros), built
+    // and summed beam by beam in one row buffer; a beam builds the rows its
+    // own trials use
+    const int cc = t.chan_chunk / 2, ntt = hg::dedisp_time_tiles(b->z.ntime_dd);
+    if (b->p.hbm_budget) {
+      size_t bytes = 0;
+      if (hg::plan_pair_bytes(b->plan, 0, b->z.ndms_all, cc, ntt, &bytes) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
+      if (b->dev_bytes + bytes + (size_t)b->nbeam * b->p.nchan * 2 > b->p.hbm_budget) return HELLA_ERR_BUDGET;
+    }
+    hg::PairDeviceTables pt;
+    const hdd_error he = hg::plan_pair_tables(b->plan, 0, b->z.ndms_all, cc, ntt, &pt);
+    if (he == HDD_MEM_ALLOC_FAILED) return HELLA_ERR_ALLOC;
+    if (he != HDD_NO_ERROR || pt.nact != b->p.nchan) return HELLA_ERR_DEDISP;  // the plan keeps every channel
+    hella_status s;
+    if (!b->d_prend && (s = dalloc(b, (void **)&b->d_prend, (size_t)b->nbeam * pt.npair * 4)) != HELLA_OK)
+      return s;
+    if (b->prend_cc != cc) {
+      std::vector<int> ends((size_t)b->nbeam * pt.npair);
+      for (int i = 0; i < b->nbeam; ++i)
+        if (hg::plan_pair_row_ends(b->plan, b->dbeams[i].dm_count, &ends[(size_t)i * pt.npair]) != HDD_NO_ERROR)
+          return HELLA_ERR_DEDISP;
+      CK(cudaStreamSynchronize(b->stream));
+      CK(cudaMemcpy(b->d_prend, ends.data(), ends.size() * 4, cudaMemcpyHostToDevice));
+      b->prend_cc = cc;
+    }
+    hg::DedispArgs a{};
+    a.nbeam = 1;
+    a.ntt = ntt;
+    int items = 0;
+    for (int i = 0; i < b->nbeam; ++i) {
+      b->dbeams[i].item0 = items;
+      items += hg::dedisp_items(b->dbeams[i].dm_count, hg::kPairDPT, ntt);
+    }
+    if (b->items_dpt != hg::kPairDPT) {
+      CK(cudaStreamSynchronize(b->stream));
+      CK(cudaMemcpy(b->d_dbeams, b->dbeams.data(), sizeof(hg::DedispBeam) * b->nbeam, cudaMemcpyHostToDevice));
+      b->items_dpt = hg::kPairDPT;
+    }
+    a.nitems = items;
+    a.group = t.group;
+    a.R = b->z.R;
+    a.dm_first = 0;
+    a.nout = b->z.ntime_dd;
+    a.out_stride = b->z.ntime_dd;
+    a.nbuf = t.stages;
+    a.unit = 1;
+    a.err = b->d_err;
+    hg::use_pair_tables(&a, pt);
+    *out = a;
+    return HELLA_OK;
+  }
   if (t.add_mode == 4) {
     // sub-band sums over every channel: a beam's killed channels are packed
     // as zeros, so the plan's tables serve every beam
@@ -508,6 +563,32 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
   return HELLA_OK;
 }
 
+// The dedispersion of every beam: one persistent launch, or (add mode 5)
+// the rows built and summed beam by beam, each launch reading its beam's
+// ring position from the device.
+hella_status dedisperse_beams(hella_batch *b, const hg::DedispArgs &da) {
+  if (da.mode != 5) {
+    CK(hg::dedisperse(da, b->stream));
+    return HELLA_OK;
+  }
+  for (int i = 0; i < b->nbeam; ++i) {
+    const int n = b->dbeams[i].dm_count;
+    if (n <= 0) continue;
+    hg::DedispArgs a = da;
+    a.beams = b->d_dbeams + i;
+    a.one = b->dbeams[i];
+    a.nitems = hg::dedisp_items(n, hg::kPairDPT, da.ntt);
+    a.pair_rend = b->d_prend + (size_t)i * da.pair_npair;
+    const cudaError_t e = hg::dedisperse(a, b->stream);
+    if (e == cudaErrorInvalidValue) {  // the DM list's stages do not fit this kernel's staging
+      cudaGetLastError();
+      return HELLA_ERR_INVALID_ARG;
+    }
+    CK(e);
+  }
+  return HELLA_OK;
+}
+
 hg::SmoothArgs smooth_args(hella_batch *b, int w0, int nw) {
   hg::SmoothArgs a{};
   a.beams = b->d_sbeams;
@@ -540,7 +621,8 @@ hella_status enqueue_gulp(hella_batch *b, const hg::DedispArgs &da, Lane &l) {
   k_ew_bandpass<<<std::min(1024, (nb * nch + 255) / 256), 256, 0, b->stream>>>(
       b->fs.bp1, b->d_ew, b->d_member, b->d_join, b->d_pos, nb, nch, b->bp_alpha);
   CK(hg::pack_gulp_dev(b->d_plain, b->d_packed, nb, nch, b->z.R, b->p.gulp, b->d_pos, b->stream, b->d_keep));
-  if (da.nitems > 0) CK(hg::dedisperse(da, b->stream));
+  hella_status st;
+  if (da.nitems > 0 && (st = dedisperse_beams(b, da)) != HELLA_OK) return st;
   for (int w0 = 0; w0 < b->z.nbox; w0 += b->nwp) {
     const hg::SmoothArgs a = smooth_args(b, w0, std::min(b->nwp, b->z.nbox - w0));
     CK(hg::smooth_planes(a, b->stream));
@@ -584,10 +666,7 @@ hella_status time_shape(hella_batch *b, const hella_tuning &t, int reps, float *
   hella_status s = dedisp_args(b, t, &da);
   if (s != HELLA_OK) return s;
   if (da.nitems == 0) return HELLA_ERR_STATE;
-  s = hg::time_runs(b->stream, reps, [&]() -> hella_status {
-    CK(hg::dedisperse(da, b->stream));
-    return HELLA_OK;
-  }, ms);
+  s = hg::time_runs(b->stream, reps, [&]() -> hella_status { return dedisperse_beams(b, da); }, ms);
   if (s != HELLA_OK) return s;
   int err = 0;
   CK(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -606,6 +685,7 @@ hella_status autotune(hella_batch *b, int reps, hella_tuning *out, float *out_ms
       &best_ms);
   if (s != HELLA_OK) return s;
   b->tune = best;
+  if (best.add_mode != 5) hg::plan_pair_release(b->plan);  // the rows are only kept for add mode 5
   for (Lane &l : b->lanes) l.stale = true;
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
@@ -992,9 +1072,10 @@ hella_status hella_batch_get_tuning(const hella_batch *b, hella_tuning *t) {
 }
 
 hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t) {
-  if (!b || !t || !hg::tuning_ok(*t) || t->add_mode == 5) return HELLA_ERR_INVALID_ARG;
+  if (!b || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
   if (any_busy(b)) return HELLA_ERR_STATE;
   b->tune = *t;
+  if (t->add_mode != 5) hg::plan_pair_release(b->plan);
   b->tune.samples_per_thread = 4;
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;

@@ -146,6 +146,7 @@ struct DedispArgs {
   const int4 *pair_rec;
   const int *pair_tile_st;
   uint32_t *pair_rows;
+  const int *pair_rend;     // [npair] end of the rows to build per pair (null: all rows)
   int pair_npair, pair_span, pair_stage;
   long pair_npos;
 };
@@ -234,8 +235,14 @@ struct PairTables {
 // channels, cc pairs per stage (4 or 8), for ntt time tiles of output.
 PairTables dedisp_pair_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
                               int dm_first, int dm_count, int cc, int ntt);
-// Builds the rows, then sums them (two launches); `a` is a single-beam
-// launch with mode 5 and dpt 16.
+// Per pair, the end of the rows that trials [dm_first, dm_first + dm_count)
+// of the tables' DM list use (the rows of a pair are in increasing relative
+// delay; a beam with a lower DM ceiling builds the pair's first rows only).
+void pair_row_ends(const PairTables &t, const int *delays_host, int nchan, const int *chans_host, int nact,
+                   int dm_first, int dm_count, int *ends);
+// Builds the rows, then sums them (two launches); `a` is a launch with mode
+// 5 and dpt 16 over one beam: `one`, or beams[0] read on the device (the
+// batched context, whose ring positions the device advances).
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s);
 // Largest delay spread over the active channels of any dpt-trial tile.
 int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int nact,

@@ -57,6 +57,9 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, Pa
 void plan_pair_release(hdd_plan p);
 // Device bytes those tables and their rows take (builds the host copy).
 hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, size_t *bytes);
+// Per pair, the end of the rows that the first `count` trials use, for the
+// tables last set up from trial 0 (a beam whose DM ceiling cuts the list).
+hdd_error plan_pair_row_ends(hdd_plan p, int count, int *ends);
 // Points a single-beam launch at add-mode-5 tables (16-trial tiles; items
 // must be counted for that tile size).
 void use_pair_tables(DedispArgs *a, const PairDeviceTables &t);

@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
   const int k = blockIdx.y;
   const long P0 = (long)blockIdx.x * kBuildCH;
-  const int r0 = a.pair_prow[k], r1 = a.pair_prow[k + 1];
+  const DedispBeam bm = a.beams ? a.beams[0] : a.one;
+  const int r0 = a.pair_prow[k], r1 = a.pair_rend ? a.pair_rend[k] : a.pair_prow[k + 1];
   bool any = false;
   for (int r = r0; r < r1; ++r) {
     const int4 in = a.pair_rinfo[r];
@@ -61,16 +62,16 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   const long R = a.R;
   uint32_t *sa = sm, *sb = sm + kBuildCH;
   // window position p lies at ring word (win0 + p) mod R
-  const uint32_t *pa = a.one.packed + (size_t)i0.x * R;
-  const long ba = (a.one.win0 + P0) % R;
+  const uint32_t *pa = bm.packed + (size_t)i0.x * R;
+  const long ba = (bm.win0 + P0) % R;
   for (int i = threadIdx.x; i < kBuildCH; i += blockDim.x) {
     long p = ba + i;
     if (p >= R) p %= R;
     sa[i] = __byte_perm(pa[p], 0u, 0x4240);
   }
   if (i0.y >= 0) {
-    const uint32_t *pb = a.one.packed + (size_t)i0.y * R;
-    long bb = (a.one.win0 + P0 + rr.x) % R;
+    const uint32_t *pb = bm.packed + (size_t)i0.y * R;
+    long bb = (bm.win0 + P0 + rr.x) % R;
     if (bb < 0) bb += R;
     const int nb = kBuildCH + rr.y - rr.x;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -108,7 +109,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   constexpr int NWARP = kDedispThreads / 32;
   constexpr int HB = stage_hdr_bytes(CC);
   const int REC = pair_rec_int4(CC);
-  const int ntiles = (a.one.dm_count + DPT - 1) / DPT;
+  const DedispBeam bm = a.beams ? a.beams[0] : a.one;
+  const int ntiles = (bm.dm_count + DPT - 1) / DPT;
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   auto full_of = [&](int b) { return sbase + 8u * b; };
   auto empty_of = [&](int b) { return sbase + 32u + 8u * b; };
@@ -288,8 +290,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
 #pragma unroll
     for (int m = 0; m < DPT; ++m) {
       const int i = tile * DPT + m;
-      if (i >= a.one.dm_count) break;
-      float *o = a.one.out + (size_t)i * a.out_stride;
+      if (i >= bm.dm_count) break;
+      float *o = bm.out + (size_t)i * a.out_stride;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int t = t0 + tid + k * S;
@@ -453,12 +455,28 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
   return t;
 }
 
+void pair_row_ends(const PairTables &t, const int *delays, int nchan, const int *chans, int nact, int dm_first,
+                   int dm_count, int *ends) {
+  for (int k = 0; k < t.npair; ++k) {
+    const int c0 = chans[2 * k], c1 = 2 * k + 1 < nact ? chans[2 * k + 1] : -1;
+    int rmax = 0;
+    for (int d = 0; d < dm_count; ++d) {
+      const int *row = delays + (size_t)(dm_first + d) * nchan;
+      const int r = c1 >= 0 ? row[c1] - row[c0] : 0;
+      rmax = d == 0 ? r : std::max(rmax, r);
+    }
+    int e = t.prow[k];  // rows of a pair are in increasing r
+    while (e < t.prow[k + 1] && t.rinfo[e].z <= rmax) ++e;
+    ends[k] = dm_count > 0 ? e : t.prow[k];
+  }
+}
+
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
-  if (a.beams || a.dpt != kPairDPT || a.mode != 5 || !a.pair_rows || !a.pair_rec || !a.pair_tile_st ||
+  if ((a.beams && a.nbeam != 1) || a.dpt != kPairDPT || a.mode != 5 || !a.pair_rows || !a.pair_rec || !a.pair_tile_st ||
       !a.pair_rinfo || !a.pair_roff || !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 ||
       a.pair_npair > 65535 || a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0)
     return cudaErrorInvalidValue;
-  if (a.R <= 0 || a.one.win0 < 0) return cudaErrorInvalidValue;
+  if (a.R <= 0 || (!a.beams && a.one.win0 < 0)) return cudaErrorInvalidValue;
   const size_t bsmem = (size_t)(2 * kBuildCH + a.pair_span) * 4;
   if (bsmem > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_pair_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);

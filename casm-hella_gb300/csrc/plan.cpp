@@ -348,6 +348,12 @@ void plan_pair_release(hdd_plan p) {
   p->pair_on_device = false;
 }
 
+hdd_error plan_pair_row_ends(hdd_plan p, int count, int *ends) {
+  if (p->pair_first != 0 || count > p->pair_count) return HDD_UNKNOWN_ERROR;
+  pair_row_ends(p->pair, p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), 0, count, ends);
+  return HDD_NO_ERROR;
+}
+
 void use_pair_tables(DedispArgs *a, const PairDeviceTables &t) {
   a->dpt = kPairDPT;
   a->mode = 5;

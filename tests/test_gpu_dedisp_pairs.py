@@ -137,7 +137,7 @@ def test_pair_rows_full_beam(hella):
 def test_pair_rows_budget_and_batch(hella):
     """The rows count against the HBM budget: a budget with room for the
     context but not for the rows refuses the mode, and the tuner passes
-    over it; the batched context does not take the mode."""
+    over it."""
     params, sky = synth.config_plain(seed=16, nchan=256, gulp=2048, dm_max=1000.0)
     held = hella.Search(hella.default_params(**params))
     dev = held.info.device_bytes
@@ -165,10 +165,53 @@ def test_pair_rows_budget_and_batch(hella):
     best, _ = s.autotune(1)
     assert best.add_mode != 5
     s.close()
-    bt = hella.Batch(hella.default_params(**dict(params, nbeam=2)))
-    with pytest.raises(hella.HellaError):
-        bt.set_tuning(hella.HellaTuning(*MODE5))
+
+
+@pytest.mark.parametrize("shape", [MODE5, MODE5_16])
+def test_pair_rows_batch_killmasks(hella, shape):
+    """The batched context in add mode 5 (the plan's rows over every channel,
+    killed channels packed as zeros, each beam building the rows its own DM
+    ceiling uses, beam by beam in one row buffer inside the gulp's graph)
+    against single-beam contexts: candidates and planes identical."""
+    params, _ = synth.config_plain(seed=44, nchan=128, gulp=2048, dm_max=400.0)
+    nb = 5
+    rng = np.random.default_rng(45)
+    ceilings = np.array([400.0, 250.0, 330.0, 120.0, 400.0], np.float32)
+    kill = (rng.random((nb, 128)) > rng.uniform(0, 0.1, (nb, 1))).astype(np.int32)
+    kill[1] = 0
+    kill[1, 77] = 1
+    kill[3, :9] = 0
+    skies = []
+    for b in range(nb):
+        sk = synth.config_plain(seed=46 + b, nchan=128, gulp=2048, dm_max=float(ceilings[b]))[1]
+        sk.bursts[0].amp *= 3
+        skies.append(sk)
+    bt = hella.Batch(hella.default_params(**dict(params, nbeam=nb)), dm_max=ceilings, killmask=kill,
+                     use_graph=True)
+    bt.set_tuning(hella.HellaTuning(*shape))
+    singles = []
+    for b in range(nb):
+        s = hella.Search(hella.default_params(**dict(params, dm_max=float(ceilings[b]), beam0=b, nbeam=1)))
+        s.set_killmask(kill[b])
+        singles.append(s)
+    total = 0
+    for g in range(max(s.info.min_gulp for s in singles) + 3):
+        x = synth.multibeam_gulp(skies, g, params["gulp"])
+        got, counts, searched = bt.process_gulp(x)
+        off = 0
+        for b, s in enumerate(singles):
+            want, sw = s.process_gulp(x[b:b + 1])
+            mine = got[off:off + counts[b]]
+            off += counts[b]
+            assert searched[b] == sw and cands_equal(mine, want), (g, b)
+            if sw:
+                assert np.array_equal(bt.copy_dedisp(b), s.copy_dedisp()), (g, b)
+            total += len(want)
+    assert total > 0
+    assert bt.get_tuning().add_mode == 5
     bt.close()
+    for s in singles:
+        s.close()
 
 
 def test_autotune_keeps_sums_exact(hella, oracle):

@@ -103,6 +103,7 @@ struct hdd_plan_struct {
   size_t smeta_cap = 0, sindex_cap = 0, spool_cap = 0;
   // add-mode-5 tables of the last DM range and shape used, host and device, and the rows
   hg::PairTables pair;
+  bool pair_rows = false;  // hdd_set_pair_rows: the execute calls take add mode 5
   int pair_first = -1, pair_count = -1, pair_cc = -1, pair_ntt = -1;
   bool pair_on_device = false;
   int4 *d_prinfo = nullptr, *d_prec = nullptr;
@@ -488,6 +489,13 @@ hdd_error hdd_set_device(int device_idx) {
   return HDD_NO_ERROR;
 }
 
+hdd_error hdd_set_pair_rows(hdd_plan p, int enable) {
+  if (!p) return HDD_INVALID_PLAN;
+  p->pair_rows = enable != 0;
+  if (!p->pair_rows) hg::plan_pair_release(p);
+  return HDD_NO_ERROR;
+}
+
 hdd_error hdd_set_stream(hdd_plan p, void *stream) {
   if (!p) return HDD_INVALID_PLAN;
   p->stream = (cudaStream_t)stream;
@@ -616,7 +624,26 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
   }
   const hg::DedispArgs a = hg::single_beam_args(tb, p->d_packed, R, 0, (int)first_dm_idx, (int)dm_count,
                                                 nout, dout, (long)(out_stride / 4), p->d_err);
-  if (a.nact == 0) {
+  bool done = false;
+  if (a.nact > 0 && p->pair_rows) {  // pair rows, 8 pairs a stage
+    hg::PairDeviceTables pt;
+    if ((e = hg::plan_pair_tables(p, (int)first_dm_idx, (int)dm_count, 8, hg::dedisp_time_tiles(nout), &pt)) !=
+        HDD_NO_ERROR)
+      return e;
+    hg::DedispArgs pa = hg::single_beam_args(hg::DeviceTables{nullptr, nullptr, hg::kPairDPT, 0, pt.nact, 8},
+                                             p->d_packed, R, 0, (int)first_dm_idx, (int)dm_count, nout, dout,
+                                             (long)(out_stride / 4), p->d_err);
+    hg::use_pair_tables(&pa, pt);
+    const cudaError_t ce = hg::dedisperse(pa, p->stream);
+    if (ce == cudaSuccess)
+      done = true;
+    else if (ce == cudaErrorInvalidValue)  // stages beyond shared memory: the channel-by-channel kernel
+      cudaGetLastError();
+    else
+      return HDD_INTERNAL_GPU_ERROR;
+  }
+  if (done) {
+  } else if (a.nact == 0) {
     for (hdd_size d = 0; d < dm_count; ++d)
       if (cudaMemsetAsync(reinterpret_cast<uint8_t *>(dout) + d * out_stride, 0, (size_t)nout * 4,
                           p->stream) != cudaSuccess)

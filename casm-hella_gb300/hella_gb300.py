@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
     _sig(L, "hdd_destroy_plan", None, [_VP])
     _sig(L, "hdd_set_device", C.c_int, [C.c_int])
     _sig(L, "hdd_set_stream", C.c_int, [_VP, _VP])
+    _sig(L, "hdd_set_pair_rows", C.c_int, [_VP, C.c_int])
     _sig(L, "hdd_set_dm_list", C.c_int, [_VP, _VP, _SZ])
     _sig(L, "hdd_generate_dm_list", C.c_int, [_VP, C.c_float, C.c_float, C.c_float, C.c_float])
     _sig(L, "hdd_set_killmask", C.c_int, [_VP, _VP])
@@ -310,6 +311,9 @@ class Plan:
 
     def set_stream(self, stream: int):
         _chk_hdd(self.L.hdd_set_stream(self.h, stream))
+
+    def set_pair_rows(self, on: bool):
+        _chk_hdd(self.L.hdd_set_pair_rows(self.h, int(bool(on))))
 
     @property
     def dm_count(self) -> int:

@@ -225,3 +225,39 @@ def test_autotune_keeps_sums_exact(hella, oracle):
     s.dedisperse(0)
     assert np.array_equal(s.copy_dedisp(), _oracle_plane(oracle, params, s, win, None))
     s.close()
+
+
+def test_plan_api_pair_rows(hella, oracle):
+    """hdd_set_pair_rows: hdd_execute_adv / hdd_execute_guru through pair rows
+    give the channel-by-channel kernel's sums and the oracle's, with a
+    killmask, host and device pointers, HDD_ASYNC, sub-ranges of trials and
+    a sample count that changes between calls; switched off, the plan goes
+    back to the channel-by-channel kernel."""
+    torch = pytest.importorskip("torch")
+    nch = 256
+    plan = hella.Plan(nch, 1e-3, 468.75, -(468.75 - 375.0) / nch)
+    plan.generate_dm_list(0.0, 1000.0, 40.0, 1.25)
+    km = (np.random.default_rng(70).random(nch) > 0.07).astype(np.int32)
+    plan.set_killmask(km)
+    rng = np.random.default_rng(71)
+    for extra in (5000, 2300):
+        x = rng.integers(0, 256, (plan.max_delay + extra, nch), dtype=np.uint8)
+        plan.set_pair_rows(False)
+        ref = plan.dedisperse(x)
+        plan.set_pair_rows(True)
+        got = plan.dedisperse(x)
+        assert np.array_equal(got, ref), extra
+        assert np.array_equal(got, oracle.dedisperse(x, plan.delay_table(), killmask=km, nout=extra)), extra
+    # a sub-range of trials, device pointers, asynchronous
+    nsamps, nout = x.shape[0], x.shape[0] - plan.max_delay
+    plan.set_stream(torch.cuda.current_stream().cuda_stream)
+    dx = torch.from_numpy(x).cuda()
+    first, count = 37, 100
+    out = torch.full((count, nout), -1.0, dtype=torch.float32, device="cuda")
+    plan.execute_guru(nsamps, dx, nch, out, nout * 4, first, count,
+                      flags=hella.HDD_DEVICE_POINTERS | hella.HDD_ASYNC)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref[first:first + count])
+    plan.set_pair_rows(False)
+    assert np.array_equal(plan.dedisperse(x), ref)
+    plan.close()

@@ -47,6 +47,9 @@ DEDISP_TRAFFIC = {
     # pair rows (add mode 5), 8 pairs a stage, groups of 8: k_pair_build 0.707 read + 5.78 written,
     # k_pair_sum 13.18 read + 0.654 written (profiles/k_pair_full_beam.md)
     (16, 4, 16, 0, 8, 5): 20.32e9,
+    # rows of channel quads (add mode 6), 8 quads a stage, groups of 8: k_pair_build<4> 0.760 read +
+    # 18.95 written, k_pair_sum 22.20 read + 0.657 written
+    (16, 4, 16, 0, 8, 6): 42.57e9,
 }
 
 
@@ -75,9 +78,9 @@ def args_():
                          "cases that profiling captures use")
     ap.add_argument("--dm-max", type=float, default=0.0,
                     help="DM ceiling of the full workload (0: 2000); a small profiling case")
-    ap.add_argument("--add-mode", type=int, default=5,
-                    help="dedispersion add mode of the single-beam workloads (hella_tuning.add_mode; 5: pair "
-                         "rows, else the channel-by-channel kernel's pipe balance)")
+    ap.add_argument("--add-mode", type=int, default=6,
+                    help="dedispersion add mode of the single-beam workloads (hella_tuning.add_mode; 6 / 5: rows "
+                         "of channel quads / pairs, else the channel-by-channel kernel's pipe balance)")
     return ap.parse_args()
 
 
@@ -278,12 +281,13 @@ def main():
         step(gi, False)
         gi += 1
     torch.cuda.synchronize()
-    # dedispersion: pair rows (add mode 5: 16-trial tiles, 8 pairs a stage, the deepest staging
-    # that fits, DM tiles walked in groups of 8 per time tile), 12.6 ms on the full beam against
-    # 19.4 ms for the channel-by-channel kernel's best shape (add mode 2, multiply-add odd lanes
-    # and addresses).  DM lists whose tiles do not fit the mode fall back to 2, then 0.
-    shapes = [hg.HellaTuning(16, 4, 16, 0, 8, 5)] if a.add_mode == 5 else []
-    shapes += [hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode if a.add_mode != 5 else 2), hg.HellaTuning(0, 4, 8, 0, 8, 0)]
+    # dedispersion: rows of channel quads (add mode 6: 16-trial tiles, 8 quads a stage, the deepest
+    # staging that fits, DM tiles walked in groups of 8 per time tile), 11.4 ms on the full beam;
+    # pairs (add mode 5) 12.5 ms; the channel-by-channel kernel's best shape (add mode 2, multiply-
+    # add odd lanes and addresses) 19.4 ms.  Shapes a DM list or the memory cannot take fall back
+    # in that order, then to add mode 0.
+    shapes = [hg.HellaTuning(16, 4, 16, 0, 8, m) for m in (6, 5) if m <= a.add_mode and a.add_mode >= 5]
+    shapes += [hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode if a.add_mode < 5 else 2), hg.HellaTuning(0, 4, 8, 0, 8, 0)]
     for shape in shapes:
         try:
             s.set_tuning(shape)
@@ -356,26 +360,30 @@ def main():
     peak_int = 2 * hg.int_add_peak(local) / 1e12  # two u8 sums per 32-bit add (16-bit SWAR lanes)
     peak_smem = hg.smem_read_peak(local) / 1e12
     achieved = adds / dd_t / 1e12
-    pairs = s.get_tuning().add_mode == 5
+    pairs = s.get_tuning().add_mode >= 5
     work = f"{info.ndms} trials x {nact} ch x {info.ntime_dd} samples"
     traffic = (DEDISP_TRAFFIC.get(tuple(s.get_tuning().as_dict().values()))
                if a.workload == "full" and not (a.nchan or a.dm_max) else None)
-    int_roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak_int, 3), "unit": "Tadd/s",
-                "frac": round(achieved / peak_int, 4),
-                "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 "
-                               "lanes: the byte-splitting channel-by-channel kernel's bound",
-                "ms_per_launch": round(dd_t * 1e3, 3)}
-    smem_roof = {"bound": "smem", "achieved": round(achieved, 3), "peak": round(peak_smem, 3), "unit": "TB/s",
-                 "frac": round(achieved / peak_smem, 4),
+    mode = s.get_tuning().add_mode
+    kernel = (f"k_pair_build + k_pair_sum (add mode {mode}: rows of channel {'quads' if mode == 6 else 'pairs'}, "
+              "timed together)") if pairs else "k_dedisp"
+    # one yardstick for every form of the dedispersion: channel-sample adds against the measured
+    # SWAR integer-add ceiling (two u8 sums per 32-bit add), the bound of the channel-by-channel
+    # kernel; the row kernels' own bound, shared-memory reads, is reported beside it
+    roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak_int, 3), "unit": "Tadd/s",
+            "frac": round(achieved / peak_int, 4),
+            "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
+            "ms_per_launch": round(dd_t * 1e3, 3), "kernel": kernel, "work_per_launch": work, "traffic": traffic,
+            "traffic_unit": "bytes per launch (ncu" + (", both kernels)" if pairs else ")")}
+    # shared-memory bytes read per channel-sample: 1 for pairs and the channel-by-channel kernel, 1/2 for quads
+    smem_b = 0.5 if mode == 6 else 1.0
+    smem_roof = {"bound": "smem", "achieved": round(achieved * smem_b, 3), "peak": round(peak_smem, 3),
+                 "unit": "TB/s", "frac": round(achieved * smem_b / peak_smem, 4),
                  "peak_source": "measured: conflict-free 16-byte shared-memory loads on all SMs "
-                                "(hella_smem_read_peak); one byte read per channel-sample",
+                                "(hella_smem_read_peak)",
+                 "note": f"{smem_b:g} byte read per channel-sample over the time of the whole dedispersion"
+                         + (" (row build included)" if pairs else ""),
                  "ms_per_launch": round(dd_t * 1e3, 3)}
-    if pairs:  # the pair rows' sums read one shared-memory byte per channel-sample: that is their bound
-        roof = dict(smem_roof, kernel="k_pair_build + k_pair_sum (add mode 5, timed together)",
-                    work_per_launch=work, traffic=traffic, traffic_unit="bytes per launch (ncu, both kernels)")
-    else:
-        roof = dict(int_roof, kernel="k_dedisp", work_per_launch=work, traffic=traffic,
-                    traffic_unit="bytes per launch (ncu)")
     hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") if (
         ROOT / "MEASURED_PEAKS.json").exists() else 6800.0
     sm_t = float(np.mean(sm_ms)) / 1e3
@@ -393,7 +401,7 @@ def main():
                     "frac": round(flag_bytes / fl_t / 1e9 / hbm, 4), "ms_per_launch": round(fl_t * 1e3, 3),
                     "note": "9 u8 passes + 1 u8 write per sample"},
     }
-    extra["dedisp_int32" if pairs else "dedisp_smem"] = int_roof if pairs else smem_roof
+    extra["dedisp_smem"] = smem_roof
     if roof["traffic"]:
         # the dominant kernel against HBM: its measured DRAM traffic over the launch time
         gbs = roof["traffic"] / dd_t / 1e9

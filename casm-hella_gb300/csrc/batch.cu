@@ -170,7 +170,7 @@ struct hella_batch {
   size_t bmeta_cap = 0, boff_cap = 0, bchans_cap = 0, bjobs_cap = 0;
   int btab_dpt = -1, btab_cc = -1;  // tile shape of the per-beam tables; -1: rebuild
   int *d_prend = nullptr;         // add mode 5: [nbeam][npair] end of the rows each beam builds
-  int prend_cc = -1;              // pairs per stage of the tables d_prend was made for; -1: remake
+  int prend_key = -1;             // shape (groups per stage, channels per group) of d_prend; -1: remake
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
   std::vector<Lane> lanes;
   std::deque<int> queue;          // lanes in submission order
@@ -338,7 +338,7 @@ hella_status upload_layout(hella_batch *b) {
   CK(cudaMemcpy(b->d_join, b->join.data(), nb * 4, cudaMemcpyHostToDevice));
   b->items_dpt = -1;  // dedisp_args re-uploads the beams with their item prefix
   b->btab_dpt = -1;   // and rebuilds the per-beam tables
-  b->prend_cc = -1;   // and the per-beam row ends of add mode 5
+  b->prend_key = -1;  // and the per-beam row ends of add modes 5 and 6
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;
 }
@@ -435,31 +435,31 @@ hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
-  if (t.add_mode == 5) {
-    // pair rows over every channel (killed channels are packed as zeros), built
+  if (t.add_mode >= 5) {
+    // rows of channel pairs (5) or quads (6) over every channel (killed channels are packed as zeros), built
     // and summed beam by beam in one row buffer; a beam builds the rows its
     // own trials use
-    const int cc = t.chan_chunk / 2, ntt = hg::dedisp_time_tiles(b->z.ntime_dd);
+    const int g = t.add_mode == 6 ? 4 : 2, cc = t.chan_chunk / 2, ntt = hg::dedisp_time_tiles(b->z.ntime_dd);
     if (b->p.hbm_budget) {
       size_t bytes = 0;
-      if (hg::plan_pair_bytes(b->plan, 0, b->z.ndms_all, cc, ntt, &bytes) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
+      if (hg::plan_pair_bytes(b->plan, 0, b->z.ndms_all, cc, ntt, g, &bytes) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
       if (b->dev_bytes + bytes + (size_t)b->nbeam * b->p.nchan * 2 > b->p.hbm_budget) return HELLA_ERR_BUDGET;
     }
     hg::PairDeviceTables pt;
-    const hdd_error he = hg::plan_pair_tables(b->plan, 0, b->z.ndms_all, cc, ntt, &pt);
+    const hdd_error he = hg::plan_pair_tables(b->plan, 0, b->z.ndms_all, cc, ntt, g, &pt);
     if (he == HDD_MEM_ALLOC_FAILED) return HELLA_ERR_ALLOC;
     if (he != HDD_NO_ERROR || pt.nact != b->p.nchan) return HELLA_ERR_DEDISP;  // the plan keeps every channel
     hella_status s;
     if (!b->d_prend && (s = dalloc(b, (void **)&b->d_prend, (size_t)b->nbeam * pt.npair * 4)) != HELLA_OK)
       return s;
-    if (b->prend_cc != cc) {
+    if (b->prend_key != cc * 16 + g) {
       std::vector<int> ends((size_t)b->nbeam * pt.npair);
       for (int i = 0; i < b->nbeam; ++i)
         if (hg::plan_pair_row_ends(b->plan, b->dbeams[i].dm_count, &ends[(size_t)i * pt.npair]) != HDD_NO_ERROR)
           return HELLA_ERR_DEDISP;
       CK(cudaStreamSynchronize(b->stream));
       CK(cudaMemcpy(b->d_prend, ends.data(), ends.size() * 4, cudaMemcpyHostToDevice));
-      b->prend_cc = cc;
+      b->prend_key = cc * 16 + g;
     }
     hg::DedispArgs a{};
     a.nbeam = 1;
@@ -563,11 +563,11 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
   return HELLA_OK;
 }
 
-// The dedispersion of every beam: one persistent launch, or (add mode 5)
+// The dedispersion of every beam: one persistent launch, or (add modes 5, 6)
 // the rows built and summed beam by beam, each launch reading its beam's
 // ring position from the device.
 hella_status dedisperse_beams(hella_batch *b, const hg::DedispArgs &da) {
-  if (da.mode != 5) {
+  if (da.mode < 5) {
     CK(hg::dedisperse(da, b->stream));
     return HELLA_OK;
   }
@@ -685,7 +685,7 @@ hella_status autotune(hella_batch *b, int reps, hella_tuning *out, float *out_ms
       &best_ms);
   if (s != HELLA_OK) return s;
   b->tune = best;
-  if (best.add_mode != 5) hg::plan_pair_release(b->plan);  // the rows are only kept for add mode 5
+  if (best.add_mode < 5) hg::plan_pair_release(b->plan);  // the rows are only kept for add modes 5 and 6
   for (Lane &l : b->lanes) l.stale = true;
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
@@ -1075,7 +1075,7 @@ hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t) {
   if (!b || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
   if (any_busy(b)) return HELLA_ERR_STATE;
   b->tune = *t;
-  if (t->add_mode != 5) hg::plan_pair_release(b->plan);
+  if (t->add_mode < 5) hg::plan_pair_release(b->plan);
   b->tune.samples_per_thread = 4;
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;

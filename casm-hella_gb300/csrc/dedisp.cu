@@ -1022,7 +1022,7 @@ cudaError_t dedisperse(const DedispArgs &a, cudaStream_t s) {
   if (a.R % 4 != 0 || a.ntt <= 0 || a.group <= 0 || a.nbeam <= 0) return cudaErrorInvalidValue;
   if (a.varied && !a.beams) return cudaErrorInvalidValue;
   if (a.mode == 4) return launch_sub(a, s);
-  if (a.mode == 5) return dedisperse_pairs(a, s);
+  if (a.mode == 5 || a.mode == 6) return dedisperse_pairs(a, s);
   switch (a.dpt) {
     case 16: return launch_cc<16>(a, s);
     case 8: return launch_cc<8>(a, s);

@@ -125,7 +125,8 @@ struct DedispArgs {
   int nbuf;                 // staging buffers, 2..4 (0: deepest that fits)
   int mode;                 // pipe balance of the adds (0-3; 1-3 need dpt >= 8), or 4: sub-band
                             // sums of four channels per pattern (dpt 16, tables below), or
-                            // 5: pair rows (dpt 16, one beam, pair tables below)
+                            // 5 / 6: rows of channel pairs / quads (dpt 16, one beam a launch,
+                            // pair tables below)
   int unit;                 // must be 1
   int max_spread;           // largest tile_meta spread
   const int4 *tile_meta;    // [ntiles][nact] {channel, smallest delay(c, d) of the tile, spread, 0}
@@ -139,6 +140,7 @@ struct DedispArgs {
   int sub_rec;              // largest record, bytes (a multiple of 16)
   // mode 5 (see PairTables): the rows are rebuilt from `one.packed` at `one.win0`
   const int4 *pair_rinfo;
+  const int4 *pair_rinfo2;
   const long long *pair_roff;
   const int *pair_rwords;
   const int *pair_prow;
@@ -146,8 +148,8 @@ struct DedispArgs {
   const int4 *pair_rec;
   const int *pair_tile_st;
   uint32_t *pair_rows;
-  const int *pair_rend;     // [npair] end of the rows to build per pair (null: all rows)
-  int pair_npair, pair_span, pair_stage;
+  const int *pair_rend;     // [npair] end of the rows to build per group (null: all rows)
+  int pair_npair, pair_span, pair_stage, pair_g, pair_lanecap;
   long pair_npos;
 };
 // One beam's tile tables gathered from a launch's tables (all nch channels):
@@ -197,52 +199,56 @@ SubTables dedisp_sub_tables(const int *delays_host, int nchan, const int *chans_
 // Shared memory of one add-mode-4 block.
 size_t dedisp_sub_smem(int max_spread, int max_words, int max_rec, int nbuf);
 
-// Add mode 5: pair rows.  The active channels are taken two at a time in
-// order (the last alone when their number is odd).  For each pair (c0, c1)
-// and each relative delay r = delay(c1, d) - delay(c0, d) that a trial of
-// the range gives it, one row holds x[c0][p] + x[c1][p + r] for the window
-// positions p that those trials read, two samples a word (p in the low and
-// p + 512 in the high 16 bits).  The rows are rebuilt from the packed ring
-// for every window (k_pair_build), after which a 16-trial tile sums, pair
-// by pair, the row of each trial's relative delay at the trial's delay of
-// c0 (k_pair_sum): half the adds of the channel-by-channel sum, with no
-// byte splitting in the inner loop.  A stage of a tile stages the windows
-// of the rows its pairs use; its record is
-//   int4 {pairs, rows, 0, 0}
+// Add modes 5 and 6: rows of channel groups.  The active channels are taken
+// g at a time in order (g = 2, pairs, in mode 5; g = 4 in mode 6; the last
+// group may be smaller).  For each group (c0, c1, ...) and each pattern of
+// relative delays r_i = delay(c_i, d) - delay(c0, d) that a trial of the
+// range gives it, one row holds x[c0][p] + sum_i x[c_i][p + r_i] for the
+// window positions p that those trials read, two samples a word (p in the
+// low and p + 512 in the high 16 bits).  The rows are rebuilt from the
+// packed ring for every window (k_pair_build), after which a 16-trial tile
+// sums, group by group, the row of each trial's pattern at the trial's
+// delay of c0 (k_pair_sum): 1/g of the adds of the channel-by-channel sum,
+// with no byte splitting in the inner loop.  A stage of a tile stages the
+// windows of the rows its groups use; its record is
+//   int4 {groups, rows, 0, 0}
 //   int  [cc][16] byte offset, in the staged rows, of each trial's window
 //   int4 [kPairRowsMax] {first word (low, high 32 bits), words, byte slot}
 constexpr int kPairDPT = 16;
 constexpr int kPairRowsMax = 32;  // rows per stage: one per lane of the staging warp
-constexpr int kPairLaneCap = 128; // pairs per 16-bit lane before widening (128 x 510 < 2^16)
+constexpr int kPairGMax = 4;      // channels per group
+// Groups per 16-bit lane before widening: lanecap x g x 255 < 2^16.
+inline int pair_lanecap(int g) { return 65535 / (255 * g); }
 __host__ __device__ constexpr int pair_rec_int4(int cc) { return 1 + cc * kPairDPT / 4 + kPairRowsMax; }
-// Staged row bytes a stage of cc pairs may hold (a single pair may exceed it).
+// Staged row bytes a stage of cc groups may hold (a single group may exceed it).
 inline int pair_stage_budget(int cc) { return cc <= 4 ? 24 * 1024 : 36 * 1024; }
 struct PairTables {
-  int cc = 0, ntt = 0, ntiles = 0, npair = 0, nrows = 0;
+  int g = 0, cc = 0, ntt = 0, ntiles = 0, npair = 0, nrows = 0, dm_count = 0;
   int max_stage = 0;            // largest staged row bytes of a stage
-  int max_span = 0;             // largest r range of one pair
+  int max_span = 0;             // largest r_i range of one group and channel
   long npos = 0;                // window positions the rows cover
   long words = 0;               // words of all rows
-  std::vector<int4> rinfo;      // [nrows] {c0, c1 (-1: alone), r, first position}
+  std::vector<int4> rinfo;      // [nrows] {c0, c1 (-1: none), r1, first position}
+  std::vector<int4> rinfo2;     // [nrows] {c2, c3 (-1: none), r2, r3}
   std::vector<long long> roff;  // [nrows] first word of the row
   std::vector<int> rwords;      // [nrows] words of the row
-  std::vector<int> prow;        // [npair + 1] first row of each pair
-  std::vector<int2> prange;     // [npair] {smallest, largest r}
+  std::vector<int> prow;        // [npair + 1] first row of each group
+  std::vector<int2> prange;     // [npair][kPairGMax - 1] {smallest, largest r_i}, i = 1..
+  std::vector<int> row_of;      // [dm_count][npair] row of each trial and group
   std::vector<int4> rec;        // stage records, pair_rec_int4(cc) int4 each
   std::vector<int> tile_st;     // [ntiles + 1] first record of each tile
 };
-// Pair tables for trials [dm_first, dm_first + dm_count) over the active
-// channels, cc pairs per stage (4 or 8), for ntt time tiles of output.
+// Group tables for trials [dm_first, dm_first + dm_count) over the active
+// channels, g channels a group (2 or 4), cc groups per stage (4 or 8), for
+// ntt time tiles of output.
 PairTables dedisp_pair_tables(const int *delays_host, int nchan, const int *chans_host, int nact,
-                              int dm_first, int dm_count, int cc, int ntt);
-// Per pair, the end of the rows that trials [dm_first, dm_first + dm_count)
-// of the tables' DM list use (the rows of a pair are in increasing relative
-// delay; a beam with a lower DM ceiling builds the pair's first rows only).
-void pair_row_ends(const PairTables &t, const int *delays_host, int nchan, const int *chans_host, int nact,
-                   int dm_first, int dm_count, int *ends);
+                              int dm_first, int dm_count, int cc, int ntt, int g);
+// Per group, the end of the rows that the tables' first `count` trials use
+// (a beam whose DM ceiling cuts the list builds those rows only).
+void pair_row_ends(const PairTables &t, int count, int *ends);
 // Builds the rows, then sums them (two launches); `a` is a launch with mode
-// 5 and dpt 16 over one beam: `one`, or beams[0] read on the device (the
-// batched context, whose ring positions the device advances).
+// 5 or 6 and dpt 16 over one beam: `one`, or beams[0] read on the device
+// (the batched context, whose ring positions the device advances).
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s);
 // Largest delay spread over the active channels of any dpt-trial tile.
 int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int nact,

@@ -36,12 +36,13 @@ hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out
 // Points a launch at add-mode-4 tables (16-trial tiles; items must be counted
 // for that tile size).
 void use_sub_tables(DedispArgs *a, const SubDeviceTables &t);
-// Add-mode-5 tables (pair rows) for trials [first, first + count) over the
-// plan's active channels with cc pairs per stage and ntt time tiles: host
-// copy cached per range and shape, device copy and row buffer set up on
-// first use.
+// Add-mode-5/6 tables (rows of g = 2 or 4 channels) for trials [first,
+// first + count) over the plan's active channels with cc groups per stage
+// and ntt time tiles: host copy cached per range and shape, device copy and
+// row buffer set up on first use.
 struct PairDeviceTables {
   const int4 *rinfo;
+  const int4 *rinfo2;
   const long long *roff;
   const int *rwords;
   const int *prow;
@@ -49,14 +50,14 @@ struct PairDeviceTables {
   const int4 *rec;
   const int *tile_st;
   uint32_t *rows;
-  int npair, span, stage, nact, cc;
+  int npair, span, stage, nact, cc, g;
   long npos;
 };
-hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, PairDeviceTables *out);
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out);
 // Frees the add-mode-5 device tables and rows (set up again on next use).
 void plan_pair_release(hdd_plan p);
 // Device bytes those tables and their rows take (builds the host copy).
-hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, size_t *bytes);
+hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, int g, size_t *bytes);
 // Per pair, the end of the rows that the first `count` trials use, for the
 // tables last set up from trial 0 (a beam whose DM ceiling cuts the list).
 hdd_error plan_pair_row_ends(hdd_plan p, int count, int *ends);

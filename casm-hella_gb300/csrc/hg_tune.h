@@ -16,7 +16,7 @@ inline bool tuning_ok(const hella_tuning &t) {
                       t.dm_per_block == 4 || t.dm_per_block == 8 || t.dm_per_block == 16;
   return dpt_ok && (t.chan_chunk == 8 || t.chan_chunk == 16) &&
          (t.stages == 0 || (t.stages >= 2 && t.stages <= 4)) && t.group >= 1 && t.group <= 4096 &&
-         t.add_mode >= 0 && t.add_mode <= 5 &&
+         t.add_mode >= 0 && t.add_mode <= 6 &&
          (t.add_mode < 4 || t.dm_per_block == 0 || t.dm_per_block == 16);
 }
 
@@ -25,8 +25,8 @@ inline bool tuning_ok(const hella_tuning &t) {
 // rounds.  time_shape(t, &ms) times one shape; HELLA_ERR_INVALID_ARG (a
 // shape the DM list cannot use), HELLA_ERR_CUDA (a launch the device
 // refused, e.g. staging beyond shared memory), HELLA_ERR_ALLOC and
-// HELLA_ERR_BUDGET (add mode 5's rows beyond the free memory or the HBM
-// budget) skip the shape, any other error ends the search.
+// HELLA_ERR_BUDGET (add mode 5's or 6's rows beyond the free memory or the
+// HBM budget) skip the shape, any other error ends the search.
 inline hella_status tune_shapes(const hella_tuning &start,
                                 const std::function<hella_status(const hella_tuning &, float *)> &time_shape,
                                 hella_tuning *best_out, float *best_ms_out) {
@@ -58,7 +58,7 @@ inline hella_status tune_shapes(const hella_tuning &start,
     return HELLA_OK;
   };
   for (int round = 0; round < 2; ++round) {
-    for (int m : {0, 1, 2, 3, 5}) {  // add mode 4 measured slower on every workload: not searched
+    for (int m : {0, 1, 2, 3, 5, 6}) {  // add mode 4 measured slower on every workload: not searched
       hella_tuning t = best;
       t.add_mode = m;
       if ((s = try_shape(t)) != HELLA_OK) return s;

@@ -1,36 +1,39 @@
-// pairs.cu -- add mode 5 of the dedispersion: pair rows (hg_internal.h).
+// pairs.cu -- add modes 5 and 6 of the dedispersion: rows of channel
+// groups, pairs (g = 2) or quads (g = 4) (hg_internal.h).
 //
 // Same exact integer sums as k_dedisp (out[d][t] = sum over active channels
 // c of x[c][t + delay(c, d)], the operation casm-hella obtains from
 // dedisp_execute_adv, src/hella/src/dedisperse.cpp:17-48), computed in two
 // launches per window:
 //
-// k_pair_build: one block per (pair, 4096 window positions).  Both
-//   channels' packed words of the chunk (plus the pair's relative-delay
-//   range for the second channel) are read from the ring once into shared
-//   memory as 16-bit lanes (bytes 0 and 2 of a packed word are the samples
-//   p and p + 512), then every row of the pair is written from them:
-//   row(r)[p] = x[c0][p] + x[c1][p + r].  Reads are the ring once per
-//   pair; writes the rows, coalesced.
+// k_pair_build: one block per (group, 4096 window positions).  The group's
+//   channels' packed words of the chunk (for channel i widened by the
+//   group's range of relative delays r_i) are read from the ring once into
+//   shared memory as 16-bit lanes (bytes 0 and 2 of a packed word are the
+//   samples p and p + 512), then every row of the group is written from
+//   them: row(r)[p] = x[c0][p] + sum_i x[c_i][p + r_i].  Reads are the ring
+//   once per group; writes the rows, coalesced.
 //
 // k_pair_sum: the persistent staging pipeline of k_dedisp (work item =
 //   16-trial tile x 1024 output samples, stages issued warp by warp with
 //   cp.async.bulk onto full/empty mbarriers, every wait bounded) over stage
 //   records instead of channels.  A stage stages the windows of the rows
-//   its pairs use (lane i copies row i) and the record's trial offsets;
-//   thread j then reads, per pair and trial, the words j and j + 256 of
+//   its groups use (lane i copies row i) and the record's trial offsets;
+//   thread j then reads, per group and trial, the words j and j + 256 of
 //   the trial's window: four output samples (j, j+256, j+512, j+768) in two
-//   SWAR registers of 16-bit lanes, two pairs per three-input add.  The
-//   lanes are widened into 32-bit totals every kPairLaneCap pairs.
+//   SWAR registers of 16-bit lanes, two groups per three-input add.  The
+//   lanes are widened into 32-bit totals every pair_lanecap(g) groups.
 //
-// Per pair and trial the inner loop is two shared loads and one add for
-// eight channel-samples, against two loads, four byte permutes and two adds
-// in k_dedisp; shared-memory traffic stays one byte per channel-sample, so
-// the sums are bound by shared-memory bandwidth rather than ALU issue.
+// Per group and trial the inner loop is two shared loads and one add for
+// 4g channel-samples, against two loads, four byte permutes and two adds
+// per eight in k_dedisp; shared-memory traffic is 2/g bytes per
+// channel-sample, so the sums are bound by shared-memory bandwidth, and
+// the build by its row writes (g = 4: about three times the rows of g = 2).
 #include "hg_internal.h"
 #include "hg_ptx.h"
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 
 namespace hg {
@@ -38,15 +41,19 @@ namespace {
 
 constexpr int S = kPackS;
 constexpr int kTileSamples = 4 * S;
-constexpr int kBuildCH = 4096;            // window positions per build block
+// window positions per build block: 4096 for pairs, 2048 for quads (whose
+// four channel windows would otherwise leave three blocks per SM)
+__host__ __device__ constexpr int build_chunk(int g) { return g <= 2 ? 4096 : 2048; }
 constexpr int kBarHdr = 448;              // full[4] | empty[4] | per-warp staging cursors
 constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
 constexpr int kMaxBuf = 4;
 
 __host__ __device__ constexpr int stage_hdr_bytes(int cc) { return 16 + cc * kPairDPT * 4; }
 
+template <int G>
 __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
+  constexpr int kBuildCH = build_chunk(G);
   const int k = blockIdx.y;
   const long P0 = (long)blockIdx.x * kBuildCH;
   const DedispBeam bm = a.beams ? a.beams[0] : a.one;
@@ -57,39 +64,48 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
     if (P0 < (long)in.w + a.pair_rwords[r] && P0 + kBuildCH > (long)in.w) any = true;
   }
   if (!any) return;
-  const int4 i0 = a.pair_rinfo[r0];
-  const int2 rr = a.pair_prange[k];
+  const int4 i0 = a.pair_rinfo[r0], j0 = a.pair_rinfo2[r0];
+  const int ch[kPairGMax] = {i0.x, i0.y, G == 4 ? j0.x : -1, G == 4 ? j0.y : -1};  // -1: fewer channels
   const long R = a.R;
-  uint32_t *sa = sm, *sb = sm + kBuildCH;
+  // channel i's words for positions [P0 + rmin_i, P0 + kBuildCH + rmax_i) at sm + off[i];
   // window position p lies at ring word (win0 + p) mod R
-  const uint32_t *pa = bm.packed + (size_t)i0.x * R;
-  const long ba = (bm.win0 + P0) % R;
-  for (int i = threadIdx.x; i < kBuildCH; i += blockDim.x) {
-    long p = ba + i;
-    if (p >= R) p %= R;
-    sa[i] = __byte_perm(pa[p], 0u, 0x4240);
-  }
-  if (i0.y >= 0) {
-    const uint32_t *pb = bm.packed + (size_t)i0.y * R;
-    long bb = (bm.win0 + P0 + rr.x) % R;
-    if (bb < 0) bb += R;
-    const int nb = kBuildCH + rr.y - rr.x;
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-      long p = bb + i;
-      if (p >= R) p %= R;
-      sb[i] = __byte_perm(pb[p], 0u, 0x4240);
+  int off[kPairGMax] = {0, 0, 0, 0}, rmin[kPairGMax] = {0, 0, 0, 0};
+  int nwin = 0;
+  for (int i = 0; i < G; ++i) {
+    const int2 rr = i == 0 ? make_int2(0, 0) : a.pair_prange[k * (kPairGMax - 1) + i - 1];
+    off[i] = nwin;
+    rmin[i] = rr.x;
+    if (ch[i] < 0) continue;
+    const int n = kBuildCH + rr.y - rr.x;
+    const uint32_t *src = bm.packed + (size_t)ch[i] * R;
+    long base = (bm.win0 + P0 + rr.x) % R;
+    if (base < 0) base += R;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      long pos = base + q;
+      if (pos >= R) pos %= R;
+      sm[nwin + q] = __byte_perm(src[pos], 0u, 0x4240);
     }
+    nwin += n;
   }
   __syncthreads();
   for (int r = r0; r < r1; ++r) {
-    const int4 in = a.pair_rinfo[r];
+    const int4 in = a.pair_rinfo[r], in2 = a.pair_rinfo2[r];
     const long lo = max(P0, (long)in.w), hi = min(P0 + kBuildCH, (long)in.w + a.pair_rwords[r]);
-    uint32_t *dst = a.pair_rows + a.pair_roff[r] - in.w;
-    if (i0.y >= 0) {
-      const int sh = in.z - rr.x;
-      for (long p = lo + threadIdx.x; p < hi; p += blockDim.x) dst[p] = sa[p - P0] + sb[p - P0 + sh];
+    uint32_t *dst = a.pair_rows + a.pair_roff[r];
+    // word q of the chunk, q = p - P0, of channel i for this row's r_i
+    const int s1 = off[1] + in.z - rmin[1], s2 = off[2] + in2.z - rmin[2], s3 = off[3] + in2.w - rmin[3];
+    const int first = (int)(lo - P0), last = (int)(hi - P0), d0 = (int)(P0 - in.w);
+    // rows are read back by other blocks much later: streaming stores
+    if (G == 4 && ch[3] >= 0) {
+      for (int q = first + threadIdx.x; q < last; q += blockDim.x)
+        __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q] + sm[s3 + q]);
+    } else if (G == 4 && ch[2] >= 0) {
+      for (int q = first + threadIdx.x; q < last; q += blockDim.x)
+        __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q]);
+    } else if (ch[1] >= 0) {
+      for (int q = first + threadIdx.x; q < last; q += blockDim.x) __stcs(dst + d0 + q, sm[q] + sm[s1 + q]);
     } else {
-      for (long p = lo + threadIdx.x; p < hi; p += blockDim.x) dst[p] = sa[p - P0];
+      for (int q = first + threadIdx.x; q < last; q += blockDim.x) __stcs(dst + d0 + q, sm[q]);
     }
   }
 }
@@ -214,7 +230,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
 #pragma unroll
       for (int k = 0; k < 4; ++k) tot[m][k] = 0u;
     }
-    int npairs = 0;  // pairs in the 16-bit lanes
+    int npairs = 0;  // groups in the 16-bit lanes
     for (int st = 0; st < nstage; ++st) {
       {
         bool to = false;
@@ -267,7 +283,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
       if (lane == 0) mbar_arrive(empty_of(b));  // this warp is done with buffer b
       ++gs_c;
       npairs += ng;
-      if (npairs + CC > kPairLaneCap) {
+      if (npairs + CC > a.pair_lanecap) {
 #pragma unroll
         for (int m = 0; m < DPT; ++m) {
           tot[m][0] += acc_a[m] & 0xffffu;
@@ -333,33 +349,50 @@ cudaError_t launch_sum(const DedispArgs &a, cudaStream_t s) {
 }  // namespace
 
 PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, int nact, int dm_first,
-                              int dm_count, int cc, int ntt) {
+                              int dm_count, int cc, int ntt, int g) {
   PairTables t;
+  t.g = g;
   t.cc = cc;
   t.ntt = ntt;
+  t.dm_count = dm_count;
   t.ntiles = (dm_count + kPairDPT - 1) / kPairDPT;
-  t.npair = (nact + 1) / 2;
+  t.npair = (nact + g - 1) / g;
   const int stage_max = pair_stage_budget(cc);
   auto dl = [&](int d, int c) { return delays[(size_t)(dm_first + d) * nchan + c]; };
-  // rows: per pair, one per distinct relative delay, in increasing r
-  std::vector<int> row_of((size_t)dm_count * t.npair), rel(dm_count), u;
+  // rows: per group, one per distinct pattern (r_1, r_2, r_3) of relative
+  // delays, in increasing (lexicographic) order
+  using Pat = std::array<int, kPairGMax - 1>;
+  std::vector<Pat> rel(dm_count), u;
+  t.row_of.assign((size_t)dm_count * t.npair, 0);
   t.prow.assign(t.npair + 1, 0);
-  t.prange.resize(t.npair);
+  t.prange.assign((size_t)t.npair * (kPairGMax - 1), make_int2(0, 0));
   for (int k = 0; k < t.npair; ++k) {
-    const int c0 = chans[2 * k], c1 = 2 * k + 1 < nact ? chans[2 * k + 1] : -1;
-    for (int d = 0; d < dm_count; ++d) rel[d] = c1 >= 0 ? dl(d, c1) - dl(d, c0) : 0;
+    int c[kPairGMax];
+    for (int i = 0; i < kPairGMax; ++i) c[i] = i < g && g * k + i < nact ? chans[g * k + i] : -1;
+    for (int d = 0; d < dm_count; ++d)
+      for (int i = 1; i < kPairGMax; ++i) rel[d][i - 1] = c[i] >= 0 ? dl(d, c[i]) - dl(d, c[0]) : 0;
     u = rel;
     std::sort(u.begin(), u.end());
     u.erase(std::unique(u.begin(), u.end()), u.end());
     const int base = (int)t.rinfo.size();
-    for (int v : u) t.rinfo.push_back(make_int4(c0, c1, v, 1 << 30));
+    for (const Pat &v : u) {
+      t.rinfo.push_back(make_int4(c[0], c[1], v[0], 1 << 30));
+      t.rinfo2.push_back(make_int4(c[2], c[3], v[1], v[2]));
+    }
     for (int d = 0; d < dm_count; ++d) {
       const int id = base + (int)(std::lower_bound(u.begin(), u.end(), rel[d]) - u.begin());
-      row_of[(size_t)d * t.npair + k] = id;
-      t.rinfo[id].w = std::min(t.rinfo[id].w, dl(d, c0));
+      t.row_of[(size_t)d * t.npair + k] = id;
+      t.rinfo[id].w = std::min(t.rinfo[id].w, dl(d, c[0]));
     }
-    t.prange[k] = make_int2(u.front(), u.back());
-    t.max_span = std::max(t.max_span, u.back() - u.front());
+    for (int i = 1; i < kPairGMax; ++i) {
+      int lo = 0, hi = 0;
+      for (size_t j = 0; j < u.size(); ++j) {
+        lo = j ? std::min(lo, u[j][i - 1]) : u[j][i - 1];
+        hi = j ? std::max(hi, u[j][i - 1]) : u[j][i - 1];
+      }
+      t.prange[(size_t)k * (kPairGMax - 1) + i - 1] = make_int2(lo, hi);
+      t.max_span = std::max(t.max_span, hi - lo);
+    }
     t.prow[k + 1] = (int)t.rinfo.size();
   }
   t.nrows = (int)t.rinfo.size();
@@ -393,10 +426,10 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
   for (int i = 0; i < t.ntiles; ++i) {
     const int d0 = i * kPairDPT, nt = std::min(kPairDPT, dm_count - d0);
     for (int k = 0; k < t.npair; ++k) {
-      const int c0 = chans[2 * k];
+      const int c0 = chans[g * k];
       int uid[kPairDPT], ub[kPairDPT], us[kPairDPT], nu = 0;
       for (int m = 0; m < nt; ++m) {
-        ids[m] = row_of[(size_t)(d0 + m) * t.npair + k];
+        ids[m] = t.row_of[(size_t)(d0 + m) * t.npair + k];
         av[m] = dl(d0 + m, c0) - t.rinfo[ids[m]].w;
         int j = 0;
         while (j < nu && uid[j] != ids[m]) ++j;
@@ -455,34 +488,32 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
   return t;
 }
 
-void pair_row_ends(const PairTables &t, const int *delays, int nchan, const int *chans, int nact, int dm_first,
-                   int dm_count, int *ends) {
+void pair_row_ends(const PairTables &t, int count, int *ends) {
   for (int k = 0; k < t.npair; ++k) {
-    const int c0 = chans[2 * k], c1 = 2 * k + 1 < nact ? chans[2 * k + 1] : -1;
-    int rmax = 0;
-    for (int d = 0; d < dm_count; ++d) {
-      const int *row = delays + (size_t)(dm_first + d) * nchan;
-      const int r = c1 >= 0 ? row[c1] - row[c0] : 0;
-      rmax = d == 0 ? r : std::max(rmax, r);
-    }
-    int e = t.prow[k];  // rows of a pair are in increasing r
-    while (e < t.prow[k + 1] && t.rinfo[e].z <= rmax) ++e;
-    ends[k] = dm_count > 0 ? e : t.prow[k];
+    int e = t.prow[k];
+    for (int d = 0; d < std::min(count, t.dm_count); ++d) e = std::max(e, t.row_of[(size_t)d * t.npair + k] + 1);
+    ends[k] = e;
   }
 }
 
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
-  if ((a.beams && a.nbeam != 1) || a.dpt != kPairDPT || a.mode != 5 || !a.pair_rows || !a.pair_rec || !a.pair_tile_st ||
-      !a.pair_rinfo || !a.pair_roff || !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 ||
-      a.pair_npair > 65535 || a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0)
+  const int g = a.pair_g;
+  if ((a.beams && a.nbeam != 1) || a.dpt != kPairDPT || (a.mode != 5 && a.mode != 6) || (g != 2 && g != 4) ||
+      !a.pair_rows || !a.pair_rec || !a.pair_tile_st || !a.pair_rinfo || !a.pair_rinfo2 || !a.pair_roff ||
+      !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 || a.pair_npair > 65535 ||
+      a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0 || a.pair_lanecap < 1 ||
+      a.pair_lanecap > pair_lanecap(g))
     return cudaErrorInvalidValue;
   if (a.R <= 0 || (!a.beams && a.one.win0 < 0)) return cudaErrorInvalidValue;
-  const size_t bsmem = (size_t)(2 * kBuildCH + a.pair_span) * 4;
+  // the group's channel windows: ch words for c0, ch + its r range for the others
+  const int ch = build_chunk(g);
+  const size_t bsmem = ((size_t)g * ch + (size_t)(g - 1) * a.pair_span) * 4;
   if (bsmem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_pair_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
+  auto kern = g == 4 ? k_pair_build<4> : k_pair_build<2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
   if (e != cudaSuccess) return e;
-  const dim3 grid((unsigned)((a.pair_npos + kBuildCH - 1) / kBuildCH), (unsigned)a.pair_npair);
-  k_pair_build<<<grid, 256, bsmem, s>>>(a);
+  const dim3 grid((unsigned)((a.pair_npos + ch - 1) / ch), (unsigned)a.pair_npair);
+  kern<<<grid, 256, bsmem, s>>>(a);
   count_launches(1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   switch (a.cc) {

@@ -103,15 +103,15 @@ struct hdd_plan_struct {
   size_t smeta_cap = 0, sindex_cap = 0, spool_cap = 0;
   // add-mode-5 tables of the last DM range and shape used, host and device, and the rows
   hg::PairTables pair;
-  bool pair_rows = false;  // hdd_set_pair_rows: the execute calls take add mode 5
-  int pair_first = -1, pair_count = -1, pair_cc = -1, pair_ntt = -1;
+  int pair_rows = 0;  // hdd_set_pair_rows: channels a group (2 or 4) of the execute calls' rows; 0: off
+  int pair_first = -1, pair_count = -1, pair_cc = -1, pair_ntt = -1, pair_g = -1;
   bool pair_on_device = false;
-  int4 *d_prinfo = nullptr, *d_prec = nullptr;
+  int4 *d_prinfo = nullptr, *d_prinfo2 = nullptr, *d_prec = nullptr;
   long long *d_proff = nullptr;
   int *d_prwords = nullptr, *d_pprow = nullptr, *d_ptile = nullptr;
   int2 *d_pprange = nullptr;
   uint32_t *d_prows = nullptr;
-  size_t prinfo_cap = 0, prec_cap = 0, proff_cap = 0, prwords_cap = 0, pprow_cap = 0, ptile_cap = 0,
+  size_t prinfo_cap = 0, prinfo2_cap = 0, prec_cap = 0, proff_cap = 0, prwords_cap = 0, pprow_cap = 0, ptile_cap = 0,
          pprange_cap = 0, prows_cap = 0;
 };
 
@@ -124,7 +124,7 @@ void invalidate_tables(hdd_plan p) {
   p->tab_on_device = false;
   p->sub_first = p->sub_count = -1;
   p->sub_on_device = false;
-  p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = -1;
+  p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = p->pair_g = -1;
   p->pair_on_device = false;
 }
 
@@ -256,20 +256,22 @@ hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out
 namespace {
 
 // Host pair tables of the range and shape, built when they differ from the cached ones.
-hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt) {
-  if (p->pair_first == first && p->pair_count == count && p->pair_cc == cc && p->pair_ntt == ntt)
+hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt, int g) {
+  if (p->pair_first == first && p->pair_count == count && p->pair_cc == cc && p->pair_ntt == ntt &&
+      p->pair_g == g)
     return HDD_NO_ERROR;
   try {
     p->pair = dedisp_pair_tables(p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), first, count,
-                                 cc, ntt);
+                                 cc, ntt, g);
   } catch (const std::bad_alloc &) {
-    p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = -1;
+    p->pair_first = p->pair_count = p->pair_cc = p->pair_ntt = p->pair_g = -1;
     return HDD_MEM_ALLOC_FAILED;
   }
   p->pair_first = first;
   p->pair_count = count;
   p->pair_cc = cc;
   p->pair_ntt = ntt;
+  p->pair_g = g;
   p->pair_on_device = false;
   return HDD_NO_ERROR;
 }
@@ -281,17 +283,17 @@ size_t vbytes(const std::vector<T> &v) {
 
 }  // namespace
 
-hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, size_t *bytes) {
-  const hdd_error e = pair_host_tables(p, first, count, cc, ntt);
+hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, int g, size_t *bytes) {
+  const hdd_error e = pair_host_tables(p, first, count, cc, ntt, g);
   if (e != HDD_NO_ERROR) return e;
   const PairTables &t = p->pair;
-  *bytes = vbytes(t.rinfo) + vbytes(t.roff) + vbytes(t.rwords) + vbytes(t.prow) + vbytes(t.prange) +
+  *bytes = vbytes(t.rinfo) + vbytes(t.rinfo2) + vbytes(t.roff) + vbytes(t.rwords) + vbytes(t.prow) + vbytes(t.prange) +
            vbytes(t.rec) + vbytes(t.tile_st) + std::max<size_t>((size_t)t.words, 4) * 4;
   return HDD_NO_ERROR;
 }
 
-hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, PairDeviceTables *out) {
-  hdd_error e = pair_host_tables(p, first, count, cc, ntt);
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out) {
+  hdd_error e = pair_host_tables(p, first, count, cc, ntt, g);
   if (e != HDD_NO_ERROR) return e;
   const PairTables &t = p->pair;
   if (!p->pair_on_device) {
@@ -302,6 +304,8 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, Pa
       return HDD_NO_ERROR;
     };
     if ((e = up((void **)&p->d_prinfo, &p->prinfo_cap, t.rinfo.data(), t.rinfo.size() * sizeof(int4))) !=
+            HDD_NO_ERROR ||
+        (e = up((void **)&p->d_prinfo2, &p->prinfo2_cap, t.rinfo2.data(), t.rinfo2.size() * sizeof(int4))) !=
             HDD_NO_ERROR ||
         (e = up((void **)&p->d_proff, &p->proff_cap, t.roff.data(), t.roff.size() * sizeof(long long))) !=
             HDD_NO_ERROR ||
@@ -318,6 +322,7 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, Pa
     p->pair_on_device = true;
   }
   out->rinfo = p->d_prinfo;
+  out->rinfo2 = p->d_prinfo2;
   out->roff = p->d_proff;
   out->rwords = p->d_prwords;
   out->prow = p->d_pprow;
@@ -330,6 +335,7 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, Pa
   out->stage = t.max_stage;
   out->nact = (int)p->chans.size();
   out->cc = t.cc;
+  out->g = t.g;
   out->npos = t.npos;
   return HDD_NO_ERROR;
 }
@@ -337,11 +343,12 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, Pa
 void plan_pair_release(hdd_plan p) {
   if (!p || !(p->d_prinfo || p->d_prows)) return;
   cudaSetDevice(p->device);
-  void **bufs[] = {(void **)&p->d_prinfo, (void **)&p->d_proff, (void **)&p->d_prwords, (void **)&p->d_pprow,
-                   (void **)&p->d_pprange, (void **)&p->d_prec, (void **)&p->d_ptile, (void **)&p->d_prows};
-  size_t *caps[] = {&p->prinfo_cap, &p->proff_cap, &p->prwords_cap, &p->pprow_cap,
+  void **bufs[] = {(void **)&p->d_prinfo, (void **)&p->d_prinfo2, (void **)&p->d_proff, (void **)&p->d_prwords,
+                   (void **)&p->d_pprow, (void **)&p->d_pprange, (void **)&p->d_prec, (void **)&p->d_ptile,
+                   (void **)&p->d_prows};
+  size_t *caps[] = {&p->prinfo_cap, &p->prinfo2_cap, &p->proff_cap, &p->prwords_cap, &p->pprow_cap,
                     &p->pprange_cap, &p->prec_cap, &p->ptile_cap, &p->prows_cap};
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 0; i < 9; ++i) {
     cudaFree(*bufs[i]);
     *bufs[i] = nullptr;
     *caps[i] = 0;
@@ -351,16 +358,19 @@ void plan_pair_release(hdd_plan p) {
 
 hdd_error plan_pair_row_ends(hdd_plan p, int count, int *ends) {
   if (p->pair_first != 0 || count > p->pair_count) return HDD_UNKNOWN_ERROR;
-  pair_row_ends(p->pair, p->delays.data(), p->nchans, p->chans.data(), (int)p->chans.size(), 0, count, ends);
+  pair_row_ends(p->pair, count, ends);
   return HDD_NO_ERROR;
 }
 
 void use_pair_tables(DedispArgs *a, const PairDeviceTables &t) {
   a->dpt = kPairDPT;
-  a->mode = 5;
+  a->mode = t.g == 4 ? 6 : 5;
   a->cc = t.cc;
   a->nact = t.nact;
+  a->pair_g = t.g;
+  a->pair_lanecap = pair_lanecap(t.g);
   a->pair_rinfo = t.rinfo;
+  a->pair_rinfo2 = t.rinfo2;
   a->pair_roff = t.roff;
   a->pair_rwords = t.rwords;
   a->pair_prow = t.prow;
@@ -467,6 +477,7 @@ void hdd_destroy_plan(hdd_plan p) {
   cudaFree(p->d_sindex);
   cudaFree(p->d_spool);
   cudaFree(p->d_prinfo);
+  cudaFree(p->d_prinfo2);
   cudaFree(p->d_proff);
   cudaFree(p->d_prwords);
   cudaFree(p->d_pprow);
@@ -489,9 +500,10 @@ hdd_error hdd_set_device(int device_idx) {
   return HDD_NO_ERROR;
 }
 
-hdd_error hdd_set_pair_rows(hdd_plan p, int enable) {
+hdd_error hdd_set_pair_rows(hdd_plan p, int channels) {
   if (!p) return HDD_INVALID_PLAN;
-  p->pair_rows = enable != 0;
+  if (channels != 0 && channels != 1 && channels != 2 && channels != 4) return HDD_UNKNOWN_ERROR;
+  p->pair_rows = channels == 1 ? 2 : channels;
   if (!p->pair_rows) hg::plan_pair_release(p);
   return HDD_NO_ERROR;
 }
@@ -627,8 +639,8 @@ hdd_error hdd_execute_guru(hdd_plan p, hdd_size nsamps, const hdd_byte *in, hdd_
   bool done = false;
   if (a.nact > 0 && p->pair_rows) {  // pair rows, 8 pairs a stage
     hg::PairDeviceTables pt;
-    if ((e = hg::plan_pair_tables(p, (int)first_dm_idx, (int)dm_count, 8, hg::dedisp_time_tiles(nout), &pt)) !=
-        HDD_NO_ERROR)
+    if ((e = hg::plan_pair_tables(p, (int)first_dm_idx, (int)dm_count, 8, hg::dedisp_time_tiles(nout),
+                                  p->pair_rows, &pt)) != HDD_NO_ERROR)
       return e;
     hg::DedispArgs pa = hg::single_beam_args(hg::DeviceTables{nullptr, nullptr, hg::kPairDPT, 0, pt.nact, 8},
                                              p->d_packed, R, 0, (int)first_dm_idx, (int)dm_count, nout, dout,

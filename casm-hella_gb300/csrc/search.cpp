@@ -249,15 +249,15 @@ hella_status dedisperse_beam(hella_ctx *c, int beam, const hella_tuning &t) {
     CK(e);
     return HELLA_OK;
   }
-  if (t.add_mode == 5) {  // pair rows: tables and a row buffer of their own, 16-trial tiles
-    const int cc = t.chan_chunk / 2, ntt = hg::dedisp_time_tiles(c->ntime_dd);
+  if (t.add_mode >= 5) {  // rows of channel pairs (5) or quads (6): tables and a row buffer of their own
+    const int g = t.add_mode == 6 ? 4 : 2, cc = t.chan_chunk / 2, ntt = hg::dedisp_time_tiles(c->ntime_dd);
     if (c->p.hbm_budget) {  // the rows are not in the creation-time estimate
       size_t bytes = 0;
-      if (hg::plan_pair_bytes(c->plan, 0, c->ndms, cc, ntt, &bytes) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
+      if (hg::plan_pair_bytes(c->plan, 0, c->ndms, cc, ntt, g, &bytes) != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
       if (c->dev_bytes + bytes > c->p.hbm_budget) return HELLA_ERR_BUDGET;
     }
     hg::PairDeviceTables pt;
-    const hdd_error he = hg::plan_pair_tables(c->plan, 0, c->ndms, cc, ntt, &pt);
+    const hdd_error he = hg::plan_pair_tables(c->plan, 0, c->ndms, cc, ntt, g, &pt);
     if (he == HDD_MEM_ALLOC_FAILED) return HELLA_ERR_ALLOC;
     if (he != HDD_NO_ERROR) return HELLA_ERR_DEDISP;
     if (pt.nact == 0) {
@@ -317,7 +317,7 @@ hella_status autotune(hella_ctx *c, int reps, hella_tuning *out, float *out_ms) 
       &best_ms);
   if (s != HELLA_OK) return s;
   c->tune = best;
-  if (best.add_mode != 5) hg::plan_pair_release(c->plan);  // the rows are only kept for add mode 5
+  if (best.add_mode < 5) hg::plan_pair_release(c->plan);  // the rows are only kept for add modes 5 and 6
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
   return HELLA_OK;
@@ -729,7 +729,7 @@ hella_status hella_set_tuning(hella_ctx *c, const hella_tuning *t) {
   if (!c || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
   c->tune = *t;
   c->tune.samples_per_thread = 4;
-  if (t->add_mode != 5) hg::plan_pair_release(c->plan);
+  if (t->add_mode < 5) hg::plan_pair_release(c->plan);
   return HELLA_OK;
 }
 

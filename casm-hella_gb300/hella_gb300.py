@@ -312,8 +312,9 @@ class Plan:
     def set_stream(self, stream: int):
         _chk_hdd(self.L.hdd_set_stream(self.h, stream))
 
-    def set_pair_rows(self, on: bool):
-        _chk_hdd(self.L.hdd_set_pair_rows(self.h, int(bool(on))))
+    def set_pair_rows(self, channels):
+        """0 / False: channel by channel; 2 / True: pair rows; 4: rows of four channels."""
+        _chk_hdd(self.L.hdd_set_pair_rows(self.h, int(channels)))
 
     @property
     def dm_count(self) -> int:

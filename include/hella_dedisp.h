@@ -93,16 +93,19 @@ hdd_error hdd_generate_dm_list(hdd_plan plan, hdd_float dm_start,
                                hdd_float dm_end, hdd_float ti, hdd_float tol);
 /* killmask[c] == 0 drops channel c from every sum. */
 hdd_error hdd_set_killmask(hdd_plan plan, const hdd_bool *killmask);
-/* hdd_set_pair_rows -- no counterpart in the reference.  enable != 0: the
- * execute calls dedisperse from pair rows (adjacent active channels summed
- * once per call and relative delay into rows in device memory, then summed
- * by 16-trial tiles): the same sums, about 1.5x faster on long DM lists,
- * for the rows' device memory (about 5.8 GB for 2048 channels, DM 0-2000,
- * 66048 output samples), which the plan holds until the mode is switched
- * off or the plan is destroyed.  A DM list whose stages do not fit shared
- * memory falls back to the channel-by-channel kernel; a failed allocation
- * returns HDD_MEM_ALLOC_FAILED.  hdd_execute_noalloc does not use it. */
-hdd_error hdd_set_pair_rows(hdd_plan plan, int enable);
+/* hdd_set_pair_rows -- no counterpart in the reference.  channels = 2 (or
+ * 1): the execute calls dedisperse from pair rows (adjacent active channels
+ * summed once per call and relative delay into rows in device memory, then
+ * summed by 16-trial tiles); 4: from rows of four channels; 0: channel by
+ * channel (the default); anything else: HDD_UNKNOWN_ERROR.  The same sums,
+ * about 1.5x (pairs) to 1.7x (quads) faster on long DM lists, for the rows'
+ * device memory (pairs: about 5.8 GB for 2048 channels, DM 0-2000, 66048
+ * output samples; quads about 3x that), which the plan holds until the mode
+ * is switched off or the plan is destroyed.  A DM list whose stages do not
+ * fit shared memory falls back to the channel-by-channel kernel; a failed
+ * allocation returns HDD_MEM_ALLOC_FAILED.  hdd_execute_noalloc does not
+ * use it. */
+hdd_error hdd_set_pair_rows(hdd_plan plan, int channels);
 
 hdd_size hdd_get_max_delay(const hdd_plan plan);
 hdd_size hdd_get_dm_delay(const hdd_plan plan, int dm_trial);

@@ -125,10 +125,14 @@ typedef struct {
                              once per window and relative delay into rows
                              in device memory, then summed by 16-trial tiles
                              (dm_per_block 0 or 16; chan_chunk/2 pairs per
-                             stage).  Single-beam contexts only; the rows
-                             (about 5.8 GB for 2048 channels, DM 0-2000,
-                             gulp 65536) are held while the mode is set and
-                             count against hbm_budget (HELLA_ERR_BUDGET) */
+                             stage; the batched context builds and sums the
+                             beams one after another in one row buffer);
+                             6: as 5 with rows of four channels (about 3x
+                             the rows, half the shared-memory reads).  The
+                             rows (mode 5: about 5.8 GB for 2048 channels,
+                             DM 0-2000, gulp 65536; mode 6: 19 GB) are held
+                             while the mode is set and count against
+                             hbm_budget (HELLA_ERR_BUDGET) */
 } hella_tuning;
 
 /* Derived sizes (casm_hella_refactored.cu:184-224). */

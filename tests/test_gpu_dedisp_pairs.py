@@ -1,6 +1,7 @@
-"""Add mode 5 of the dedispersion: pair rows.  Adjacent active channels are
-summed once per window and relative delay into rows in HBM, and each
-16-trial tile sums the rows of its trials' relative delays.  Integer sums
+"""Add modes 5 and 6 of the dedispersion: rows of channel pairs / quads.
+Adjacent active channels are summed once per window and pattern of
+relative delays into rows in HBM, and each 16-trial tile sums the rows of
+its trials' patterns.  Integer sums
 in any grouping are the same numbers, so every plane must be bit-exact
 against the oracle's channel-by-channel sums and against the other add
 modes: odd active-channel counts (the last channel alone), pairs of
@@ -17,6 +18,8 @@ pytestmark = pytest.mark.gpu
 
 MODE5 = (0, 4, 8, 0, 8, 5)     # dm_per_block, samples, chan_chunk, stages, group, add_mode
 MODE5_16 = (16, 4, 16, 0, 8, 5)
+MODE6 = (16, 4, 16, 0, 8, 6)     # rows of four channels
+MODE6_8 = (0, 4, 8, 0, 8, 6)
 
 
 def _window(hella, params, sky, killmask=None, gulps=None):
@@ -40,7 +43,7 @@ def _oracle_plane(oracle, params, s, win, killmask):
     return oracle.dedisperse(win, delays, killmask=killmask, nout=s.info.ntime_dd)
 
 
-@pytest.mark.parametrize("shape", [MODE5, MODE5_16])
+@pytest.mark.parametrize("shape", [MODE5, MODE5_16, MODE6, MODE6_8])
 @pytest.mark.parametrize("nchan,dm_max,kill", [(128, 400.0, 0), (160, 300.0, 1), (256, 1000.0, 2), (96, 60.0, 3),
                                                (64, 800.0, 4)])
 def test_pair_rows_planes_exact(hella, oracle, nchan, dm_max, kill, shape):
@@ -74,12 +77,13 @@ def test_pair_rows_planes_exact(hella, oracle, nchan, dm_max, kill, shape):
     s.close()
 
 
-def test_pair_rows_window_wraps(hella, oracle):
+@pytest.mark.parametrize("shape", [MODE5, MODE6])
+def test_pair_rows_window_wraps(hella, oracle, shape):
     """Windows that start anywhere in the ring (gulps 3..6 of a ring of
     about two gulps): every window's plane exact."""
     params, sky = synth.config_plain(seed=61, nchan=96, gulp=1024, dm_max=200.0)
     s = hella.Search(hella.default_params(**params))
-    s.set_tuning(hella.HellaTuning(*MODE5))
+    s.set_tuning(hella.HellaTuning(*shape))
     checked = 0
     for g in range(s.info.min_gulp + 5):
         s.clear_peaks()
@@ -95,13 +99,14 @@ def test_pair_rows_window_wraps(hella, oracle):
     s.close()
 
 
-def test_pair_rows_gulp_loop_candidates(hella, oracle):
+@pytest.mark.parametrize("shape", [MODE5, MODE6])
+def test_pair_rows_gulp_loop_candidates(hella, oracle, shape):
     params, sky = synth.config_plain(seed=15, nchan=160, gulp=2048, dm_max=300.0)
     sky.bursts[0].amp *= 4
     km = (np.random.default_rng(15).random(params["nchan"]) > 0.15).astype(np.int32)
     s = hella.Search(hella.default_params(**params))
     s.set_killmask(km)
-    s.set_tuning(hella.HellaTuning(*MODE5))
+    s.set_tuning(hella.HellaTuning(*shape))
     pl = oracle_pipeline(oracle, params)
     pl.set_killmask(0, km)
     total = 0
@@ -117,20 +122,23 @@ def test_pair_rows_gulp_loop_candidates(hella, oracle):
 
 def test_pair_rows_full_beam(hella):
     """The full single beam (2048 channels, 2501 trials): the whole plane
-    identical to add mode 2's, both stage widths, and faster."""
+    identical to add mode 2's, both stage widths and both group sizes, and
+    faster."""
     params, sky = synth.config_full(seed=2)
     s = _window(hella, params, sky)
     s.set_tuning(hella.HellaTuning(0, 4, 8, 0, 8, 2))
     s.dedisperse(0)
     ref = s.copy_dedisp()
-    for shape in (MODE5, MODE5_16):
+    for shape in (MODE5, MODE5_16, MODE6):
         s.set_tuning(hella.HellaTuning(*shape))
         s.dedisperse(0)
         assert np.array_equal(s.copy_dedisp(), ref), shape
+    ms6 = s.time_dedisp(hella.HellaTuning(*MODE6), 3)
     ms5 = s.time_dedisp(hella.HellaTuning(*MODE5_16), 3)
     ms2 = s.time_dedisp(hella.HellaTuning(0, 4, 8, 0, 8, 2), 3)
-    print(f"full beam dedispersion: add mode 5 {ms5:.2f} ms (rows built and summed), add mode 2 {ms2:.2f} ms")
-    assert ms5 < ms2
+    print(f"full beam dedispersion (rows built and summed): add mode 6 {ms6:.2f} ms, add mode 5 {ms5:.2f} ms, "
+          f"add mode 2 {ms2:.2f} ms")
+    assert ms5 < ms2 and ms6 < ms2
     s.close()
 
 
@@ -167,7 +175,7 @@ def test_pair_rows_budget_and_batch(hella):
     s.close()
 
 
-@pytest.mark.parametrize("shape", [MODE5, MODE5_16])
+@pytest.mark.parametrize("shape", [MODE5, MODE5_16, MODE6])
 def test_pair_rows_batch_killmasks(hella, shape):
     """The batched context in add mode 5 (the plan's rows over every channel,
     killed channels packed as zeros, each beam building the rows its own DM
@@ -208,7 +216,7 @@ def test_pair_rows_batch_killmasks(hella, shape):
                 assert np.array_equal(bt.copy_dedisp(b), s.copy_dedisp()), (g, b)
             total += len(want)
     assert total > 0
-    assert bt.get_tuning().add_mode == 5
+    assert bt.get_tuning().add_mode == shape[5]
     bt.close()
     for s in singles:
         s.close()
@@ -240,14 +248,16 @@ def test_plan_api_pair_rows(hella, oracle):
     km = (np.random.default_rng(70).random(nch) > 0.07).astype(np.int32)
     plan.set_killmask(km)
     rng = np.random.default_rng(71)
-    for extra in (5000, 2300):
+    for extra, group in ((5000, 2), (2300, 2), (3100, 4)):
         x = rng.integers(0, 256, (plan.max_delay + extra, nch), dtype=np.uint8)
-        plan.set_pair_rows(False)
+        plan.set_pair_rows(0)
         ref = plan.dedisperse(x)
-        plan.set_pair_rows(True)
+        plan.set_pair_rows(group)
         got = plan.dedisperse(x)
         assert np.array_equal(got, ref), extra
         assert np.array_equal(got, oracle.dedisperse(x, plan.delay_table(), killmask=km, nout=extra)), extra
+    with pytest.raises(hella.HellaError):
+        plan.set_pair_rows(3)
     # a sub-range of trials, device pointers, asynchronous
     nsamps, nout = x.shape[0], x.shape[0] - plan.max_delay
     plan.set_stream(torch.cuda.current_stream().cuda_stream)
@@ -258,6 +268,6 @@ def test_plan_api_pair_rows(hella, oracle):
                       flags=hella.HDD_DEVICE_POINTERS | hella.HDD_ASYNC)
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), ref[first:first + count])
-    plan.set_pair_rows(False)
+    plan.set_pair_rows(0)
     assert np.array_equal(plan.dedisperse(x), ref)
     plan.close()

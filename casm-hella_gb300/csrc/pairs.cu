@@ -58,12 +58,12 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   const long P0 = (long)blockIdx.x * kBuildCH;
   const DedispBeam bm = a.beams ? a.beams[0] : a.one;
   const int r0 = a.pair_prow[k], r1 = a.pair_rend ? a.pair_rend[k] : a.pair_prow[k + 1];
-  bool any = false;
-  for (int r = r0; r < r1; ++r) {
-    const int4 in = a.pair_rinfo[r];
-    if (P0 < (long)in.w + a.pair_rwords[r] && P0 + kBuildCH > (long)in.w) any = true;
+  int any = 0;  // does a row of the group cover a position of this chunk?
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const int w = a.pair_rinfo[r].w;
+    any |= P0 < (long)w + a.pair_rwords[r] && P0 + kBuildCH > (long)w;
   }
-  if (!any) return;
+  if (!__syncthreads_or(any)) return;
   const int4 i0 = a.pair_rinfo[r0], j0 = a.pair_rinfo2[r0];
   const int ch[kPairGMax] = {i0.x, i0.y, G == 4 ? j0.x : -1, G == 4 ? j0.y : -1};  // -1: fewer channels
   const long R = a.R;
@@ -88,24 +88,26 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
     nwin += n;
   }
   __syncthreads();
-  for (int r = r0; r < r1; ++r) {
-    const int4 in = a.pair_rinfo[r], in2 = a.pair_rinfo2[r];
+  // one warp per row: the row's metadata is loaded once for 2048-4096 words
+  const int lane = threadIdx.x & 31;
+  for (int r = r0 + (threadIdx.x >> 5); r < r1; r += blockDim.x >> 5) {
+    const int4 in = a.pair_rinfo[r];
     const long lo = max(P0, (long)in.w), hi = min(P0 + kBuildCH, (long)in.w + a.pair_rwords[r]);
+    if (lo >= hi) continue;
+    const int4 in2 = G == 4 ? a.pair_rinfo2[r] : make_int4(-1, -1, 0, 0);
     uint32_t *dst = a.pair_rows + a.pair_roff[r];
     // word q of the chunk, q = p - P0, of channel i for this row's r_i
     const int s1 = off[1] + in.z - rmin[1], s2 = off[2] + in2.z - rmin[2], s3 = off[3] + in2.w - rmin[3];
     const int first = (int)(lo - P0), last = (int)(hi - P0), d0 = (int)(P0 - in.w);
     // rows are read back by other blocks much later: streaming stores
     if (G == 4 && ch[3] >= 0) {
-      for (int q = first + threadIdx.x; q < last; q += blockDim.x)
-        __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q] + sm[s3 + q]);
+      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q] + sm[s3 + q]);
     } else if (G == 4 && ch[2] >= 0) {
-      for (int q = first + threadIdx.x; q < last; q += blockDim.x)
-        __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q]);
+      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q]);
     } else if (ch[1] >= 0) {
-      for (int q = first + threadIdx.x; q < last; q += blockDim.x) __stcs(dst + d0 + q, sm[q] + sm[s1 + q]);
+      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q]);
     } else {
-      for (int q = first + threadIdx.x; q < last; q += blockDim.x) __stcs(dst + d0 + q, sm[q]);
+      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q]);
     }
   }
 }

@@ -50,6 +50,8 @@ DEDISP_TRAFFIC = {
     # rows of channel quads (add mode 6), 8 quads a stage, groups of 8: k_pair_build<4> 0.760 read +
     # 18.95 written, k_pair_sum 22.20 read + 0.657 written
     (16, 4, 16, 0, 8, 6): 42.57e9,
+    # the same in groups of 4 (the bench's shape): 0.737 + 18.94, 26.32 + 0.657
+    (16, 4, 16, 0, 4, 6): 46.65e9,
 }
 
 
@@ -282,11 +284,11 @@ def main():
         gi += 1
     torch.cuda.synchronize()
     # dedispersion: rows of channel quads (add mode 6: 16-trial tiles, 8 quads a stage, the deepest
-    # staging that fits, DM tiles walked in groups of 8 per time tile), 11.4 ms on the full beam;
-    # pairs (add mode 5) 12.5 ms; the channel-by-channel kernel's best shape (add mode 2, multiply-
-    # add odd lanes and addresses) 19.4 ms.  Shapes a DM list or the memory cannot take fall back
-    # in that order, then to add mode 0.
-    shapes = [hg.HellaTuning(16, 4, 16, 0, 8, m) for m in (6, 5) if m <= a.add_mode and a.add_mode >= 5]
+    # staging that fits, DM tiles walked in groups of 4 per time tile), 10.2 ms on the full beam
+    # (the autotuner's pick is within 0.1 %); pairs (add mode 5) 12.4 ms; the channel-by-channel
+    # kernel's best shape (add mode 2, multiply-add odd lanes and addresses) 19.4 ms.  Shapes a DM
+    # list or the memory cannot take fall back in that order, then to add mode 0.
+    shapes = [hg.HellaTuning(16, 4, 16, 0, 4 if m == 6 else 8, m) for m in (6, 5) if m <= a.add_mode and a.add_mode >= 5]
     shapes += [hg.HellaTuning(0, 4, 8, 0, 8, a.add_mode if a.add_mode < 5 else 2), hg.HellaTuning(0, 4, 8, 0, 8, 0)]
     for shape in shapes:
         try:

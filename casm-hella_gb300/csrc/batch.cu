@@ -169,7 +169,10 @@ struct hella_batch {
   hg::TableJob *d_bjobs = nullptr;
   size_t bmeta_cap = 0, boff_cap = 0, bchans_cap = 0, bjobs_cap = 0;
   int btab_dpt = -1, btab_cc = -1;  // tile shape of the per-beam tables; -1: rebuild
-  int *d_prend = nullptr;         // add mode 5: [nbeam][npair] end of the rows each beam builds
+  int *d_prend = nullptr;         // add modes 5, 6: [nbeam][npair] end of the rows each beam builds
+  uint32_t *d_krows = nullptr;    // add modes 5, 6: rows of kbeams beams, krows_words apart
+  long krows_words = 0;
+  int kbeams = 0;
   int prend_key = -1;             // shape (groups per stage, channels per group) of d_prend; -1: remake
   hella_tuning tune{0, 4, 8, 0, hg::kDedispGroup, 0};
   std::vector<Lane> lanes;
@@ -432,6 +435,17 @@ hella_status beam_tables(hella_batch *b, const hg::DeviceTables &tb) {
   return HELLA_OK;
 }
 
+// Frees the rows of add modes 5 and 6 (set up again on next use).
+void release_krows(hella_batch *b) {
+  if (b->d_krows) {
+    cudaFree(b->d_krows);
+    b->dev_bytes -= (size_t)b->kbeams * std::max<long>(b->krows_words, 4) * 4;
+  }
+  b->d_krows = nullptr;
+  b->krows_words = 0;
+  b->kbeams = 0;
+}
+
 // Dedispersion launch over all beams with tile shape t (tables uploaded).
 hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *out) {
   if (!hg::tuning_ok(t)) return HELLA_ERR_INVALID_ARG;
@@ -446,10 +460,27 @@ hella_status dedisp_args(hella_batch *b, const hella_tuning &t, hg::DedispArgs *
       if (b->dev_bytes + bytes + (size_t)b->nbeam * b->p.nchan * 2 > b->p.hbm_budget) return HELLA_ERR_BUDGET;
     }
     hg::PairDeviceTables pt;
-    const hdd_error he = hg::plan_pair_tables(b->plan, 0, b->z.ndms_all, cc, ntt, g, &pt);
+    const hdd_error he = hg::plan_pair_tables(b->plan, 0, b->z.ndms_all, cc, ntt, g, &pt, false);
     if (he == HDD_MEM_ALLOC_FAILED) return HELLA_ERR_ALLOC;
     if (he != HDD_NO_ERROR || pt.nact != b->p.nchan) return HELLA_ERR_DEDISP;  // the plan keeps every channel
     hella_status s;
+    if (b->krows_words != pt.words) {  // rows of up to kPairMaxBeams beams, as many as memory and budget allow
+      release_krows(b);
+      const size_t per = (size_t)std::max<long>(pt.words, 4) * 4;
+      for (int k = hg::kPairMaxBeams; k >= 1 && !b->d_krows; k /= 2) {
+        if (b->p.hbm_budget && b->dev_bytes + k * per > b->p.hbm_budget) continue;
+        if (cudaMalloc((void **)&b->d_krows, k * per) != cudaSuccess) {
+          cudaGetLastError();
+          b->d_krows = nullptr;
+          continue;
+        }
+        b->kbeams = k;
+        b->dev_bytes += k * per;
+      }
+      if (!b->d_krows) return b->p.hbm_budget ? HELLA_ERR_BUDGET : HELLA_ERR_ALLOC;
+      b->krows_words = pt.words;
+    }
+    pt.rows = b->d_krows;
     if (!b->d_prend && (s = dalloc(b, (void **)&b->d_prend, (size_t)b->nbeam * pt.npair * 4)) != HELLA_OK)
       return s;
     if (b->prend_key != cc * 16 + g) {
@@ -571,13 +602,16 @@ hella_status dedisperse_beams(hella_batch *b, const hg::DedispArgs &da) {
     CK(hg::dedisperse(da, b->stream));
     return HELLA_OK;
   }
-  for (int i = 0; i < b->nbeam; ++i) {
-    const int n = b->dbeams[i].dm_count;
-    if (n <= 0) continue;
+  for (int i = 0; i < b->nbeam; i += b->kbeams) {  // kbeams beams a build and a sum launch
+    const int nk = std::min(b->kbeams, b->nbeam - i);
+    int items = 0;
+    for (int z = 0; z < nk; ++z) items += hg::dedisp_items(b->dbeams[i + z].dm_count, hg::kPairDPT, da.ntt);
+    if (items == 0) continue;
     hg::DedispArgs a = da;
     a.beams = b->d_dbeams + i;
+    a.nbeam = nk;
     a.one = b->dbeams[i];
-    a.nitems = hg::dedisp_items(n, hg::kPairDPT, da.ntt);
+    a.nitems = items;
     a.pair_rend = b->d_prend + (size_t)i * da.pair_npair;
     const cudaError_t e = hg::dedisperse(a, b->stream);
     if (e == cudaErrorInvalidValue) {  // the DM list's stages do not fit this kernel's staging
@@ -685,7 +719,10 @@ hella_status autotune(hella_batch *b, int reps, hella_tuning *out, float *out_ms
       &best_ms);
   if (s != HELLA_OK) return s;
   b->tune = best;
-  if (best.add_mode < 5) hg::plan_pair_release(b->plan);  // the rows are only kept for add modes 5 and 6
+  if (best.add_mode < 5) {  // the rows are only kept for add modes 5 and 6
+    hg::plan_pair_release(b->plan);
+    release_krows(b);
+  }
   for (Lane &l : b->lanes) l.stale = true;
   if (out) *out = best;
   if (out_ms) *out_ms = best_ms;
@@ -724,7 +761,8 @@ void hella_batch_destroy(hella_batch *b) {
   }
   for (void *ptr : b->dallocs) cudaFree(ptr);
   for (void *ptr : b->hallocs) cudaFreeHost(ptr);
-  for (void *ptr : {(void *)b->d_bmeta, (void *)b->d_boff, (void *)b->d_bchans, (void *)b->d_bjobs})
+  for (void *ptr : {(void *)b->d_bmeta, (void *)b->d_boff, (void *)b->d_bchans, (void *)b->d_bjobs,
+                    (void *)b->d_krows})
     if (ptr) cudaFree(ptr);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
@@ -1075,7 +1113,10 @@ hella_status hella_batch_set_tuning(hella_batch *b, const hella_tuning *t) {
   if (!b || !t || !hg::tuning_ok(*t)) return HELLA_ERR_INVALID_ARG;
   if (any_busy(b)) return HELLA_ERR_STATE;
   b->tune = *t;
-  if (t->add_mode < 5) hg::plan_pair_release(b->plan);
+  if (t->add_mode < 5) {
+    hg::plan_pair_release(b->plan);
+    release_krows(b);
+  }
   b->tune.samples_per_thread = 4;
   for (Lane &l : b->lanes) l.stale = true;
   return HELLA_OK;

@@ -148,7 +148,8 @@ struct DedispArgs {
   const int4 *pair_rec;
   const int *pair_tile_st;
   uint32_t *pair_rows;
-  const int *pair_rend;     // [npair] end of the rows to build per group (null: all rows)
+  const int *pair_rend;     // [nbeam][npair] end of the rows to build per group (null: all rows)
+  long pair_rows_stride;    // words between the rows of consecutive beams of the launch
   int pair_npair, pair_span, pair_stage, pair_g, pair_lanecap;
   long pair_npos;
 };
@@ -217,6 +218,7 @@ size_t dedisp_sub_smem(int max_spread, int max_words, int max_rec, int nbuf);
 constexpr int kPairDPT = 16;
 constexpr int kPairRowsMax = 32;  // rows per stage: one per lane of the staging warp
 constexpr int kPairGMax = 4;      // channels per group
+constexpr int kPairMaxBeams = 4;  // beams one pair of launches serves (batched context)
 // Groups per 16-bit lane before widening: lanecap x g x 255 < 2^16.
 inline int pair_lanecap(int g) { return 65535 / (255 * g); }
 __host__ __device__ constexpr int pair_rec_int4(int cc) { return 1 + cc * kPairDPT / 4 + kPairRowsMax; }
@@ -247,8 +249,11 @@ PairTables dedisp_pair_tables(const int *delays_host, int nchan, const int *chan
 // (a beam whose DM ceiling cuts the list builds those rows only).
 void pair_row_ends(const PairTables &t, int count, int *ends);
 // Builds the rows, then sums them (two launches); `a` is a launch with mode
-// 5 or 6 and dpt 16 over one beam: `one`, or beams[0] read on the device
-// (the batched context, whose ring positions the device advances).
+// 5 or 6 and dpt 16 over one beam, `one`, or over beams[0 .. nbeam) read on
+// the device (the batched context, whose ring positions the device
+// advances; up to kPairMaxBeams beams, their rows pair_rows_stride words
+// apart, their items one after another from beams[0].item0, beam z's row
+// ends at pair_rend + z * npair).
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s);
 // Largest delay spread over the active channels of any dpt-trial tile.
 int dedisp_spread(const int *delays_host, int nchan, const int *chans_host, int nact,

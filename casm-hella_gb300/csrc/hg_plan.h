@@ -51,9 +51,11 @@ struct PairDeviceTables {
   const int *tile_st;
   uint32_t *rows;
   int npair, span, stage, nact, cc, g;
-  long npos;
+  long npos, words;  // positions the rows cover; words of one beam's rows
 };
-hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out);
+// rows = false: the tables only (the caller holds the rows; `rows` is null).
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out,
+                           bool rows = true);
 // Frees the add-mode-5 device tables and rows (set up again on next use).
 void plan_pair_release(hdd_plan p);
 // Device bytes those tables and their rows take (builds the host copy).

@@ -54,10 +54,11 @@ template <int G>
 __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
   constexpr int kBuildCH = build_chunk(G);
-  const int k = blockIdx.y;
+  const int k = blockIdx.y, z = blockIdx.z;  // group, beam of the launch
   const long P0 = (long)blockIdx.x * kBuildCH;
-  const DedispBeam bm = a.beams ? a.beams[0] : a.one;
-  const int r0 = a.pair_prow[k], r1 = a.pair_rend ? a.pair_rend[k] : a.pair_prow[k + 1];
+  const DedispBeam bm = a.beams ? a.beams[z] : a.one;
+  const int r0 = a.pair_prow[k];
+  const int r1 = a.pair_rend ? a.pair_rend[(size_t)z * a.pair_npair + k] : a.pair_prow[k + 1];
   int any = 0;  // does a row of the group cover a position of this chunk?
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int w = a.pair_rinfo[r].w;
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
     const long lo = max(P0, (long)in.w), hi = min(P0 + kBuildCH, (long)in.w + a.pair_rwords[r]);
     if (lo >= hi) continue;
     const int4 in2 = G == 4 ? a.pair_rinfo2[r] : make_int4(-1, -1, 0, 0);
-    uint32_t *dst = a.pair_rows + a.pair_roff[r];
+    uint32_t *dst = a.pair_rows + (size_t)z * a.pair_rows_stride + a.pair_roff[r];
     // word q of the chunk, q = p - P0, of channel i for this row's r_i
     const int s1 = off[1] + in.z - rmin[1], s2 = off[2] + in2.z - rmin[2], s3 = off[3] + in2.w - rmin[3];
     const int first = (int)(lo - P0), last = (int)(hi - P0), d0 = (int)(P0 - in.w);
@@ -127,8 +128,6 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   constexpr int NWARP = kDedispThreads / 32;
   constexpr int HB = stage_hdr_bytes(CC);
   const int REC = pair_rec_int4(CC);
-  const DedispBeam bm = a.beams ? a.beams[0] : a.one;
-  const int ntiles = (bm.dm_count + DPT - 1) / DPT;
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   auto full_of = [&](int b) { return sbase + 8u * b; };
   auto empty_of = [&](int b) { return sbase + 32u + 8u * b; };
@@ -136,7 +135,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // the stage a warp stages next: stage st of the nst stages of block-local item k
   struct Cursor {
-    int k, st, s0, nst, t0;
+    int k, st, s0, nst, t0, z;  // z: beam of the item in the launch
   };
   static_assert(64 + NWARP * sizeof(Cursor) <= kBarHdr, "staging cursors");
   Cursor *cur = reinterpret_cast<Cursor *>(reinterpret_cast<char *>(smem) + 64) + warp;
@@ -150,13 +149,29 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   __syncthreads();
   if (blockIdx.x >= a.nitems) return;
 
+  // Beam z of launch item `item` and the item's tile and time tile: the
+  // items of the launch's beams follow one another (beam z's from
+  // beams[z].item0 - beams[0].item0 on; a beam without trials has none).
+  auto locate = [&](int item, int *z, int *tile, int *tt) -> DedispBeam {
+    int zz = 0;
+    DedispBeam bz = a.one;
+    if (a.beams) {
+      const int g = a.beams[0].item0 + item;
+      while (zz + 1 < a.nbeam && a.beams[zz + 1].item0 <= g) ++zz;
+      bz = a.beams[zz];
+      item = g - bz.item0;
+    }
+    *z = zz;
+    pair_item(a, (bz.dm_count + DPT - 1) / DPT, item, tile, tt);
+    return bz;
+  };
   auto load_item = [&](int k) -> bool {  // lane 0
     const int item = blockIdx.x + k * gridDim.x;
     if (item >= a.nitems) return false;
-    int tile, tt;
-    pair_item(a, ntiles, item, &tile, &tt);
+    int z, tile, tt;
+    locate(item, &z, &tile, &tt);
     const int s0 = a.pair_tile_st[tile];
-    *cur = Cursor{k, 0, s0, a.pair_tile_st[tile + 1] - s0, tt * kTileSamples};
+    *cur = Cursor{k, 0, s0, a.pair_tile_st[tile + 1] - s0, tt * kTileSamples, z};
     return true;
   };
   auto advance = [&](int n) -> bool {  // lane 0
@@ -200,7 +215,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
       const long start = (long)(((unsigned long long)(unsigned)rw.y << 32) | (unsigned)rw.x);
       const uint32_t nb = (uint32_t)rw.z * 4u;
       mbar_arrive_tx(bar, nb + (lane == 0 ? (uint32_t)HB : 0u));
-      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, a.pair_rows + start + t0, nb, bar);
+      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, a.pair_rows + (size_t)cur->z * a.pair_rows_stride + start + t0, nb,
+               bar);
       if (lane == 0) bulk_g2s(buf_of(b), r, HB, bar);
     } else {
       mbar_arrive(bar);
@@ -222,8 +238,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
 
   unsigned gs_c = 0;  // stages consumed
   for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
-    int tile, tt;
-    pair_item(a, ntiles, item, &tile, &tt);
+    int z, tile, tt;
+    const DedispBeam bm = locate(item, &z, &tile, &tt);
     const int nstage = a.pair_tile_st[tile + 1] - a.pair_tile_st[tile];
     uint32_t acc_a[DPT], acc_b[DPT], tot[DPT][4];  // acc_a: samples j, j+512; acc_b: j+256, j+768
 #pragma unroll
@@ -500,7 +516,8 @@ void pair_row_ends(const PairTables &t, int count, int *ends) {
 
 cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
   const int g = a.pair_g;
-  if ((a.beams && a.nbeam != 1) || a.dpt != kPairDPT || (a.mode != 5 && a.mode != 6) || (g != 2 && g != 4) ||
+  if ((a.beams && (a.nbeam < 1 || a.nbeam > kPairMaxBeams || (a.nbeam > 1 && a.pair_rows_stride <= 0))) ||
+      a.dpt != kPairDPT || (a.mode != 5 && a.mode != 6) || (g != 2 && g != 4) ||
       !a.pair_rows || !a.pair_rec || !a.pair_tile_st || !a.pair_rinfo || !a.pair_rinfo2 || !a.pair_roff ||
       !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 || a.pair_npair > 65535 ||
       a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0 || a.pair_lanecap < 1 ||
@@ -514,7 +531,7 @@ cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
   auto kern = g == 4 ? k_pair_build<4> : k_pair_build<2>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
   if (e != cudaSuccess) return e;
-  const dim3 grid((unsigned)((a.pair_npos + ch - 1) / ch), (unsigned)a.pair_npair);
+  const dim3 grid((unsigned)((a.pair_npos + ch - 1) / ch), (unsigned)a.pair_npair, (unsigned)(a.beams ? a.nbeam : 1));
   kern<<<grid, 256, bsmem, s>>>(a);
   count_launches(1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -292,7 +292,8 @@ hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, int
   return HDD_NO_ERROR;
 }
 
-hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out) {
+hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out,
+                           bool rows) {
   hdd_error e = pair_host_tables(p, first, count, cc, ntt, g);
   if (e != HDD_NO_ERROR) return e;
   const PairTables &t = p->pair;
@@ -316,11 +317,13 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, in
             HDD_NO_ERROR ||
         (e = up((void **)&p->d_prec, &p->prec_cap, t.rec.data(), t.rec.size() * sizeof(int4))) != HDD_NO_ERROR ||
         (e = up((void **)&p->d_ptile, &p->ptile_cap, t.tile_st.data(), t.tile_st.size() * sizeof(int))) !=
-            HDD_NO_ERROR ||
-        (e = grow((void **)&p->d_prows, &p->prows_cap, std::max<size_t>((size_t)t.words, 4) * 4)) != HDD_NO_ERROR)
+            HDD_NO_ERROR)
       return e;
     p->pair_on_device = true;
   }
+  if (rows && (e = grow((void **)&p->d_prows, &p->prows_cap, std::max<size_t>((size_t)t.words, 4) * 4)) !=
+                  HDD_NO_ERROR)
+    return e;
   out->rinfo = p->d_prinfo;
   out->rinfo2 = p->d_prinfo2;
   out->roff = p->d_proff;
@@ -329,7 +332,8 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, in
   out->prange = p->d_pprange;
   out->rec = p->d_prec;
   out->tile_st = p->d_ptile;
-  out->rows = p->d_prows;
+  out->rows = rows ? p->d_prows : nullptr;
+  out->words = t.words;
   out->npair = t.npair;
   out->span = t.max_span;
   out->stage = t.max_stage;
@@ -378,6 +382,7 @@ void use_pair_tables(DedispArgs *a, const PairDeviceTables &t) {
   a->pair_rec = t.rec;
   a->pair_tile_st = t.tile_st;
   a->pair_rows = t.rows;
+  a->pair_rows_stride = t.words;
   a->pair_npair = t.npair;
   a->pair_span = t.span;
   a->pair_stage = t.stage;

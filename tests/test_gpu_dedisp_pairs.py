@@ -271,3 +271,45 @@ def test_plan_api_pair_rows(hella, oracle):
     plan.set_pair_rows(0)
     assert np.array_equal(plan.dedisperse(x), ref)
     plan.close()
+
+
+@pytest.mark.parametrize("shape", [MODE5, MODE6])
+def test_pair_rows_batch_chunks(hella, shape):
+    """19 beams: rows built and summed 4 beams per launch pair (4 x 4 + 3),
+    DM ceilings from 60 to 300 and killmasks differing per beam; every
+    beam's plane and candidates identical to its single-beam context."""
+    nb, nch = 19, 64
+    params, _ = synth.config_plain(seed=95, nchan=nch, gulp=1024, dm_max=300.0)
+    rng = np.random.default_rng(96)
+    ceilings = rng.uniform(60.0, 300.0, nb).astype(np.float32)
+    ceilings[[0, 9]] = 300.0
+    kill = (rng.random((nb, nch)) > rng.uniform(0, 0.15, (nb, 1))).astype(np.int32)
+    skies = []
+    for b in range(nb):
+        sk = synth.config_plain(seed=97 + b, nchan=nch, gulp=1024, dm_max=float(ceilings[b]))[1]
+        sk.bursts[0].amp *= 4
+        skies.append(sk)
+    bt = hella.Batch(hella.default_params(**dict(params, nbeam=nb)), dm_max=ceilings, killmask=kill)
+    bt.set_tuning(hella.HellaTuning(*shape))
+    singles = []
+    for b in range(nb):
+        s = hella.Search(hella.default_params(**dict(params, dm_max=float(ceilings[b]), beam0=b, nbeam=1)))
+        s.set_killmask(kill[b])
+        singles.append(s)
+    total = 0
+    for g in range(max(s.info.min_gulp for s in singles) + 2):
+        x = synth.multibeam_gulp(skies, g, params["gulp"])
+        got, counts, searched = bt.process_gulp(x)
+        off = 0
+        for b, s in enumerate(singles):
+            want, sw = s.process_gulp(x[b:b + 1])
+            mine = got[off:off + counts[b]]
+            off += counts[b]
+            assert searched[b] == sw and cands_equal(mine, want), (g, b)
+            if sw:
+                assert np.array_equal(bt.copy_dedisp(b), s.copy_dedisp()), (g, b)
+            total += len(want)
+    assert total > 0
+    bt.close()
+    for s in singles:
+        s.close()

@@ -21,7 +21,10 @@ def _ew(prev, bp):
     return (prev + (a * (bp - prev).astype(np.float32)).astype(np.float32)).astype(np.float32)
 
 
-def test_stream_join_leave_matches_fresh_contexts(hella):
+@pytest.mark.parametrize("add_mode", [None, 6])
+def test_stream_join_leave_matches_fresh_contexts(hella, add_mode):
+    """add_mode 6: the dedispersion through quad rows, built and summed for
+    several slots per launch pair, slots without trials among them."""
     params, _ = synth.config_plain(seed=80, nchan=128, gulp=2048, dm_max=400.0)
     rng = np.random.default_rng(80)
     skies = []
@@ -32,6 +35,8 @@ def test_stream_join_leave_matches_fresh_contexts(hella):
     base = hella.default_params(**dict(params, nbeam=NS))
     member = [1, 1, 1, 0, 0]
     bt = hella.Batch(base, dynamic=True, member=member, inflight=2, bp_alpha=ALPHA)
+    if add_mode:
+        bt.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, add_mode))
     # membership events before gulp g: (slot, member, dm_max, killmask)
     km3 = (rng.random(128) > 0.08).astype(np.int32)
     events = {3: [(3, 1, 250.0, km3)], 5: [(1, 0, 0.0, None)], 6: [(4, 1, 400.0, None)]}

@@ -121,7 +121,9 @@ __device__ __forceinline__ void pair_item(const DedispArgs &a, int ntiles, int l
   *tile = g * a.group + (r - *tt * gsz);
 }
 
-template <int CC>
+// MULTI: the launch serves several beams (a.beams, batched context): each
+// item looks up its beam; else the one beam's record stays in registers.
+template <int CC, bool MULTI>
 __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, int bufbytes, int nbuf) {
   extern __shared__ __align__(128) uint32_t smem[];
   constexpr int DPT = kPairDPT;
@@ -152,10 +154,11 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   // Beam z of launch item `item` and the item's tile and time tile: the
   // items of the launch's beams follow one another (beam z's from
   // beams[z].item0 - beams[0].item0 on; a beam without trials has none).
+  const DedispBeam b0 = MULTI ? a.one : (a.beams ? a.beams[0] : a.one);
   auto locate = [&](int item, int *z, int *tile, int *tt) -> DedispBeam {
     int zz = 0;
-    DedispBeam bz = a.one;
-    if (a.beams) {
+    DedispBeam bz = b0;
+    if (MULTI) {
       const int g = a.beams[0].item0 + item;
       while (zz + 1 < a.nbeam && a.beams[zz + 1].item0 <= g) ++zz;
       bz = a.beams[zz];
@@ -215,8 +218,8 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
       const long start = (long)(((unsigned long long)(unsigned)rw.y << 32) | (unsigned)rw.x);
       const uint32_t nb = (uint32_t)rw.z * 4u;
       mbar_arrive_tx(bar, nb + (lane == 0 ? (uint32_t)HB : 0u));
-      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, a.pair_rows + (size_t)cur->z * a.pair_rows_stride + start + t0, nb,
-               bar);
+      const uint32_t *rows = MULTI ? a.pair_rows + (size_t)cur->z * a.pair_rows_stride : a.pair_rows;
+      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, rows + start + t0, nb, bar);
       if (lane == 0) bulk_g2s(buf_of(b), r, HB, bar);
     } else {
       mbar_arrive(bar);
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
   }
 }
 
-template <int CC>
+template <int CC, bool MULTI>
 cudaError_t launch_sum(const DedispArgs &a, cudaStream_t s) {
   const int bufbytes = stage_hdr_bytes(CC) + a.pair_stage;
   int nbuf = a.nbuf;
@@ -350,7 +353,7 @@ cudaError_t launch_sum(const DedispArgs &a, cudaStream_t s) {
   if (nbuf < 2 || nbuf > kMaxBuf) return cudaErrorInvalidValue;
   const size_t smem = kBarHdr + (size_t)nbuf * bufbytes;
   if (smem > 227 * 1024) return cudaErrorInvalidValue;
-  auto kern = k_pair_sum<CC>;
+  auto kern = k_pair_sum<CC, MULTI>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -535,9 +538,12 @@ cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
   kern<<<grid, 256, bsmem, s>>>(a);
   count_launches(1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  switch (a.cc) {
-    case 4: return launch_sum<4>(a, s);
-    case 8: return launch_sum<8>(a, s);
+  const bool multi = a.beams && a.nbeam > 1;
+  switch (a.cc * 2 + (multi ? 1 : 0)) {
+    case 8: return launch_sum<4, false>(a, s);
+    case 9: return launch_sum<4, true>(a, s);
+    case 16: return launch_sum<8, false>(a, s);
+    case 17: return launch_sum<8, true>(a, s);
   }
   return cudaErrorInvalidValue;
 }

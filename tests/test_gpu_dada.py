@@ -43,13 +43,18 @@ def test_dada_flagger_bit_exact(hella, oracle, entries):
         s.rewind()
 
 
-def test_dada_gulp_loop_and_batch(hella, oracle):
+@pytest.mark.parametrize("add_mode", [None, 6])
+def test_dada_gulp_loop_and_batch(hella, oracle, add_mode):
+    """add_mode 6: both contexts dedisperse through quad rows."""
     params, _ = synth.config_plain(seed=43, nchan=128, gulp=2048, dm_max=400.0)
     skies = [synth.config_plain(seed=44 + b, nchan=128, gulp=2048, dm_max=400.0)[1] for b in range(2)]
     for sk in skies:
         sk.bursts[0].amp *= 3
     s = hella.Search(hella.default_params(**dict(params, nbeam=2), input_format=1))
     bt = hella.Batch(hella.default_params(**dict(params, nbeam=2), input_format=1))
+    if add_mode:
+        s.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, add_mode))
+        bt.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, add_mode))
     pl = oracle_pipeline(oracle, params, nbeam=2)
     total = 0
     for g in range(pl.min_gulp + 2):

@@ -63,8 +63,9 @@ DM_TOL = 2.0  # scripts/verify_injection_fil.py:30-40: loudest candidate within 
 
 
 def test_full_beam_candidates_and_injection_recovery(hella, oracle):
-    """The benchmarked workload end to end: the first searched gulp's
-    candidate list bit-exact against the oracle pipeline, and every injected
+    """The benchmarked workload end to end, with the benchmark's tile shape
+    (quad rows): the first searched gulp's candidate list bit-exact against
+    the oracle pipeline, and every injected
     burst of injected S/N >= 12 recovered by the reference's criterion,
     applied per burst: the loudest candidate within wmax samples of its
     arrival (DM above 20, clear of the broadband spikes) lies within DM_TOL
@@ -73,6 +74,7 @@ def test_full_beam_candidates_and_injection_recovery(hella, oracle):
     params, sky = synth.config_full(seed=2)
     G, wmax = params["gulp"], params["width_max"]
     s = hella.Search(hella.default_params(**params))
+    s.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, 6))  # the benchmark's dedispersion: quad rows
     oracle.set_threads(0)
     pl = oracle_pipeline(oracle, params)
     for g in range(pl.min_gulp + 1):

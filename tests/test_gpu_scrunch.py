@@ -40,7 +40,9 @@ def test_scrunch_flagger_bit_exact(hella, oracle, entries, flags):
     assert fspec.max() > 0
 
 
-def test_scrunch_gulp_loop_and_batch(hella, oracle):
+@pytest.mark.parametrize("add_mode", [None, 6])
+def test_scrunch_gulp_loop_and_batch(hella, oracle, add_mode):
+    """add_mode 6: both contexts dedisperse through quad rows."""
     params, _ = synth.config_plain(seed=33, nchan=128, gulp=2048, dm_max=400.0)
     skies = [synth.config_plain(seed=34 + b, nchan=128, gulp=2048, dm_max=400.0)[1] for b in range(2)]
     for sk in skies:
@@ -48,6 +50,9 @@ def test_scrunch_gulp_loop_and_batch(hella, oracle):
     s = hella.Search(hella.default_params(**dict(params, nbeam=2), scrunches=SCR[:2]))
     pl = oracle_pipeline(oracle, params, nbeam=2, scrunches=SCR[:2])
     bt = hella.Batch(hella.default_params(**dict(params, nbeam=2), scrunches=SCR[:2]))
+    if add_mode:
+        s.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, add_mode))
+        bt.set_tuning(hella.HellaTuning(16, 4, 16, 0, 4, add_mode))
     # flag statistics fed from the device's cumulative flag spectrum each gulp
     # (casm_hella_refactored.cu:708-716), counted like the host model below
     ntime = s.info.ntime

@@ -56,6 +56,8 @@ struct PairDeviceTables {
 // rows = false: the tables only (the caller holds the rows; `rows` is null).
 hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, int g, PairDeviceTables *out,
                            bool rows = true);
+// Builds (or keeps) the plan's host group-row tables for that range and shape.
+hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt, int g);
 // Frees the add-mode-5 device tables and rows (set up again on next use).
 void plan_pair_release(hdd_plan p);
 // Device bytes those tables and their rows take (builds the host copy).

@@ -253,8 +253,6 @@ hdd_error plan_sub_tables(hdd_plan p, int first, int count, SubDeviceTables *out
   return HDD_NO_ERROR;
 }
 
-namespace {
-
 // Host pair tables of the range and shape, built when they differ from the cached ones.
 hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt, int g) {
   if (p->pair_first == first && p->pair_count == count && p->pair_cc == cc && p->pair_ntt == ntt &&
@@ -275,6 +273,8 @@ hdd_error pair_host_tables(hdd_plan p, int first, int count, int cc, int ntt, in
   p->pair_on_device = false;
   return HDD_NO_ERROR;
 }
+
+namespace {
 
 template <class T>
 size_t vbytes(const std::vector<T> &v) {
@@ -510,6 +510,40 @@ hdd_error hdd_set_pair_rows(hdd_plan p, int channels) {
   if (channels != 0 && channels != 1 && channels != 2 && channels != 4) return HDD_UNKNOWN_ERROR;
   p->pair_rows = channels == 1 ? 2 : channels;
   if (!p->pair_rows) hg::plan_pair_release(p);
+  return HDD_NO_ERROR;
+}
+
+hdd_error hdd_get_pair_tables(hdd_plan p, hdd_size first, hdd_size count, int channels, int stage_groups,
+                              int time_tiles, hdd_pair_tables_view *out) {
+  if (!p) return HDD_INVALID_PLAN;
+  if (!out) return HDD_INVALID_POINTER;
+  if (p->dms.empty()) return HDD_NO_DM_LIST_SET;
+  if ((channels != 2 && channels != 4) || (stage_groups != 4 && stage_groups != 8) || time_tiles < 1 ||
+      count == 0 || first + count > p->dms.size() || p->chans.empty())
+    return HDD_UNKNOWN_ERROR;
+  const hdd_error e = hg::pair_host_tables(p, (int)first, (int)count, stage_groups, time_tiles, channels);
+  if (e != HDD_NO_ERROR) return e;
+  const hg::PairTables &t = p->pair;
+  out->channels = t.g;
+  out->stage_groups = t.cc;
+  out->time_tiles = t.ntt;
+  out->ntiles = t.ntiles;
+  out->ngroups = t.npair;
+  out->nrows = t.nrows;
+  out->rec_ints = hg::pair_rec_int4(t.cc) * 4;
+  out->nrec = (int)(t.rec.size() / hg::pair_rec_int4(t.cc));
+  out->max_stage_bytes = t.max_stage;
+  out->max_span = t.max_span;
+  out->npos = t.npos;
+  out->words = t.words;
+  out->rinfo = reinterpret_cast<const int *>(t.rinfo.data());
+  out->rinfo2 = reinterpret_cast<const int *>(t.rinfo2.data());
+  out->roff = t.roff.data();
+  out->rwords = t.rwords.data();
+  out->prow = t.prow.data();
+  out->prange = reinterpret_cast<const int *>(t.prange.data());
+  out->rec = reinterpret_cast<const int *>(t.rec.data());
+  out->tile_st = t.tile_st.data();
   return HDD_NO_ERROR;
 }
 

@@ -74,6 +74,16 @@ class RefineParams(C.Structure):
                 ("f0_mhz", C.c_double), ("df_mhz", C.c_double), ("device", C.c_int)]
 
 
+class PairTablesView(C.Structure):
+    """hdd_pair_tables_view: host group-row tables of a plan (tests)."""
+    _fields_ = [("channels", C.c_int), ("stage_groups", C.c_int), ("time_tiles", C.c_int), ("ntiles", C.c_int),
+                ("ngroups", C.c_int), ("nrows", C.c_int), ("nrec", C.c_int), ("rec_ints", C.c_int),
+                ("max_stage_bytes", C.c_int), ("max_span", C.c_int), ("npos", C.c_long), ("words", C.c_long),
+                ("rinfo", C.POINTER(C.c_int)), ("rinfo2", C.POINTER(C.c_int)), ("roff", C.POINTER(C.c_longlong)),
+                ("rwords", C.POINTER(C.c_int)), ("prow", C.POINTER(C.c_int)), ("prange", C.POINTER(C.c_int)),
+                ("rec", C.POINTER(C.c_int)), ("tile_st", C.POINTER(C.c_int))]
+
+
 class HellaTuning(C.Structure):
     _fields_ = [("dm_per_block", C.c_int), ("samples_per_thread", C.c_int), ("chan_chunk", C.c_int),
                 ("stages", C.c_int), ("group", C.c_int), ("add_mode", C.c_int)]
@@ -133,6 +143,8 @@ def lib() -> C.CDLL:
     _sig(L, "hdd_get_dm_list", C.POINTER(C.c_float), [_VP])
     _sig(L, "hdd_get_killmask", C.POINTER(C.c_int), [_VP])
     _sig(L, "hdd_get_delay_table", C.POINTER(C.c_int), [_VP])
+    _sig(L, "hdd_get_pair_tables", C.c_int, [_VP, C.c_size_t, C.c_size_t, C.c_int, C.c_int, C.c_int,
+                                             C.POINTER(PairTablesView)])
     for n in ("hdd_get_dt", "hdd_get_df", "hdd_get_f0"):
         _sig(L, n, C.c_float, [_VP])
     _sig(L, "hdd_execute", C.c_int, [_VP, _SZ, _VP, _SZ, _VP, _SZ, C.c_uint])
@@ -336,6 +348,19 @@ class Plan:
     def delay_table(self) -> np.ndarray:
         p = self.L.hdd_get_delay_table(self.h)
         return np.ctypeslib.as_array(p, shape=(self.dm_count, self.nchans)).copy()
+
+    def pair_tables(self, first: int, count: int, channels: int, stage_groups: int, time_tiles: int) -> dict:
+        """Copies of the group-row host tables (hdd_get_pair_tables)."""
+        v = PairTablesView()
+        _chk_hdd(self.L.hdd_get_pair_tables(self.h, first, count, channels, stage_groups, time_tiles, C.byref(v)))
+        a = lambda ptr, n: np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+        return dict(channels=v.channels, stage_groups=v.stage_groups, time_tiles=v.time_tiles, ntiles=v.ntiles,
+                    ngroups=v.ngroups, nrows=v.nrows, max_stage_bytes=v.max_stage_bytes, max_span=v.max_span,
+                    npos=v.npos, words=v.words, rinfo=a(v.rinfo, 4 * v.nrows).reshape(-1, 4),
+                    rinfo2=a(v.rinfo2, 4 * v.nrows).reshape(-1, 4), roff=a(v.roff, v.nrows),
+                    rwords=a(v.rwords, v.nrows), prow=a(v.prow, v.ngroups + 1),
+                    prange=a(v.prange, 6 * v.ngroups).reshape(-1, 3, 2),
+                    rec=a(v.rec, v.nrec * v.rec_ints).reshape(v.nrec, v.rec_ints), tile_st=a(v.tile_st, v.ntiles + 1))
 
     def execute_adv(self, nsamps, inp, in_stride, out, out_stride, flags=HDD_HOST_POINTERS, in_nbits=8,
                     out_nbits=32):

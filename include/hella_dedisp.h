@@ -106,6 +106,31 @@ hdd_error hdd_set_killmask(hdd_plan plan, const hdd_bool *killmask);
  * allocation returns HDD_MEM_ALLOC_FAILED.  hdd_execute_noalloc does not
  * use it. */
 hdd_error hdd_set_pair_rows(hdd_plan plan, int channels);
+/* hdd_get_pair_tables -- no counterpart in the reference; for tests.  Host
+ * copies of the group-row tables the plan builds for trials [first_dm_idx,
+ * first_dm_idx + dm_count), `channels` (2 or 4) a group, stage_groups (4
+ * or 8) groups a stage and time_tiles tiles of 1024 output samples, as the
+ * execute calls would use them.  The pointers stay valid until the plan's
+ * tables change.  Row r of group k holds, at window position p,
+ * x[c0][p] + sum_i x[c_i][p + r_i] in the low 16 bits of word p - first
+ * position and the same at p + 512 in the high bits; a stage record is
+ * {groups, rows, 0, 0}, then stage_groups x 16 trial byte offsets into the
+ * staged rows, then 32 x {first word low, high, words, byte slot}. */
+typedef struct {
+  int channels, stage_groups, time_tiles, ntiles, ngroups, nrows, nrec, rec_ints;
+  int max_stage_bytes, max_span;
+  long npos, words;
+  const int *rinfo;       /* [nrows][4] c0, c1 (-1: none), r1, first position */
+  const int *rinfo2;      /* [nrows][4] c2, c3 (-1: none), r2, r3 */
+  const long long *roff;  /* [nrows] first word of the row */
+  const int *rwords;      /* [nrows] words of the row */
+  const int *prow;        /* [ngroups + 1] first row of each group */
+  const int *prange;      /* [ngroups][3][2] smallest, largest r_i */
+  const int *rec;         /* [nrec][rec_ints] stage records */
+  const int *tile_st;     /* [ntiles + 1] first record of each 16-trial tile */
+} hdd_pair_tables_view;
+hdd_error hdd_get_pair_tables(hdd_plan plan, hdd_size first_dm_idx, hdd_size dm_count, int channels,
+                              int stage_groups, int time_tiles, hdd_pair_tables_view *out);
 
 hdd_size hdd_get_max_delay(const hdd_plan plan);
 hdd_size hdd_get_dm_delay(const hdd_plan plan, int dm_trial);

@@ -143,6 +143,7 @@ struct DedispArgs {
   const int4 *pair_rinfo2;
   const long long *pair_roff;
   const int *pair_rwords;
+  const int *pair_rtile;
   const int *pair_prow;
   const int2 *pair_prange;
   const int4 *pair_rec;
@@ -214,7 +215,9 @@ size_t dedisp_sub_smem(int max_spread, int max_words, int max_rec, int nbuf);
 // windows of the rows its groups use; its record is
 //   int4 {groups, rows, 0, 0}
 //   int  [cc][16] byte offset, in the staged rows, of each trial's window
-//   int4 [kPairRowsMax] {first word (low, high 32 bits), words, byte slot}
+//   int4 [kPairRowsMax] {first word of tile 0 (low, high 32 bits),
+//                        words | byte slot / 16 << 16, the row's words per time tile}
+// (a copy of time tile tt starts at first word + tt x words per time tile).
 constexpr int kPairDPT = 16;
 constexpr int kPairRowsMax = 32;  // rows per stage: one per lane of the staging warp
 constexpr int kPairGMax = 4;      // channels per group
@@ -230,10 +233,11 @@ struct PairTables {
   int max_span = 0;             // largest r_i range of one group and channel
   long npos = 0;                // window positions the rows cover
   long words = 0;               // words of all rows
-  std::vector<int4> rinfo;      // [nrows] {c0, c1 (-1: none), r1, first position}
+  std::vector<int4> rinfo;      // [nrows] {c0, c1 (-1: none), r1, position of word 0}
   std::vector<int4> rinfo2;     // [nrows] {c2, c3 (-1: none), r2, r3}
   std::vector<long long> roff;  // [nrows] first word of the row
   std::vector<int> rwords;      // [nrows] words of the row
+  std::vector<int> rtile;       // [nrows] words per time tile: 1024 (one run) or its tiles' window
   std::vector<int> prow;        // [npair + 1] first row of each group
   std::vector<int2> prange;     // [npair][kPairGMax - 1] {smallest, largest r_i}, i = 1..
   std::vector<int> row_of;      // [dm_count][npair] row of each trial and group

@@ -45,6 +45,7 @@ struct PairDeviceTables {
   const int4 *rinfo2;
   const long long *roff;
   const int *rwords;
+  const int *rtile;
   const int *prow;
   const int2 *prange;
   const int4 *rec;

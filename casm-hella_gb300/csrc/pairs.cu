@@ -50,6 +50,13 @@ constexpr int kMaxBuf = 4;
 
 __host__ __device__ constexpr int stage_hdr_bytes(int cc) { return 16 + cc * kPairDPT * 4; }
 
+// Window positions a row spans from its first position: all its words for
+// a single run, (ntt - 1) tiles of 1024 and one stride for tiled rows.
+__device__ __forceinline__ long row_positions(const DedispArgs &a, int r) {
+  const int stride = a.pair_rtile[r];
+  return stride == kTileSamples ? (long)a.pair_rwords[r] : (long)(a.ntt - 1) * kTileSamples + stride;
+}
+
 template <int G>
 __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
@@ -62,7 +69,7 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   int any = 0;  // does a row of the group cover a position of this chunk?
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int w = a.pair_rinfo[r].w;
-    any |= P0 < (long)w + a.pair_rwords[r] && P0 + kBuildCH > (long)w;
+    any |= P0 < (long)w + row_positions(a, r) && P0 + kBuildCH > (long)w;
   }
   if (!__syncthreads_or(any)) return;
   const int4 i0 = a.pair_rinfo[r0], j0 = a.pair_rinfo2[r0];
@@ -93,22 +100,36 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   const int lane = threadIdx.x & 31;
   for (int r = r0 + (threadIdx.x >> 5); r < r1; r += blockDim.x >> 5) {
     const int4 in = a.pair_rinfo[r];
-    const long lo = max(P0, (long)in.w), hi = min(P0 + kBuildCH, (long)in.w + a.pair_rwords[r]);
-    if (lo >= hi) continue;
+    if (P0 >= (long)in.w + row_positions(a, r) || P0 + kBuildCH <= (long)in.w) continue;
     const int4 in2 = G == 4 ? a.pair_rinfo2[r] : make_int4(-1, -1, 0, 0);
     uint32_t *dst = a.pair_rows + (size_t)z * a.pair_rows_stride + a.pair_roff[r];
     // word q of the chunk, q = p - P0, of channel i for this row's r_i
     const int s1 = off[1] + in.z - rmin[1], s2 = off[2] + in2.z - rmin[2], s3 = off[3] + in2.w - rmin[3];
-    const int first = (int)(lo - P0), last = (int)(hi - P0), d0 = (int)(P0 - in.w);
-    // rows are read back by other blocks much later: streaming stores
-    if (G == 4 && ch[3] >= 0) {
-      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q] + sm[s3 + q]);
-    } else if (G == 4 && ch[2] >= 0) {
-      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q] + sm[s2 + q]);
-    } else if (ch[1] >= 0) {
-      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q] + sm[s1 + q]);
-    } else {
-      for (int q = first + lane; q < last; q += 32) __stcs(dst + d0 + q, sm[q]);
+    // the row's tiles: tile tt holds positions [first + 1024 tt, + stride) at words tt * stride on
+    // (one run from word 0 when stride = 1024)
+    const int stride = a.pair_rtile[r];
+    const long rel0 = P0 - in.w;  // chunk start relative to the row's first position
+    const int tt0 = (int)max(0L, rel0 / kTileSamples - 1);
+    const int tt1 = (int)min((long)a.ntt - 1, (rel0 + kBuildCH) / kTileSamples);
+    for (int tt = stride == kTileSamples ? 0 : tt0; tt <= (stride == kTileSamples ? 0 : tt1); ++tt) {
+      // positions of this tile's words (the whole row for stride 1024), clipped to the chunk
+      const long pb = (long)in.w + (long)tt * kTileSamples;
+      const long pe = stride == kTileSamples ? (long)in.w + a.pair_rwords[r] : pb + stride;
+      const long lo = max(P0, pb), hi = min(P0 + kBuildCH, pe);
+      if (lo >= hi) continue;
+      const int first = (int)(lo - P0), last = (int)(hi - P0);
+      const long d0l = (long)tt * stride + (P0 - pb);  // word of chunk offset q is d0 + q
+      uint32_t *dt = dst + d0l;
+      // rows are read back by other blocks much later: streaming stores
+      if (G == 4 && ch[3] >= 0) {
+        for (int q = first + lane; q < last; q += 32) __stcs(dt + q, sm[q] + sm[s1 + q] + sm[s2 + q] + sm[s3 + q]);
+      } else if (G == 4 && ch[2] >= 0) {
+        for (int q = first + lane; q < last; q += 32) __stcs(dt + q, sm[q] + sm[s1 + q] + sm[s2 + q]);
+      } else if (ch[1] >= 0) {
+        for (int q = first + lane; q < last; q += 32) __stcs(dt + q, sm[q] + sm[s1 + q]);
+      } else {
+        for (int q = first + lane; q < last; q += 32) __stcs(dt + q, sm[q]);
+      }
     }
   }
 }
@@ -209,17 +230,18 @@ __global__ void __launch_bounds__(kDedispThreads, 2) k_pair_sum(DedispArgs a, in
       }
     }
     const int4 *r = a.pair_rec + (size_t)(cur->s0 + cur->st) * REC;
-    const int t0 = cur->t0;
+    const int tt = cur->t0 / kTileSamples;
     const int nrows = __ldg(&r->y);
     const uint32_t bar = full_of(b);
     fence_proxy_async();
     if (lane < nrows) {
-      const int4 rw = __ldg(r + 1 + CC * DPT / 4 + lane);  // {first word lo, hi, words, byte slot}
+      // {first word (low, high), words | byte slot / 16 << 16, the row's words per time tile}
+      const int4 rw = __ldg(r + 1 + CC * DPT / 4 + lane);
       const long start = (long)(((unsigned long long)(unsigned)rw.y << 32) | (unsigned)rw.x);
-      const uint32_t nb = (uint32_t)rw.z * 4u;
+      const uint32_t nb = ((uint32_t)rw.z & 0xffffu) * 4u, slot = ((uint32_t)rw.z >> 16) * 16u;
       mbar_arrive_tx(bar, nb + (lane == 0 ? (uint32_t)HB : 0u));
       const uint32_t *rows = MULTI ? a.pair_rows + (size_t)cur->z * a.pair_rows_stride : a.pair_rows;
-      bulk_g2s(buf_of(b) + HB + (uint32_t)rw.w, rows + start + t0, nb, bar);
+      bulk_g2s(buf_of(b) + HB + slot, rows + start + (long)tt * rw.w, nb, bar);
       if (lane == 0) bulk_g2s(buf_of(b), r, HB, bar);
     } else {
       mbar_arrive(bar);
@@ -417,7 +439,9 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
     t.prow[k + 1] = (int)t.rinfo.size();
   }
   t.nrows = (int)t.rinfo.size();
-  std::vector<long long> need(t.nrows, 0);
+  // per row, the union of its copies' windows within a time tile: [lo, hi) words from its first position
+  std::vector<long long> lo(t.nrows, 1LL << 60), hi(t.nrows, 0);
+  int max_nw = 0;
   // stage records
   const int REC = pair_rec_int4(cc);
   const int offs0 = 4, rows0 = 4 + cc * kPairDPT;  // int positions in a record
@@ -476,10 +500,11 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
         for (int m = 0; m < nt; ++m)
           if (ids[m] == uid[j]) rec[offs0 + ng * kPairDPT + m] = slot + (av[m] - bal[j]) * 4;
         int *rw = &rec[rows0 + 4 * nr];
-        rw[2] = nw[j];
-        rw[3] = slot;
+        rw[2] = (nw[j] & 0xffff) | (slot / 16) << 16;  // words (< 2^16) | byte slot / 16
+        max_nw = std::max(max_nw, nw[j]);
         pending.push_back(Fix{(size_t)(rows0 + 4 * nr), uid[j], bal[j]});
-        need[uid[j]] = std::max(need[uid[j]], (long long)bal[j] + nw[j]);
+        lo[uid[j]] = std::min(lo[uid[j]], (long long)bal[j]);
+        hi[uid[j]] = std::max(hi[uid[j]], (long long)bal[j] + nw[j]);
         ++nr;
         bytes += nw[j] * 4;
       }
@@ -488,23 +513,36 @@ PairTables dedisp_pair_tables(const int *delays, int nchan, const int *chans, in
     if (ng > 0) flush();
     t.tile_st.push_back((int)(t.rec.size() / REC));
   }
-  // row lengths and offsets (multiples of 4 words: every copy starts 16-byte aligned)
+  // Row layout.  A row keeps, for each time tile tt, the words its copies read: [tt * 1024 + lo,
+  // tt * 1024 + hi) of its positions.  When hi - lo < 1024 the tiles' windows do not meet and are
+  // stored one after another (tile stride hi - lo words); else the row is one run from lo (stride
+  // 1024: the tiles' windows overlap).  Word i then holds position
+  //   first + (i / stride) * 1024 + i % stride,   first = (smallest delay of its trials) + lo,
+  // and a copy of tile tt starts at word tt * stride + (bal - lo).  Offsets and lengths stay
+  // multiples of 4 words, so every copy starts 16-byte aligned.
   t.roff.resize(t.nrows);
   t.rwords.resize(t.nrows);
+  t.rtile.resize(t.nrows);
   long long off = 0;
   for (int r = 0; r < t.nrows; ++r) {
-    const long long w = ((long long)(ntt - 1) * kTileSamples + need[r] + 3) / 4 * 4;
+    const long long span = hi[r] - lo[r];  // multiple of 4: lo and hi are
+    const int stride = span < kTileSamples ? (int)span : kTileSamples;
+    const long long w = (long long)(ntt - 1) * stride + span;
+    t.rinfo[r].w += (int)lo[r];
     t.roff[r] = off;
     t.rwords[r] = (int)w;
+    t.rtile[r] = stride;
     off += w;
-    t.npos = std::max(t.npos, (long)(t.rinfo[r].w + w));
+    t.npos = std::max(t.npos, (long)t.rinfo[r].w + (long)(ntt - 1) * kTileSamples + (long)span);
   }
   t.words = (long)off;
+  if (max_nw > 0xffff) t.max_stage = 1 << 30;  // a copy longer than its 16-bit field: no launch takes these
   int *ri = reinterpret_cast<int *>(t.rec.data());
   for (const Fix &f : fixes) {
-    const unsigned long long start = (unsigned long long)(t.roff[f.row] + f.bal);
+    const unsigned long long start = (unsigned long long)(t.roff[f.row] + f.bal - lo[f.row]);
     ri[f.rec_int] = (int)(unsigned)(start & 0xffffffffull);
     ri[f.rec_int + 1] = (int)(unsigned)(start >> 32);
+    ri[f.rec_int + 3] = t.rtile[f.row];
   }
   return t;
 }
@@ -522,7 +560,8 @@ cudaError_t dedisperse_pairs(const DedispArgs &a, cudaStream_t s) {
   if ((a.beams && (a.nbeam < 1 || a.nbeam > kPairMaxBeams || (a.nbeam > 1 && a.pair_rows_stride <= 0))) ||
       a.dpt != kPairDPT || (a.mode != 5 && a.mode != 6) || (g != 2 && g != 4) ||
       !a.pair_rows || !a.pair_rec || !a.pair_tile_st || !a.pair_rinfo || !a.pair_rinfo2 || !a.pair_roff ||
-      !a.pair_rwords || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 || a.pair_npair > 65535 ||
+      !a.pair_rwords || !a.pair_rtile || !a.pair_prow || !a.pair_prange || a.pair_npair <= 0 ||
+      a.pair_npair > 65535 ||
       a.pair_stage <= 0 || a.pair_stage % 16 != 0 || a.pair_span < 0 || a.pair_lanecap < 1 ||
       a.pair_lanecap > pair_lanecap(g))
     return cudaErrorInvalidValue;

@@ -108,10 +108,10 @@ struct hdd_plan_struct {
   bool pair_on_device = false;
   int4 *d_prinfo = nullptr, *d_prinfo2 = nullptr, *d_prec = nullptr;
   long long *d_proff = nullptr;
-  int *d_prwords = nullptr, *d_pprow = nullptr, *d_ptile = nullptr;
+  int *d_prwords = nullptr, *d_prtile = nullptr, *d_pprow = nullptr, *d_ptile = nullptr;
   int2 *d_pprange = nullptr;
   uint32_t *d_prows = nullptr;
-  size_t prinfo_cap = 0, prinfo2_cap = 0, prec_cap = 0, proff_cap = 0, prwords_cap = 0, pprow_cap = 0, ptile_cap = 0,
+  size_t prinfo_cap = 0, prinfo2_cap = 0, prtile_cap = 0, prec_cap = 0, proff_cap = 0, prwords_cap = 0, pprow_cap = 0, ptile_cap = 0,
          pprange_cap = 0, prows_cap = 0;
 };
 
@@ -287,7 +287,7 @@ hdd_error plan_pair_bytes(hdd_plan p, int first, int count, int cc, int ntt, int
   const hdd_error e = pair_host_tables(p, first, count, cc, ntt, g);
   if (e != HDD_NO_ERROR) return e;
   const PairTables &t = p->pair;
-  *bytes = vbytes(t.rinfo) + vbytes(t.rinfo2) + vbytes(t.roff) + vbytes(t.rwords) + vbytes(t.prow) + vbytes(t.prange) +
+  *bytes = vbytes(t.rinfo) + vbytes(t.rinfo2) + vbytes(t.roff) + vbytes(t.rwords) + vbytes(t.rtile) + vbytes(t.prow) + vbytes(t.prange) +
            vbytes(t.rec) + vbytes(t.tile_st) + std::max<size_t>((size_t)t.words, 4) * 4;
   return HDD_NO_ERROR;
 }
@@ -312,6 +312,8 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, in
             HDD_NO_ERROR ||
         (e = up((void **)&p->d_prwords, &p->prwords_cap, t.rwords.data(), t.rwords.size() * sizeof(int))) !=
             HDD_NO_ERROR ||
+        (e = up((void **)&p->d_prtile, &p->prtile_cap, t.rtile.data(), t.rtile.size() * sizeof(int))) !=
+            HDD_NO_ERROR ||
         (e = up((void **)&p->d_pprow, &p->pprow_cap, t.prow.data(), t.prow.size() * sizeof(int))) != HDD_NO_ERROR ||
         (e = up((void **)&p->d_pprange, &p->pprange_cap, t.prange.data(), t.prange.size() * sizeof(int2))) !=
             HDD_NO_ERROR ||
@@ -328,6 +330,7 @@ hdd_error plan_pair_tables(hdd_plan p, int first, int count, int cc, int ntt, in
   out->rinfo2 = p->d_prinfo2;
   out->roff = p->d_proff;
   out->rwords = p->d_prwords;
+  out->rtile = p->d_prtile;
   out->prow = p->d_pprow;
   out->prange = p->d_pprange;
   out->rec = p->d_prec;
@@ -348,11 +351,11 @@ void plan_pair_release(hdd_plan p) {
   if (!p || !(p->d_prinfo || p->d_prows)) return;
   cudaSetDevice(p->device);
   void **bufs[] = {(void **)&p->d_prinfo, (void **)&p->d_prinfo2, (void **)&p->d_proff, (void **)&p->d_prwords,
-                   (void **)&p->d_pprow, (void **)&p->d_pprange, (void **)&p->d_prec, (void **)&p->d_ptile,
-                   (void **)&p->d_prows};
-  size_t *caps[] = {&p->prinfo_cap, &p->prinfo2_cap, &p->proff_cap, &p->prwords_cap, &p->pprow_cap,
-                    &p->pprange_cap, &p->prec_cap, &p->ptile_cap, &p->prows_cap};
-  for (int i = 0; i < 9; ++i) {
+                   (void **)&p->d_prtile, (void **)&p->d_pprow, (void **)&p->d_pprange, (void **)&p->d_prec,
+                   (void **)&p->d_ptile, (void **)&p->d_prows};
+  size_t *caps[] = {&p->prinfo_cap, &p->prinfo2_cap, &p->proff_cap, &p->prwords_cap, &p->prtile_cap,
+                    &p->pprow_cap, &p->pprange_cap, &p->prec_cap, &p->ptile_cap, &p->prows_cap};
+  for (int i = 0; i < 10; ++i) {
     cudaFree(*bufs[i]);
     *bufs[i] = nullptr;
     *caps[i] = 0;
@@ -377,6 +380,7 @@ void use_pair_tables(DedispArgs *a, const PairDeviceTables &t) {
   a->pair_rinfo2 = t.rinfo2;
   a->pair_roff = t.roff;
   a->pair_rwords = t.rwords;
+  a->pair_rtile = t.rtile;
   a->pair_prow = t.prow;
   a->pair_prange = t.prange;
   a->pair_rec = t.rec;
@@ -485,6 +489,7 @@ void hdd_destroy_plan(hdd_plan p) {
   cudaFree(p->d_prinfo2);
   cudaFree(p->d_proff);
   cudaFree(p->d_prwords);
+  cudaFree(p->d_prtile);
   cudaFree(p->d_pprow);
   cudaFree(p->d_pprange);
   cudaFree(p->d_prec);
@@ -540,6 +545,7 @@ hdd_error hdd_get_pair_tables(hdd_plan p, hdd_size first, hdd_size count, int ch
   out->rinfo2 = reinterpret_cast<const int *>(t.rinfo2.data());
   out->roff = t.roff.data();
   out->rwords = t.rwords.data();
+  out->rtile = t.rtile.data();
   out->prow = t.prow.data();
   out->prange = reinterpret_cast<const int *>(t.prange.data());
   out->rec = reinterpret_cast<const int *>(t.rec.data());

@@ -80,7 +80,8 @@ class PairTablesView(C.Structure):
                 ("ngroups", C.c_int), ("nrows", C.c_int), ("nrec", C.c_int), ("rec_ints", C.c_int),
                 ("max_stage_bytes", C.c_int), ("max_span", C.c_int), ("npos", C.c_long), ("words", C.c_long),
                 ("rinfo", C.POINTER(C.c_int)), ("rinfo2", C.POINTER(C.c_int)), ("roff", C.POINTER(C.c_longlong)),
-                ("rwords", C.POINTER(C.c_int)), ("prow", C.POINTER(C.c_int)), ("prange", C.POINTER(C.c_int)),
+                ("rwords", C.POINTER(C.c_int)), ("rtile", C.POINTER(C.c_int)), ("prow", C.POINTER(C.c_int)),
+                ("prange", C.POINTER(C.c_int)),
                 ("rec", C.POINTER(C.c_int)), ("tile_st", C.POINTER(C.c_int))]
 
 
@@ -358,7 +359,7 @@ class Plan:
                     ngroups=v.ngroups, nrows=v.nrows, max_stage_bytes=v.max_stage_bytes, max_span=v.max_span,
                     npos=v.npos, words=v.words, rinfo=a(v.rinfo, 4 * v.nrows).reshape(-1, 4),
                     rinfo2=a(v.rinfo2, 4 * v.nrows).reshape(-1, 4), roff=a(v.roff, v.nrows),
-                    rwords=a(v.rwords, v.nrows), prow=a(v.prow, v.ngroups + 1),
+                    rwords=a(v.rwords, v.nrows), rtile=a(v.rtile, v.nrows), prow=a(v.prow, v.ngroups + 1),
                     prange=a(v.prange, 6 * v.ngroups).reshape(-1, 3, 2),
                     rec=a(v.rec, v.nrec * v.rec_ints).reshape(v.nrec, v.rec_ints), tile_st=a(v.tile_st, v.ntiles + 1))
 

@@ -111,19 +111,22 @@ hdd_error hdd_set_pair_rows(hdd_plan plan, int channels);
  * first_dm_idx + dm_count), `channels` (2 or 4) a group, stage_groups (4
  * or 8) groups a stage and time_tiles tiles of 1024 output samples, as the
  * execute calls would use them.  The pointers stay valid until the plan's
- * tables change.  Row r of group k holds, at window position p,
- * x[c0][p] + sum_i x[c_i][p + r_i] in the low 16 bits of word p - first
- * position and the same at p + 512 in the high bits; a stage record is
+ * tables change.  Word i of row r (group k) holds, for the window position
+ * p = first + (i / stride) * 1024 + i % stride (first = rinfo[r][3],
+ * stride = rtile[r]), x[c0][p] + sum_i x[c_i][p + r_i] in its low 16 bits
+ * and the same at p + 512 in the high bits; a stage record is
  * {groups, rows, 0, 0}, then stage_groups x 16 trial byte offsets into the
- * staged rows, then 32 x {first word low, high, words, byte slot}. */
+ * staged rows, then 32 x {first word of time tile 0 (low, high 32 bits),
+ * words | byte slot / 16 << 16, the row's words per time tile}. */
 typedef struct {
   int channels, stage_groups, time_tiles, ntiles, ngroups, nrows, nrec, rec_ints;
   int max_stage_bytes, max_span;
   long npos, words;
-  const int *rinfo;       /* [nrows][4] c0, c1 (-1: none), r1, first position */
+  const int *rinfo;       /* [nrows][4] c0, c1 (-1: none), r1, position of word 0 */
   const int *rinfo2;      /* [nrows][4] c2, c3 (-1: none), r2, r3 */
   const long long *roff;  /* [nrows] first word of the row */
   const int *rwords;      /* [nrows] words of the row */
+  const int *rtile;       /* [nrows] words per time tile (1024: one run) */
   const int *prow;        /* [ngroups + 1] first row of each group */
   const int *prange;      /* [ngroups][3][2] smallest, largest r_i */
   const int *rec;         /* [nrec][rec_ints] stage records */

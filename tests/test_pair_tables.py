@@ -23,9 +23,11 @@ def emulate(T, x_ring, win0, nout, ndm):
     assert np.all(roff % 4 == 0) and np.all(rw % 4 == 0) and roff[-1] + rw[-1] == T["words"]
     for k in range(T["ngroups"]):
         for r in range(T["prow"][k], T["prow"][k + 1]):
-            c0, c1, r1, dmin = T["rinfo"][r]
+            c0, c1, r1, first = T["rinfo"][r]
             c2, c3, r2, r3 = T["rinfo2"][r]
-            p = dmin + np.arange(rw[r])
+            stride = T["rtile"][r]
+            i = np.arange(rw[r])
+            p = first + (i // stride) * 1024 + i % stride  # position of word i
             lo = x_ring[c0, (win0 + p) % R].copy()
             hi = x_ring[c0, (win0 + p + 512) % R].copy()
             for i, (c, rel) in enumerate(((c1, r1), (c2, r2), (c3, r3))):
@@ -50,12 +52,15 @@ def emulate(T, x_ring, win0, nout, ndm):
                 assert 1 <= ng <= cc and 1 <= nr <= RMAX
                 buf = []
                 for j in range(nr):
-                    lo, hi, nw, slot = r[rows0 + 4 * j: rows0 + 4 * j + 4]
+                    lo, hi, packed, stride = r[rows0 + 4 * j: rows0 + 4 * j + 4]
                     start = (lo & 0xffffffff) | (hi << 32)
+                    nw, slot = packed & 0xffff, (packed >> 16) * 16
                     u = np.searchsorted(roff, start, side="right") - 1
+                    assert stride == T["rtile"][u] and (stride == 1024 or nw <= stride)
                     assert start % 4 == 0 and nw % 4 == 0 and slot == 4 * sum(len(b) for b in buf)
-                    assert start + (ntt - 1) * 1024 + nw <= roff[u] + rw[u]  # inside the row, last tile too
-                    buf.append(rows[start + t0: start + t0 + nw])
+                    assert start + (ntt - 1) * stride + nw <= roff[u] + rw[u]  # inside the row, last tile too
+                    assert start - roff[u] + nw <= stride or stride == 1024   # inside its tile's window
+                    buf.append(rows[start + tt * stride: start + tt * stride + nw])
                 buf = np.concatenate(buf)
                 assert buf.size * 4 <= T["max_stage_bytes"] or ng == 1
                 for i in range(ng):
@@ -115,6 +120,28 @@ def test_pair_tables_sum_like_the_oracle(hella, oracle, channels, stage_groups, 
     window = x[:, (win0 + np.arange(nout + md)) % R].T.astype(np.uint8)  # [nsamps][nchan]
     want = oracle.dedisperse(window, delays, killmask=km, nout=nout)
     assert np.array_equal(got, want.astype(np.int64))
+    plan.close()
+
+
+def test_pair_tables_long_rows(hella, oracle):
+    """512 channels, DM 0-300: adjacent channels keep one relative delay
+    over hundreds of trials, so some pair rows are read over more than a
+    tile's width and are kept as one run (words per tile 1024), the rest in
+    per-tile windows; both kinds in one set of tables."""
+    nch = 512
+    plan = hella.Plan(nch, 1e-3, 468.75, -(468.75 - 375.0) / nch)
+    plan.generate_dm_list(0.0, 300.0, 40.0, 1.25)
+    nout, ndm = 1600, plan.dm_count
+    T = plan.pair_tables(0, ndm, 2, 8, 2)
+    assert (T["rtile"] == 1024).sum() > 100 and (T["rtile"] < 1024).sum() > 100
+    rng = np.random.default_rng(7)
+    md = int(plan.max_delay)
+    R = (nout + md + 700) // 4 * 4
+    x = rng.integers(0, 256, (nch, R))
+    win0 = int(rng.integers(0, R))
+    got = emulate(T, x, win0, nout, ndm)
+    window = x[:, (win0 + np.arange(nout + md)) % R].T.astype(np.uint8)
+    assert np.array_equal(got, oracle.dedisperse(window, plan.delay_table(), nout=nout).astype(np.int64))
     plan.close()
 
 

@@ -50,8 +50,9 @@ DEDISP_TRAFFIC = {
     # rows of channel quads (add mode 6), 8 quads a stage, groups of 8: k_pair_build<4> 0.760 read +
     # 18.95 written, k_pair_sum 22.20 read + 0.657 written
     (16, 4, 16, 0, 8, 6): 42.57e9,
-    # the same in groups of 4 (the bench's shape): 0.737 + 18.94, 26.32 + 0.657
-    (16, 4, 16, 0, 4, 6): 46.65e9,
+    # the same in groups of 4 (the bench's shape), rows kept as per-tile windows where those are
+    # shorter than a tile, three staging buffers: 0.718 read + 14.88 written, 23.70 + 0.652
+    (16, 4, 16, 0, 4, 6): 39.95e9,
 }
 
 
@@ -284,8 +285,8 @@ def main():
         gi += 1
     torch.cuda.synchronize()
     # dedispersion: rows of channel quads (add mode 6: 16-trial tiles, 8 quads a stage, the deepest
-    # staging that fits, DM tiles walked in groups of 4 per time tile), 10.2 ms on the full beam
-    # (the autotuner's pick is within 0.1 %); pairs (add mode 5) 12.4 ms; the channel-by-channel
+    # staging that fits, DM tiles walked in groups of 4 per time tile), 9.8 ms on the full beam
+    # (the autotuner's pick is within 1 %); pairs (add mode 5) 12.4 ms; the channel-by-channel
     # kernel's best shape (add mode 2, multiply-add odd lanes and addresses) 19.4 ms.  Shapes a DM
     # list or the memory cannot take fall back in that order, then to add mode 0.
     shapes = [hg.HellaTuning(16, 4, 16, 0, 4 if m == 6 else 8, m) for m in (6, 5) if m <= a.add_mode and a.add_mode >= 5]

@@ -45,7 +45,7 @@ constexpr int kTileSamples = 4 * S;
 // four channel windows would otherwise leave three blocks per SM)
 __host__ __device__ constexpr int build_chunk(int g) { return g <= 2 ? 4096 : 2048; }
 constexpr int kBarHdr = 448;              // full[4] | empty[4] | per-warp staging cursors
-constexpr size_t kSmemBudget = 110 * 1024;  // two resident blocks per SM
+constexpr size_t kSmemBudget = 113 * 1024;  // two resident blocks per SM (228 KB less 1 KB a block)
 constexpr int kMaxBuf = 4;
 
 __host__ __device__ constexpr int stage_hdr_bytes(int cc) { return 16 + cc * kPairDPT * 4; }

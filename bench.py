@@ -642,6 +642,23 @@ def main_stream(a, rank, world, local, dist):
     per_width = fit(slots, 2) - fit(slots, 1)
     nbox = len([w for w in range(16) if params["width_min"] << w < params["width_max"]])
     wpp = int(min(nbox, (budget - (fit(slots, 1) - per_width)) // per_width))
+    # dedispersion through rows of channel pairs (add mode 5: on these 8192-sample gulps pairs and
+    # quads both take 33.6 ms for all 64 slots against 41.3 ms channel by channel, and pair rows
+    # are the smaller) when their rows -- up to four slots' worth -- and tables fit in the same
+    # budget beside the slots, paid for with smoothing widths per pass (each extra pass re-reads
+    # the dedispersed planes); sized from the plan's own tables
+    ntt = -(-(G + params["width_max"]) // 1024)
+    pl = hg.Plan(nch, params["plan_dt"], params["f0_mhz"], params["df_mhz"])
+    pl.generate_dm_list(params["dm_min"], params["dm_max"], params["ti_us"], params["dm_tol"])
+    tab = pl.pair_tables(0, pl.dm_count, 2, 8, ntt)
+    pl.close()
+    rows_bytes = (4 * tab["words"] * 4 + tab["rec"].nbytes + 64 * tab["nrows"] + slots * nch * 2
+                  + (16 << 20))
+    wpp_rows = int(min(nbox, (budget - rows_bytes - (fit(slots, 1) - per_width)) // per_width))
+    use_rows = wpp_rows >= 1
+    if use_rows:
+        wpp = wpp_rows
+    shape = hg.HellaTuning(16, 4, 16, 0, 4, 5) if use_rows else hg.HellaTuning(0, 4, 8, 0, 8, 2)
     rng = np.random.default_rng(7 + rank)
     # requests: 48 beams from the start, 16 more at 25% of the run; 12 leave at 50%
     join_at = {b: 0 if b < 48 else ngulps // 4 for b in range(NB)}
@@ -667,6 +684,7 @@ def main_stream(a, rank, world, local, dist):
         flight, else gulp g arrives at g * period_s and is polled at once."""
         bt = hg.Batch(hg.default_params(**dict(params, nbeam=slots, device=local, hbm_budget=budget)),
                       member=np.zeros(slots, np.int32), widths_per_pass=wpp, **kw)
+        bt.set_tuning(shape)
         slot_of, free, waiting = {}, list(range(slots)), []
         st = dict(admitted=0, waited=0, searched=0, lat=[], dev=[], ncand=[], arrival=[])
         pending = []
@@ -736,7 +754,9 @@ def main_stream(a, rank, world, local, dist):
         "data": "synthetic (seeded noise, drifting RFI, bursts 1 per beam per 30 s; drawn on the GPU)",
         "config": {"workload": STREAM_WORKLOAD.format(sec=a.seconds), "beam_requests": NB,
                    "slots_in_budget": slots, "hbm_budget_gb": round(budget / 1e9, 2),
-                   "widths_per_pass": wpp, "admitted": fast["admitted"], "waited_for_a_slot": fast["waited"],
+                   "widths_per_pass": wpp, "tuning": shape.as_dict(),
+                   "rows_gb": round(rows_bytes / 1e9, 2) if use_rows else 0.0,
+                   "admitted": fast["admitted"], "waited_for_a_slot": fast["waited"],
                    "gulps": ngulps, "searched_beam_gulps": beam_gulps,
                    "cadence": (f"value and e2e.value: gulps back to back, two in flight; e2e latencies: gulps "
                                f"released every {period * 1e3:.0f} ms (the 8.6 s real-time period compressed), "

@@ -371,6 +371,154 @@ __global__ void __launch_bounds__(kTF, R == 32 ? 3 : 5) k_firR(SmoothArgs a) {
   }
 }
 
+// k_firS: the arithmetic of k_firR for launches whose widths are all at
+// most 32 (wmin 1, wmax <= 64: spans of at most 64 samples), the widths of
+// the plain, batched and streaming configurations, whose few taps per width
+// left k_firR's per-width window set-up, stores, transposes and barriers as
+// large as the multiply-adds.  256 threads, 8 outputs each (the same
+// 2048-output chunks); thread t keeps the 72 y values its outputs read in
+// registers, so every tap is eight multiply-adds on registers; each width's
+// outputs get their own slot of a shared buffer, so one barrier pair per
+// chunk serves the row-mean partials of every width.  Per output: the same
+// multiply-add chain over the taps in order from zero, the same y values
+// and the same partial order as k_firR.
+constexpr int kSO = 8;                  // outputs per thread
+constexpr int kST = 256;                // threads per block
+constexpr int kSC = kSO * kST;          // outputs per chunk (k_firR's)
+constexpr int kSSpan = 64;              // largest span served
+constexpr int kSW = 6;                  // widths 1, 2, 4, 8, 16, 32
+constexpr int kSWin = kSO + kSSpan;     // y values a thread reads (72)
+constexpr int kSY = kSC + kSSpan + kSO; // y values staged per chunk (2120)
+constexpr int kSTap = 68;               // taps kept per width (65 used at most, float4 loads)
+static_assert(kSWin % 4 == 0 && kSY % 4 == 0 && kSTap % 4 == 0, "float4 staging");
+
+// One width (2 SM + 1 taps) of a thread's 8 outputs from its register window.
+template <int SM, int ANCHOR>
+__device__ __forceinline__ void firS_width(const float (&win)[kSWin], const float *tp, float (&acc)[kSO]) {
+  constexpr int NT = 2 * SM + 1, OFF = ANCHOR ? kSSpan - 2 * SM : 0;
+#pragma unroll
+  for (int i = 0; i < kSO; ++i) acc[i] = 0.f;
+#pragma unroll
+  for (int n4 = 0; n4 < NT; n4 += 4) {
+    const float4 c4 = *reinterpret_cast<const float4 *>(tp + n4);
+    const float cf[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int n = n4 + jj;
+      if (n < NT) {
+#pragma unroll
+        for (int i = 0; i < kSO; ++i) acc[i] = __fmaf_rn(cf[jj], win[OFF + i + n], acc[i]);
+      }
+    }
+  }
+}
+
+template <int ANCHOR>
+__global__ void __launch_bounds__(kST, 2) k_firS(SmoothArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  float *Ys = sm;                     // [kSY]
+  float *out_s = Ys + kSY;            // [kSW][kSC]
+  float *part_s = out_s + kSW * kSC;  // [kSW][256]
+  float *taps = part_s + kSW * 256;   // [kSW][kSTap]
+  int r;
+  const SmoothBeam &B = row_beam(a, blockIdx.x, &r);
+  if (!*B.active) return;
+  const int h = B.h, tid = threadIdx.x, bw0 = a.w0, bw1 = a.w0 + a.nw;
+  for (int i = tid; i < kSW * kSTap; i += kST) {
+    const int b = i / kSTap, n = i - b * kSTap;
+    taps[i] = b < a.nbox && n < a.tap_n[b] ? a.taps[a.tap_off[b] + n] : 0.f;
+  }
+  for (int i = tid; i < kSW * 256; i += kST) part_s[i] = 0.f;
+  float mx[kSW];
+#pragma unroll
+  for (int b = 0; b < kSW; ++b) mx[b] = -INFINITY;
+  const float *ra = B.dd + (size_t)r * B.dd_stride;
+  const float *rb = ra + B.dd_stride;
+  const float *rc = rb + B.dd_stride;
+  const int nwcol = 256 * (a.ntime_out / 256);
+  const int org = a.wmax / 2 - (ANCHOR ? kSSpan : 0);
+  constexpr int NL = (kSY + kST - 1) / kST;  // staged values per thread
+  for (int cs = 0; cs < a.ntime_out; cs += kSC) {
+    __syncthreads();  // the previous chunk's shared reads are done
+    {
+      float va[NL], vb[NL], vc[NL];
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int sx = tid + u * kST;
+        int col = cs + org + sx;
+        col = col < 0 ? 0 : (col >= a.ntime_dd ? a.ntime_dd - 1 : col);
+        if (sx < kSY) {
+          va[u] = ra[col];
+          vb[u] = rb[col];
+          vc[u] = rc[col];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int sx = tid + u * kST;
+        if (sx < kSY) Ys[sx] = __fmaf_rn(0.3f, __fadd_rn(va[u], vc[u]), vb[u]);
+      }
+    }
+    __syncthreads();
+    float win[kSWin];
+#pragma unroll
+    for (int q = 0; q < kSWin / 4; ++q) {
+      const float4 v = *reinterpret_cast<const float4 *>(Ys + kSO * tid + 4 * q);
+      win[4 * q] = v.x;
+      win[4 * q + 1] = v.y;
+      win[4 * q + 2] = v.z;
+      win[4 * q + 3] = v.w;
+    }
+    const bool valid = cs + kSO * tid < a.ntime_out;  // ntime_out % kSO == 0
+    float acc[kSO];
+    auto emit = [&](int b) {
+      if (valid) {
+        float4 *dst = reinterpret_cast<float4 *>(B.boxes + ((size_t)(b - a.w0) * h + r) * a.ntime_out + cs +
+                                                 kSO * tid);
+        dst[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        dst[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+#pragma unroll
+        for (int i = 0; i < kSO; ++i) mx[b] = fmaxf(mx[b], acc[i]);
+      }
+      float4 *o = reinterpret_cast<float4 *>(out_s + b * kSC + kSO * tid);
+      o[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      o[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+    };
+    if (bw0 <= 0 && 0 < bw1) { firS_width<1, ANCHOR>(win, taps + 0 * kSTap, acc); emit(0); }
+    if (bw0 <= 1 && 1 < bw1) { firS_width<2, ANCHOR>(win, taps + 1 * kSTap, acc); emit(1); }
+    if (bw0 <= 2 && 2 < bw1) { firS_width<4, ANCHOR>(win, taps + 2 * kSTap, acc); emit(2); }
+    if (bw0 <= 3 && 3 < bw1) { firS_width<8, ANCHOR>(win, taps + 3 * kSTap, acc); emit(3); }
+    if (bw0 <= 4 && 4 < bw1) { firS_width<16, ANCHOR>(win, taps + 4 * kSTap, acc); emit(4); }
+    if (bw0 <= 5 && 5 < bw1) { firS_width<32, ANCHOR>(win, taps + 5 * kSTap, acc); emit(5); }
+    __syncthreads();
+    // row-mean partials in the reference's order: owner jo adds columns jo, jo + 256, ...
+    const int c0 = cs + tid;
+    const int nm = c0 < nwcol ? min(kSC / 256, (nwcol - c0 + 255) >> 8) : 0;
+    for (int b = bw0; b < bw1; ++b) {
+      float ps = part_s[b * 256 + tid];
+#pragma unroll
+      for (int m = 0; m < kSC / 256; ++m)
+        if (m < nm) ps = __fadd_rn(ps, out_s[b * kSC + tid + 256 * m]);
+      part_s[b * 256 + tid] = ps;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < kSW; ++b)
+    if (b >= bw0 && b < bw1) out_s[b * 256 + tid] = mx[b];
+  __syncthreads();
+  for (int b = bw0 + (tid >> 5); b < bw1; b += kST / 32) {
+    const float tot = block256_tree(part_s + b * 256);
+    float m = -INFINITY;
+    for (int i = threadIdx.x & 31; i < kST; i += 32) m = fmaxf(m, out_s[b * 256 + i]);
+    for (int o = 16; o > 0; o /= 2) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((tid & 31) == 0) {
+      B.rowmean[(size_t)b * h + r] = __fdiv_rn(tot, (float)nwcol);
+      B.rowmax[(size_t)b * h + r] = m;
+    }
+  }
+}
+
 // Sequential sum of v[0..n) in index order (the reference's host loop),
 // in thread 0 of a kFin-thread block: the block stages kFinChunk values at
 // a time in shared memory with coalesced loads, thread 0 adds them.
@@ -673,6 +821,15 @@ cudaError_t launch_firR(const SmoothArgs &a, cudaStream_t s) {
 
 cudaError_t smooth_planes(const SmoothArgs &a0, cudaStream_t s) {
   if (a0.nrows <= 0 || a0.nw <= 0) return cudaSuccess;
+  if (a0.wmin == 1 && a0.wmax <= kSSpan && a0.nbox <= kSW && a0.w0 + a0.nw <= kSW && a0.ntime_out % kSO == 0) {
+    const size_t smem = sizeof(float) * ((size_t)kSY + kSW * kSC + kSW * 256 + kSW * kSTap);
+    auto kern = a0.anchor ? k_firS<1> : k_firS<0>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<a0.nrows, kST, smem, s>>>(a0);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   SmoothArgs a = a0;
   a.split = a.w0 + a.nw;
   const int M = a.ntime_out % kFirR == 0 ? fir_stride<kFirR>(2 * (a.wmin << (a.w0 + a.nw - 1))) : 0;

@@ -57,8 +57,20 @@ __device__ __forceinline__ long row_positions(const DedispArgs &a, int r) {
   return stride == kTileSamples ? (long)a.pair_rwords[r] : (long)(a.ntt - 1) * kTileSamples + stride;
 }
 
+// A row's metadata, all of it loaded together (one wait per row).
+struct BuildRow {
+  int w, z1, z2, z3, stride, words;
+  long long off;
+};
+
+__device__ __forceinline__ BuildRow build_row(const DedispArgs &a, int r, bool quad) {
+  const int4 in = a.pair_rinfo[r];
+  const int4 in2 = quad ? a.pair_rinfo2[r] : make_int4(-1, -1, 0, 0);
+  return BuildRow{in.w, in.z, in2.z, in2.w, a.pair_rtile[r], a.pair_rwords[r], a.pair_roff[r]};
+}
+
 template <int G>
-__global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
+__global__ void __launch_bounds__(256, 5) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
   constexpr int kBuildCH = build_chunk(G);
   const int k = blockIdx.y, z = blockIdx.z;  // group, beam of the launch
@@ -66,55 +78,87 @@ __global__ void __launch_bounds__(256) k_pair_build(DedispArgs a) {
   const DedispBeam bm = a.beams ? a.beams[z] : a.one;
   const int r0 = a.pair_prow[k];
   const int r1 = a.pair_rend ? a.pair_rend[(size_t)z * a.pair_npair + k] : a.pair_prow[k + 1];
+  // the group's channels and relative-delay ranges, loaded beside the chunk test's rows
+  const int4 i0 = a.pair_rinfo[r0], j0 = a.pair_rinfo2[r0];
+  int2 rr[kPairGMax];
+  rr[0] = make_int2(0, 0);
+#pragma unroll
+  for (int i = 1; i < kPairGMax; ++i) rr[i] = i < G ? a.pair_prange[k * (kPairGMax - 1) + i - 1] : make_int2(0, 0);
   int any = 0;  // does a row of the group cover a position of this chunk?
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int w = a.pair_rinfo[r].w;
     any |= P0 < (long)w + row_positions(a, r) && P0 + kBuildCH > (long)w;
   }
   if (!__syncthreads_or(any)) return;
-  const int4 i0 = a.pair_rinfo[r0], j0 = a.pair_rinfo2[r0];
   const int ch[kPairGMax] = {i0.x, i0.y, G == 4 ? j0.x : -1, G == 4 ? j0.y : -1};  // -1: fewer channels
   const long R = a.R;
   // channel i's words for positions [P0 + rmin_i, P0 + kBuildCH + rmax_i) at sm + off[i];
   // window position p lies at ring word (win0 + p) mod R
-  int off[kPairGMax] = {0, 0, 0, 0}, rmin[kPairGMax] = {0, 0, 0, 0};
+  int off[kPairGMax + 1], rmin[kPairGMax];
+  long base[kPairGMax];
   int nwin = 0;
-  for (int i = 0; i < G; ++i) {
-    const int2 rr = i == 0 ? make_int2(0, 0) : a.pair_prange[k * (kPairGMax - 1) + i - 1];
+#pragma unroll
+  for (int i = 0; i < kPairGMax; ++i) {
     off[i] = nwin;
-    rmin[i] = rr.x;
-    if (ch[i] < 0) continue;
-    const int n = kBuildCH + rr.y - rr.x;
-    const uint32_t *src = bm.packed + (size_t)ch[i] * R;
-    long base = (bm.win0 + P0 + rr.x) % R;
-    if (base < 0) base += R;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-      long pos = base + q;
-      if (pos >= R) pos %= R;
-      sm[nwin + q] = __byte_perm(src[pos], 0u, 0x4240);
+    rmin[i] = rr[i].x;
+    base[i] = 0;
+    if (i >= G || ch[i] < 0) continue;
+    long b = (bm.win0 + P0 + rr[i].x) % R;
+    base[i] = b < 0 ? b + R : b;
+    nwin += kBuildCH + rr[i].y - rr[i].x;
+  }
+  off[kPairGMax] = nwin;
+  // all the group's windows as one run of words, kLoads ring loads in flight per thread (a
+  // window word's channel: the last i with off[i] <= q; absent channels hold no words)
+  constexpr int kLoads = 8;
+  for (int q0 = threadIdx.x; q0 < nwin; q0 += kLoads * blockDim.x) {
+    uint32_t v[kLoads];
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < nwin) {
+        int i = 0;
+#pragma unroll
+        for (int j = 1; j < G; ++j) i += q >= off[j] ? 1 : 0;
+        const int c = i == 0 ? ch[0] : i == 1 ? ch[1] : i == 2 ? ch[2] : ch[3];
+        const long b = i == 0 ? base[0] : i == 1 ? base[1] : i == 2 ? base[2] : base[3];
+        const int o = i == 0 ? off[0] : i == 1 ? off[1] : i == 2 ? off[2] : off[3];
+        long pos = b + (q - o);
+        if (pos >= R) pos %= R;
+        v[u] = bm.packed[(size_t)c * R + pos];
+      }
     }
-    nwin += n;
+#pragma unroll
+    for (int u = 0; u < kLoads; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < nwin) sm[q] = __byte_perm(v[u], 0u, 0x4240);
+    }
   }
   __syncthreads();
-  // one warp per row: the row's metadata is loaded once for 2048-4096 words
-  const int lane = threadIdx.x & 31;
-  for (int r = r0 + (threadIdx.x >> 5); r < r1; r += blockDim.x >> 5) {
-    const int4 in = a.pair_rinfo[r];
-    if (P0 >= (long)in.w + row_positions(a, r) || P0 + kBuildCH <= (long)in.w) continue;
-    const int4 in2 = G == 4 ? a.pair_rinfo2[r] : make_int4(-1, -1, 0, 0);
-    uint32_t *dst = a.pair_rows + (size_t)z * a.pair_rows_stride + a.pair_roff[r];
+  // one warp per row: the row's metadata is loaded once for 2048-4096 words, the next row's
+  // while this one is written
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  int r = r0 + (threadIdx.x >> 5);
+  BuildRow nx{};
+  if (r < r1) nx = build_row(a, r, G == 4);
+  for (; r < r1; r += nwarp) {
+    const BuildRow in = nx;
+    if (r + nwarp < r1) nx = build_row(a, r + nwarp, G == 4);
+    const long npos = in.stride == kTileSamples ? (long)in.words : (long)(a.ntt - 1) * kTileSamples + in.stride;
+    if (P0 >= (long)in.w + npos || P0 + kBuildCH <= (long)in.w) continue;
+    uint32_t *dst = a.pair_rows + (size_t)z * a.pair_rows_stride + in.off;
     // word q of the chunk, q = p - P0, of channel i for this row's r_i
-    const int s1 = off[1] + in.z - rmin[1], s2 = off[2] + in2.z - rmin[2], s3 = off[3] + in2.w - rmin[3];
+    const int s1 = off[1] + in.z1 - rmin[1], s2 = off[2] + in.z2 - rmin[2], s3 = off[3] + in.z3 - rmin[3];
     // the row's tiles: tile tt holds positions [first + 1024 tt, + stride) at words tt * stride on
     // (one run from word 0 when stride = 1024)
-    const int stride = a.pair_rtile[r];
+    const int stride = in.stride;
     const long rel0 = P0 - in.w;  // chunk start relative to the row's first position
     const int tt0 = (int)max(0L, rel0 / kTileSamples - 1);
     const int tt1 = (int)min((long)a.ntt - 1, (rel0 + kBuildCH) / kTileSamples);
     for (int tt = stride == kTileSamples ? 0 : tt0; tt <= (stride == kTileSamples ? 0 : tt1); ++tt) {
       // positions of this tile's words (the whole row for stride 1024), clipped to the chunk
       const long pb = (long)in.w + (long)tt * kTileSamples;
-      const long pe = stride == kTileSamples ? (long)in.w + a.pair_rwords[r] : pb + stride;
+      const long pe = stride == kTileSamples ? (long)in.w + in.words : pb + stride;
       const long lo = max(P0, pb), hi = min(P0 + kBuildCH, pe);
       if (lo >= hi) continue;
       const int first = (int)(lo - P0), last = (int)(hi - P0);

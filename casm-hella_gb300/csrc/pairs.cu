@@ -70,7 +70,7 @@ __device__ __forceinline__ BuildRow build_row(const DedispArgs &a, int r, bool q
 }
 
 template <int G>
-__global__ void __launch_bounds__(256, 5) k_pair_build(DedispArgs a) {
+__global__ void __launch_bounds__(256, G == 4 ? 5 : 6) k_pair_build(DedispArgs a) {
   extern __shared__ uint32_t sm[];
   constexpr int kBuildCH = build_chunk(G);
   const int k = blockIdx.y, z = blockIdx.z;  // group, beam of the launch

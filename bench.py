@@ -592,6 +592,7 @@ def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool 
         dist.barrier()
     w0 = time.perf_counter()
     bt.submit(host[gi % ngen].data_ptr())
+    first_submit_ms = 1e3 * (time.perf_counter() - w0)
     gi += 1
     for k in range(steps):
         if k + 1 < steps:
@@ -612,8 +613,12 @@ def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool 
     adds = float(sum(i.ndms * int(kill[b].sum()) * i.ntime_dd for b, i in enumerate(infos)))
     peak = 2 * hg.int_add_peak(local) / 1e12
     achieved = adds / (dd_ms / 1e3) / 1e12
+    dd_kernel = ("k_pair_build + k_pair_sum (add mode {m}: rows of channel {g}, beams in chunks of up to four "
+                 "per launch pair, timed together)".format(m=tune["add_mode"],
+                                                           g="quads" if tune["add_mode"] == 6 else "pairs")
+                 if tune["add_mode"] >= 5 else "k_dedisp (all beams, one launch)")
     roof = {"bound": "int32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tadd/s",
-            "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_dedisp (all beams, one launch)",
+            "frac": round(achieved / peak, 4), "traffic": None, "kernel": dd_kernel,
             "work_per_launch": f"sum over {NB} beams of trials x unkilled channels x {infos[0].ntime_dd} samples",
             "peak_source": "measured: register-only 32-bit add chains on all SMs (hella_int_add_peak) x2 lanes",
             "ms_per_launch": round(dd_ms, 3)}
@@ -638,6 +643,10 @@ def batched_leg(a, rank, world, local, dist, steps: int, warmup: int, cpu: bool 
                 "device_ms_p50": round(float(np.percentile(e2e_dev, 50)), 2),
                 "period_ms": round(1e3 * e2e_s / steps, 2),
                 "first_gulp_ms": round(1e3 * (polled[0] - w0), 2),
+                "first_gulp_device_ms": round(float(e2e_dev[0]), 2),
+                "first_submit_ms": round(first_submit_ms, 2),
+                "latency_ms_each": [round(1e3 * x, 1) for x in lat],
+                "device_ms_each": [round(float(x), 1) for x in e2e_dev],
                 "steady_period_ms_p50": round(float(np.percentile(steady, 50)), 2)},
         "gpu_launches": int(steps * 2 * bt.graph_kernels()),
         "roofline": roof,

@@ -6,13 +6,17 @@
 // dedisp_execute_adv, src/hella/src/dedisperse.cpp:17-48), computed in two
 // launches per window:
 //
-// k_pair_build: one block per (group, 4096 window positions).  The group's
-//   channels' packed words of the chunk (for channel i widened by the
-//   group's range of relative delays r_i) are read from the ring once into
-//   shared memory as 16-bit lanes (bytes 0 and 2 of a packed word are the
-//   samples p and p + 512), then every row of the group is written from
-//   them: row(r)[p] = x[c0][p] + sum_i x[c_i][p + r_i].  Reads are the ring
-//   once per group; writes the rows, coalesced.
+// k_pair_build: one block per (group, 4096 window positions for pairs, 2048
+//   for quads).  The group's channels' packed words of the chunk (for
+//   channel i widened by the group's range of relative delays r_i) are read
+//   from the ring once into shared memory as 16-bit lanes (bytes 0 and 2 of
+//   a packed word are the samples p and p + 512), eight loads in flight per
+//   thread, then one warp per row writes every row of the group from them:
+//   row(r)[p] = x[c0][p] + sum_i x[c_i][p + r_i], the next row's metadata
+//   loaded while a row is written.  Reads are the ring once per group;
+//   writes the rows, coalesced, with streaming stores.  A row keeps, tile
+//   by tile, only the words its trials read where those span less than a
+//   1024-sample tile.
 //
 // k_pair_sum: the persistent staging pipeline of k_dedisp (work item =
 //   16-trial tile x 1024 output samples, stages issued warp by warp with
